@@ -1,0 +1,217 @@
+"""clovers_gb300 -- the clovers render hot path on GB300 (sm_103a).
+
+A drop-in for the reference's render path (clovers-cli's ``draw_cpu::draw``
+and the scene it renders).  The names and argument meanings below mirror the
+reference:
+
+* :class:`GlobalOptions`, :class:`RenderOptions` -- clovers-cli/src/lib.rs:17-25,
+  clovers-cli/src/render.rs:16-49 (same fields, same defaults);
+* :func:`initialize` -- clovers-cli/src/json_scene.rs:12-27;
+* :func:`draw` -- clovers-cli/src/draw_cpu.rs:26-98, returning the
+  ``Vec<Xyz<E>>`` pixel buffer as a ``(height*width, 3)`` float32 array, row 0
+  at the top of the image;
+* :func:`render` -- clovers-cli/src/render.rs:81-183 (load, draw, write).
+
+All computation runs in ``libclovers_gb300.so`` (CUDA kernels for sm_103a);
+there is no CPU fallback.
+"""
+
+import ctypes
+import dataclasses
+import os
+from typing import List, Optional
+
+import numpy as np
+
+from . import _lib
+from ._lib import ClvError, check, lib
+
+__all__ = ["GlobalOptions", "RenderOptions", "Scene", "DeviceScene", "initialize", "draw", "render",
+           "raycast", "resolve_srgb", "ClvError"]
+
+
+@dataclasses.dataclass
+class GlobalOptions:
+    """clovers-cli/src/lib.rs:17-25"""
+    debug: bool = False
+    quiet: bool = False
+
+
+@dataclasses.dataclass
+class RenderOptions:
+    """clovers-cli/src/render.rs:16-49, same defaults; ``seed`` selects the random streams."""
+    input: str = ""
+    output: Optional[str] = None
+    width: int = 1024
+    height: int = 1024
+    samples: int = 64
+    max_depth: int = 64
+    mode: str = "path-tracing"
+    sampler: str = "random"
+    bvh: str = "sah"
+    formats: List[str] = dataclasses.field(default_factory=lambda: ["png"])
+    seed: int = 0
+
+
+def _bvh_code(bvh):
+    if bvh == "sah":
+        return _lib.CLV_BVH_SAH
+    if bvh == "lam":
+        return _lib.CLV_BVH_LAM
+    raise ValueError("unknown BVH algorithm %r" % bvh)
+
+
+class Scene:
+    """A scene flattened on the host (clovers::scenes::Scene equivalent)."""
+
+    def __init__(self, handle):
+        self._h = ctypes.c_void_p(handle)
+
+    @classmethod
+    def from_json(cls, path, width, height, bvh="sah"):
+        out = ctypes.c_void_p()
+        check(lib().clv_scene_load_json(os.fsencode(path), width, height, _bvh_code(bvh), ctypes.byref(out)))
+        return cls(out.value)
+
+    @classmethod
+    def from_json_text(cls, text, width, height, base_dir=".", bvh="sah"):
+        out = ctypes.c_void_p()
+        check(lib().clv_scene_load_json_text(text.encode(), os.fsencode(base_dir), width, height, _bvh_code(bvh),
+                                             ctypes.byref(out)))
+        return cls(out.value)
+
+    @classmethod
+    def from_mesh(cls, vertices, indices):
+        v = np.ascontiguousarray(vertices, dtype=np.float32).reshape(-1, 3)
+        i = np.ascontiguousarray(indices, dtype=np.uint32).reshape(-1, 3)
+        out = ctypes.c_void_p()
+        check(lib().clv_scene_from_mesh(v.ctypes.data, v.shape[0], i.ctypes.data, i.shape[0], ctypes.byref(out)))
+        return cls(out.value)
+
+    def info(self):
+        inf = _lib.SceneInfoC()
+        check(lib().clv_scene_info_get(self._h, ctypes.byref(inf)))
+        return {f: getattr(inf, f) for f, _ in _lib.SceneInfoC._fields_}
+
+    def upload(self):
+        return DeviceScene(self)
+
+    def close(self):
+        if self._h and self._h.value:
+            lib().clv_scene_free(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class DeviceScene:
+    """A scene resident in GPU memory."""
+
+    def __init__(self, scene):
+        out = ctypes.c_void_p()
+        check(lib().clv_scene_upload(scene._h, ctypes.byref(out)))
+        self._h = out
+        self.info = scene.info()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if self._h and self._h.value:
+            lib().clv_device_scene_free(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def status(self):
+        f = ctypes.c_uint32()
+        check(lib().clv_device_status(self._h, ctypes.byref(f)))
+        return f.value
+
+
+def render_opts(opts: RenderOptions, sample_offset=0, samples_per_thread=0):
+    if opts.sampler != "random":
+        raise ClvError(_lib.CLV_E_INVALID, "only the random sampler is supported")
+    if opts.mode not in _lib.MODES:
+        raise ValueError("unknown render mode %r" % opts.mode)
+    return _lib.RenderOptsC(opts.width, opts.height, opts.samples, opts.max_depth, _lib.MODES[opts.mode], 0,
+                            opts.seed, sample_offset, samples_per_thread)
+
+
+def initialize(path, bvh, width, height):
+    """json_scene::initialize: load + flatten + upload; returns a DeviceScene."""
+    return Scene.from_json(path, width, height, bvh).upload()
+
+
+def draw(global_options: GlobalOptions, render_options: RenderOptions, scene: DeviceScene, sampler=None,
+         stats=None):
+    """draw_cpu::draw: the (height*width, 3) float32 XYZ(E) pixel buffer, row 0 at the top."""
+    del global_options, sampler
+    o = render_opts(render_options)
+    out = np.empty((render_options.height * render_options.width, 3), dtype=np.float32)
+    st = _lib.StatsC()
+    check(lib().clv_render(scene.handle, ctypes.byref(o), out.ctypes.data, ctypes.byref(st)))
+    if stats is not None:
+        stats.update(gpu_ms=st.gpu_ms, samples=st.samples, device_errors=st.device_errors,
+                     kernel_launches=st.kernel_launches)
+    return out
+
+
+def raycast(scene: DeviceScene, rays, with_counts=False):
+    """Closest hits of rays (n, 8) = {ox,oy,oz,tmin,dx,dy,dz,tmax}: (prim_id u32, t f32[, nodes, tests])."""
+    r = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 8)
+    n = r.shape[0]
+    prim = np.empty(n, np.uint32)
+    t = np.empty(n, np.float32)
+    nodes = np.empty(n, np.uint32) if with_counts else None
+    tests = np.empty(n, np.uint32) if with_counts else None
+    check(lib().clv_raycast(scene.handle, r.ctypes.data, n, prim.ctypes.data, t.ctypes.data,
+                            nodes.ctypes.data if with_counts else None, tests.ctypes.data if with_counts else None))
+    return (prim, t, nodes, tests) if with_counts else (prim, t)
+
+
+def resolve_srgb(xyz, width, height):
+    """write.rs:39-44 colour conversion: XYZ(E) means -> sRGB u8, (height*width, 3)."""
+    x = np.ascontiguousarray(xyz, dtype=np.float32).reshape(-1, 3)
+    out = np.empty((width * height, 3), np.uint8)
+    check(lib().clv_resolve_srgb(x.ctypes.data, width, height, out.ctypes.data))
+    return out
+
+
+def render(global_options: GlobalOptions, render_options: RenderOptions):
+    """render.rs:81-183: load the scene, draw, write the requested formats."""
+    from .imageio import write_png, write_exr
+    import time
+
+    if not render_options.input.endswith(".json"):
+        raise ClvError(_lib.CLV_E_INVALID, "Unknown file type")
+    scene = initialize(render_options.input, render_options.bvh, render_options.width, render_options.height)
+    t0 = time.perf_counter()
+    pixels = draw(global_options, render_options, scene)
+    duration = time.perf_counter() - t0
+    if not global_options.quiet:
+        print("Finished render in %.3fs" % duration)
+    written = []
+    for fmt in render_options.formats:
+        target = (render_options.output or os.path.join("renders", str(int(time.time())))) + "." + fmt
+        os.makedirs(os.path.dirname(target) or ".", exist_ok=True)
+        if fmt == "png":
+            rgb = resolve_srgb(pixels, render_options.width, render_options.height)
+            write_png(target, rgb, render_options.width, render_options.height, render_options, duration)
+        elif fmt == "exr":
+            write_exr(target, pixels, render_options.width, render_options.height)
+        else:
+            raise ValueError("unknown format %r" % fmt)
+        written.append(target)
+        if not global_options.quiet:
+            print("Image saved to: %s" % target)
+    return written

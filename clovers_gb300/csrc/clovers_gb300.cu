@@ -1,0 +1,717 @@
+// Kernels and the C ABI (include/clovers_gpu.h) of the GB300 render path.
+//
+//  raycast_kernel  closest-hit ray casts (the parity path), one thread per ray
+//  render_kernel   path tracing: one thread per (pixel, chunk of samples);
+//                  camera ray -> trace (clovers-cli/src/trace.rs:21-122, as a
+//                  loop) -> film rule (draw_cpu.rs:131-142) -> f64 sums
+//  resolve_kernel  f64 film -> mean XYZ(E) -> sRGB u8 (write.rs:39-44)
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/clovers_gpu.h"
+#include "clv_device.cuh"
+#include "scene.hpp"
+#include "spectral.hpp"
+
+using namespace clvd;
+
+// ------------------------------------------------------------------ kernels --
+
+__global__ void __launch_bounds__(128) raycast_kernel(ClvDeviceScene S, const float4* __restrict__ rays, uint64_t n,
+                                                      uint32_t* __restrict__ prim, float* __restrict__ tout,
+                                                      uint32_t* __restrict__ nodes, uint32_t* __restrict__ tests,
+                                                      uint32_t* err) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const float4 a = __ldcs(rays + 2 * i), b = __ldcs(rays + 2 * i + 1);
+    Ray r{mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), 0.0f, 600};
+    Hit h;
+    Counters c{0u, 0u};
+    Rng rng;
+    rng.init(0, (uint32_t)i, 0);
+    const bool want = nodes != nullptr || tests != nullptr;
+    const bool any = closest_hit(S, r, a.w, b.w, &rng, h, want ? &c : nullptr, err);
+    __stcs(prim + i, any ? hit_gid(S, h.ref) : 0xFFFFFFFFu);
+    __stcs(tout + i, any ? h.t : 0.0f);
+    if (nodes) nodes[i] = c.nodes;
+    if (tests) tests[i] = c.prims;
+  }
+}
+
+struct RenderParams {
+  uint32_t width, height, spp, max_depth;
+  uint32_t sample_offset, spt, chunks;
+  uint32_t mode;
+  uint64_t seed;
+  uint64_t npix;
+};
+
+__device__ __forceinline__ void rotate_wavelength(int hero, int w[4]) {  // wavelength.rs:55-60
+#pragma unroll
+  for (int j = 0; j < 4; ++j) w[j] = 380 + (hero - 380 + j * 100) % 400;
+}
+
+// The camera ray of one sample (draw_cpu.rs:113-127, camera.rs:103-126).
+__device__ __forceinline__ Ray camera_ray(const ClvDeviceScene& S, const RenderParams& P, uint32_t x, uint32_t row,
+                                          uint32_t sample, Rng& rng) {
+  rng.init(P.seed, row * P.width + x, sample);
+  const float ox = rng.f32(), oy = rng.f32();
+  float lx, ly;
+  random_in_unit_disk(rng, lx, ly);
+  const float time = rng.f32();
+  const int lambda = random_wavelength(rng);
+  const uint32_t y = P.height - 1 - row;  // draw_cpu.rs:51: buffer row 0 is the top of the image
+  const float pu = ((float)x + ox) / (float)P.width;
+  const float pv = ((float)y + oy) / (float)P.height;
+  const ClvCamera& C = S.camera;
+  lx *= C.lens_radius;
+  ly *= C.lens_radius;
+  const V off = add(scl(lx, ld3(C.u)), scl(ly, ld3(C.v)));
+  const V dir = sub(sub(add(add(ld3(C.llc), scl(pu, ld3(C.horizontal))), scl(pv, ld3(C.vertical))), ld3(C.origin)), off);
+  return Ray{add(ld3(C.origin), off), unit(dir), time, lambda};
+}
+
+// trace() as a loop: the path throughput `beta` carries the products of the
+// recursion's attenuation factors.
+__device__ void trace_path(const ClvDeviceScene& S, Ray ray, uint32_t max_depth, Rng& rng, float p[4], uint32_t* err) {
+  const int hero = ray.lambda;
+  int waves[4];
+  rotate_wavelength(hero, waves);
+  float L[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+  float beta[4] = {1.0f, 1.0f, 1.0f, 1.0f};
+  for (uint32_t depth = 0;; ++depth) {
+    if (depth > max_depth) break;
+    Hit h;
+    if (!closest_hit(S, ray, CLV_EPS_ACNE, CLV_FLT_MAX, &rng, h, nullptr, err)) {
+#pragma unroll
+      for (int i = 0; i < 4; ++i) L[i] += beta[i] * spd_get(S, S.background_spd, waves[i]);
+      break;
+    }
+    Rec rec;
+    hit_record(S, ray, h, rec);
+    const ClvMaterial& m = S.materials[rec.mat];
+    const uint32_t kind = m.kind;
+    if (kind == CLV_MAT_DIFFUSELIGHT || kind == CLV_MAT_CONELIGHT) {  // no scatter: emitted only
+#pragma unroll
+      for (int i = 0; i < 4; ++i) L[i] += beta[i] * mat_emit(S, m, ray, waves[i], rec);
+      break;
+    }
+    // emission of the remaining kinds is 0 and adds nothing
+    Ray next;
+    next.time = ray.time;
+    next.lambda = ray.lambda;
+    next.o = rec.p;
+    bool specular = true;
+    float spdf = 0.0f, mis = 1.0f;
+    if (kind == CLV_MAT_METAL) {  // metal.rs:27-51
+      const V refl = reflect(ray.d, rec.n);
+      next.d = unit(add(refl, scl(m.fuzz, random_unit_vector(rng))));
+    } else if (kind == CLV_MAT_DIELECTRIC || kind == CLV_MAT_DISPERSIVE) {  // dielectric.rs / dispersive.rs
+      const float ri = kind == CLV_MAT_DIELECTRIC ? m.refractive_index : dispersive_index(m, ray.lambda);
+      const float ratio = rec.front ? 1.0f / ri : ri;
+      const float ct = fminf(-dot(ray.d, rec.n), 1.0f);
+      const float st = sqrtf(1.0f - ct * ct);
+      if (ratio * st > 1.0f) {
+        next.d = reflect(ray.d, rec.n);
+      } else {
+        const float rp = schlick(ct, ratio);
+        next.d = rng.f32() < rp ? reflect(ray.d, rec.n) : refract(ray.d, rec.n, ratio);
+      }
+    } else {  // Lambertian (CosinePDF) or Isotropic (SpherePDF): MixturePDF with the light tree
+      specular = false;
+      const bool lamb = kind == CLV_MAT_LAMBERTIAN;
+      V gen;
+      if (rng.boolean()) {
+        gen = mis_random(S, rec.p, rng);
+      } else if (lamb) {  // CosinePDF::generate: ONB::build_from_w(normal).local(cosine dir)
+        const V w = rec.n;
+        const V a = fabsf(w.x) > 0.9f ? unit(mk(0.0f, 1.0f, 0.0f)) : unit(mk(1.0f, 0.0f, 0.0f));
+        const V vv = unit(cross(w, a));
+        const V uu = unit(cross(w, vv));
+        const V c = random_cosine_direction(rng);
+        gen = unit(add(add(scl(c.x, uu), scl(c.y, vv)), scl(c.z, w)));
+      } else {
+        gen = random_unit_vector(rng);
+      }
+      next.d = unit(gen);
+      const float light_v = mis_pdf(S, rec.p, next.d, hero, ray.time, err);
+      float bsdf_v;
+      if (lamb) {
+        const float cosine = dot(unit(next.d), rec.n);
+        bsdf_v = cosine <= 0.0f ? 0.0f : cosine / CLV_PI;
+      } else {
+        bsdf_v = 1.0f / (4.0f * CLV_PI);
+      }
+      mis = 0.5f * light_v + 0.5f * bsdf_v;
+      if (lamb) {  // Lambertian::scattering_pdf: None below the surface
+        const float c = dot(rec.n, unit(next.d));
+        if (c < 0.0f) break;
+        spdf = c / CLV_PI;
+      } else {
+        spdf = 1.0f / (4.0f * CLV_PI);
+      }
+    }
+    // attenuation: hero only on wavelength-dependent materials (trace.rs:61-70)
+    float atten[4];
+    if (m.wavelength_dependent) {
+      atten[0] = mat_color(S, m, ray, hero, rec);
+      atten[1] = atten[2] = atten[3] = 0.0f;
+    } else {
+#pragma unroll
+      for (int i = 0; i < 4; ++i) atten[i] = mat_color(S, m, ray, waves[i], rec);
+    }
+    if (specular) {
+#pragma unroll
+      for (int i = 0; i < 4; ++i) beta[i] = beta[i] * atten[i];
+    } else {
+#pragma unroll
+      for (int i = 0; i < 4; ++i) beta[i] = beta[i] * (atten[i] * spdf / mis);
+    }
+    ray = next;
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) p[i] = L[i];
+}
+
+__device__ __forceinline__ bool is_normal_pos(float v) {
+  const float a = fabsf(v);
+  return v > 0.0f && a >= 1.17549435e-38f && a <= 3.40282347e+38f;
+}
+
+__global__ void __launch_bounds__(128) render_kernel(ClvDeviceScene S, RenderParams P, double* __restrict__ film,
+                                                     uint32_t* err) {
+  const uint64_t total = P.npix * (uint64_t)P.chunks;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; tid < total; tid += stride) {
+    const uint64_t pix = tid % P.npix;
+    const uint32_t chunk = (uint32_t)(tid / P.npix);
+    const uint32_t x = (uint32_t)(pix % P.width), row = (uint32_t)(pix / P.width);
+    const uint32_t s0 = chunk * P.spt, s1 = min(P.spp, s0 + P.spt);
+    double acc0 = 0.0, acc1 = 0.0, acc2 = 0.0;
+    for (uint32_t s = s0; s < s1; ++s) {
+      Rng rng;
+      const Ray ray = camera_ray(S, P, x, row, s + P.sample_offset, rng);
+      int waves[4];
+      rotate_wavelength(ray.lambda, waves);
+      float p[4];
+      trace_path(S, ray, P.max_depth, rng, p, err);
+      // film rule, draw_cpu.rs:131-142
+      if (p[1] == 0.0f && p[2] == 0.0f && p[3] == 0.0f) {
+        const float* c = S.cmf + 3 * (waves[0] - 380);
+        acc0 += (double)(__ldg(c) * p[0]);
+        acc1 += (double)(__ldg(c + 1) * p[0]);
+        acc2 += (double)(__ldg(c + 2) * p[0]);
+      } else {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          if (is_normal_pos(p[i])) {
+            const float* c = S.cmf + 3 * (waves[i] - 380);
+            acc0 += (double)(__ldg(c) * p[i] / 4.0f);
+            acc1 += (double)(__ldg(c + 1) * p[i] / 4.0f);
+            acc2 += (double)(__ldg(c + 2) * p[i] / 4.0f);
+          }
+        }
+      }
+    }
+    double* f = film + 3 * pix;
+    if (P.chunks == 1) {
+      f[0] += acc0;
+      f[1] += acc1;
+      f[2] += acc2;
+    } else {
+      atomicAdd(f, acc0);
+      atomicAdd(f + 1, acc1);
+      atomicAdd(f + 2, acc2);
+    }
+  }
+}
+
+// Debug render modes (draw_cpu.rs:148-207): one centred ray per pixel.
+__global__ void debug_kernel(ClvDeviceScene S, RenderParams P, double* __restrict__ film, uint32_t* err) {
+  const uint64_t pix = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (pix >= P.npix) return;
+  const uint32_t x = (uint32_t)(pix % P.width), row = (uint32_t)(pix / P.width);
+  const uint32_t y = P.height - 1 - row;
+  Rng rng;
+  rng.init(P.seed, (uint32_t)pix, P.sample_offset);
+  const int lambda = random_wavelength(rng);
+  const float time = rng.f32();
+  (void)time;
+  const ClvCamera& C = S.camera;
+  const float pu = (float)x / (float)P.width, pv = (float)y / (float)P.height;
+  const V dir = sub(add(add(ld3(C.llc), scl(pu, ld3(C.horizontal))), scl(pv, ld3(C.vertical))), ld3(C.origin));
+  Ray r{ld3(C.origin), unit(dir), 0.0f, lambda};
+  float rgb[3] = {0.0f, 0.0f, 0.0f};  // linear sRGB
+  Hit h;
+  Counters c{0u, 0u};
+  const bool any = closest_hit(S, r, CLV_EPS_ACNE, CLV_FLT_MAX, &rng, h, &c, err);
+  if (P.mode == CLV_MODE_NORMAL_MAP) {  // normals.rs:11-37
+    if (any) {
+      Rec rec;
+      hit_record(S, r, h, rec);
+      const V n = mk(-rec.n.x, rec.n.y, -rec.n.z);
+      rgb[0] = 0.5f + 0.5f * n.x;
+      rgb[1] = 0.5f + 0.5f * n.y;
+      rgb[2] = n.z < 0.0f ? 0.0f : n.z;
+    }
+  } else {  // debug_visualizations.rs:18-35 colour ramp
+    const uint32_t d = P.mode == CLV_MODE_BVH_TEST_COUNT ? c.nodes : c.prims;
+    if (d <= 255) { rgb[0] = rgb[1] = rgb[2] = (float)d / 255.0f; }
+    else if (d <= 511) { rgb[0] = 1.0f; rgb[1] = 1.0f; }
+    else if (d <= 1023) { rgb[0] = 1.0f; rgb[1] = 0.5f; }
+    else { rgb[0] = 1.0f; }
+  }
+  // store linear sRGB in the film; the host converts to XYZ(E) with the same matrices
+  double* f = film + 3 * pix;
+  f[0] += rgb[0];
+  f[1] += rgb[1];
+  f[2] += rgb[2];
+}
+
+struct ResolveParams {
+  double m[9];  // XYZ(E) -> linear sRGB (D65)
+  double inv_spp;
+  uint32_t width, height;
+};
+__global__ void resolve_kernel(ResolveParams R, const double* __restrict__ film, float* __restrict__ xyz,
+                               uint8_t* __restrict__ rgb) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (uint64_t)R.width * R.height) return;
+  float c[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) c[k] = (float)(film[3 * i + k] * R.inv_spp);
+  if (xyz) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) xyz[3 * i + k] = c[k];
+  }
+  if (rgb) {
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      const float lin = (float)(R.m[r * 3] * (double)c[0] + R.m[r * 3 + 1] * (double)c[1] + R.m[r * 3 + 2] * (double)c[2]);
+      const float e = lin <= 0.0031308f ? lin * 12.92f : 1.055f * powf(lin, 1.0f / 2.4f) - 0.055f;
+      float v = roundf(e * 255.0f);
+      if (!(v > 0.0f)) v = 0.0f;
+      if (v > 255.0f) v = 255.0f;
+      rgb[3 * i + r] = (uint8_t)v;
+    }
+  }
+}
+
+// --------------------------------------------------------------- host side --
+
+namespace {
+
+thread_local std::string g_error;
+
+int fail(int code, const std::string& msg) {
+  g_error = msg;
+  return code;
+}
+
+struct CudaError : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+void ck(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) throw CudaError(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+template <class T>
+T* upload(const std::vector<T>& v, std::vector<void*>& owned) {
+  if (v.empty()) return nullptr;
+  void* p = nullptr;
+  ck(cudaMalloc(&p, v.size() * sizeof(T)), "cudaMalloc");
+  owned.push_back(p);
+  ck(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice), "cudaMemcpy H2D");
+  return static_cast<T*>(p);
+}
+
+int sm_count() {
+  static int n = 0;
+  if (n == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 1;
+  }
+  return n;
+}
+
+}  // namespace
+
+struct clv_scene {
+  clv::HostScene host;
+};
+
+struct clv_device_scene {
+  ClvDeviceScene view{};
+  std::vector<void*> owned;
+  uint32_t* err = nullptr;  // device error word
+  uint32_t width = 0, height = 0;
+  bool has_camera = false;
+  // scratch reused by the host-buffer entry points
+  void* scratch = nullptr;
+  size_t scratch_bytes = 0;
+  ~clv_device_scene() {
+    for (void* p : owned) cudaFree(p);
+    if (err) cudaFree(err);
+    if (scratch) cudaFree(scratch);
+  }
+  void* ensure_scratch(size_t bytes) {
+    if (bytes > scratch_bytes) {
+      if (scratch) cudaFree(scratch);
+      scratch = nullptr;
+      scratch_bytes = 0;
+      ck(cudaMalloc(&scratch, bytes), "cudaMalloc scratch");
+      scratch_bytes = bytes;
+    }
+    return scratch;
+  }
+};
+
+static uint32_t launch_grid(uint64_t work, int block) {
+  const uint64_t want = (work + block - 1) / block;
+  const uint64_t cap = (uint64_t)sm_count() * 16;  // persistent-style grid-stride cap
+  return (uint32_t)std::max<uint64_t>(1, std::min(want, cap));
+}
+
+static int check_opts(const clv_device_scene* d, const clv_render_opts* o) {
+  if (!d || !o) return fail(CLV_E_INVALID, "null argument");
+  if (!d->has_camera) return fail(CLV_E_INVALID, "this scene has no camera (mesh scenes are for ray casts)");
+  if (o->width != d->width || o->height != d->height)
+    return fail(CLV_E_INVALID, "render size differs from the size the scene was loaded with (camera aspect)");
+  if (o->samples == 0) return fail(CLV_E_INVALID, "samples must be positive");
+  if (o->sampler != 0) return fail(CLV_E_INVALID, "only the random sampler is supported (blue-noise tables are absent)");
+  if (o->mode > CLV_MODE_PRIMITIVE_TEST_COUNT) return fail(CLV_E_INVALID, "unknown render mode");
+  if ((uint64_t)o->width * o->height > 0x1FFFFFFFull) return fail(CLV_E_INVALID, "image too large");
+  return CLV_OK;
+}
+
+static RenderParams make_params(const clv_render_opts* o) {
+  RenderParams P{};
+  P.width = o->width;
+  P.height = o->height;
+  P.spp = o->samples;
+  P.max_depth = o->max_depth;
+  P.sample_offset = o->sample_offset;
+  P.mode = o->mode;
+  P.seed = o->seed;
+  P.npix = (uint64_t)o->width * o->height;
+  uint32_t spt = o->samples_per_thread;
+  if (spt == 0) {
+    // enough threads to fill the GPU several times over, otherwise long chunks
+    const uint64_t target = (uint64_t)sm_count() * 2048 * 4;
+    const uint64_t chunks = std::max<uint64_t>(1, std::min<uint64_t>(o->samples, (target + P.npix - 1) / P.npix));
+    spt = (uint32_t)((o->samples + chunks - 1) / chunks);
+  }
+  P.spt = std::max<uint32_t>(1, std::min(spt, o->samples));
+  P.chunks = (o->samples + P.spt - 1) / P.spt;
+  return P;
+}
+
+extern "C" {
+
+const char* clv_last_error(void) { return g_error.c_str(); }
+const char* clv_version(void) { return "clovers_gb300 0.1 (sm_103a)"; }
+
+int clv_scene_load_json_text(const char* json, const char* base_dir, uint32_t width, uint32_t height, int bvh_alg,
+                             clv_scene** out) {
+  if (!json || !out) return fail(CLV_E_INVALID, "null argument");
+  if (bvh_alg != CLV_BVH_SAH) return fail(CLV_E_INVALID, "only the SAH BVH builder is supported");
+  try {
+    std::unique_ptr<clv_scene> s(new clv_scene());
+    s->host = clv::load_scene_text(json, width, height, base_dir ? base_dir : ".");
+    if (s->host.tree_depth > CLV_STACK) return fail(CLV_E_SCENE, "BVH deeper than the traversal stack");
+    if (s->host.mis_depth > CLV_MIS_STACK) return fail(CLV_E_SCENE, "MIS tree deeper than its evaluation stack");
+    *out = s.release();
+    return CLV_OK;
+  } catch (std::exception& e) {
+    return fail(CLV_E_SCENE, e.what());
+  }
+}
+
+int clv_scene_load_json(const char* path, uint32_t width, uint32_t height, int bvh_alg, clv_scene** out) {
+  if (!path || !out) return fail(CLV_E_INVALID, "null argument");
+  if (bvh_alg != CLV_BVH_SAH) return fail(CLV_E_INVALID, "only the SAH BVH builder is supported");
+  try {
+    std::unique_ptr<clv_scene> s(new clv_scene());
+    s->host = clv::load_scene_json(path, width, height);
+    if (s->host.tree_depth > CLV_STACK) return fail(CLV_E_SCENE, "BVH deeper than the traversal stack");
+    if (s->host.mis_depth > CLV_MIS_STACK) return fail(CLV_E_SCENE, "MIS tree deeper than its evaluation stack");
+    *out = s.release();
+    return CLV_OK;
+  } catch (std::exception& e) {
+    return fail(CLV_E_SCENE, e.what());
+  }
+}
+
+int clv_scene_from_mesh(const float* verts, uint32_t nverts, const uint32_t* indices, uint32_t ntris,
+                        clv_scene** out) {
+  if (!verts || !indices || !out) return fail(CLV_E_INVALID, "null argument");
+  try {
+    std::unique_ptr<clv_scene> s(new clv_scene());
+    s->host = clv::mesh_scene(verts, nverts, indices, ntris);
+    if (s->host.tree_depth > CLV_STACK) return fail(CLV_E_SCENE, "BVH deeper than the traversal stack");
+    *out = s.release();
+    return CLV_OK;
+  } catch (std::exception& e) {
+    return fail(CLV_E_SCENE, e.what());
+  }
+}
+
+int clv_scene_info_get(const clv_scene* s, clv_scene_info* out) {
+  if (!s || !out) return fail(CLV_E_INVALID, "null argument");
+  const clv::HostScene& h = s->host;
+  out->objects = h.object_count;
+  out->nodes = (uint32_t)h.nodes.size();
+  out->triangles = (uint32_t)h.tris.size();
+  out->quads = (uint32_t)h.quads.size();
+  out->spheres = (uint32_t)(h.spheres.size() / 4);
+  out->compound = (uint32_t)h.objs.size();
+  out->materials = (uint32_t)h.materials.size();
+  out->tree_depth = h.tree_depth;
+  out->mis_nodes = (uint32_t)h.mis_nodes.size();
+  out->width = h.width;
+  out->height = h.height;
+  return CLV_OK;
+}
+
+void clv_scene_free(clv_scene* s) { delete s; }
+
+int clv_scene_upload(const clv_scene* s, clv_device_scene** out) {
+  if (!s || !out) return fail(CLV_E_INVALID, "null argument");
+  try {
+    const clv::HostScene& h = s->host;
+    std::unique_ptr<clv_device_scene> d(new clv_device_scene());
+    ClvDeviceScene& v = d->view;
+    auto& o = d->owned;
+    v.nodes = upload(h.nodes, o);
+    v.tris = upload(h.tris, o);
+    v.quads = upload(h.quads, o);
+    v.spheres = upload(h.spheres, o);
+    v.objs = upload(h.objs, o);
+    v.obj_children = upload(h.obj_children, o);
+    v.tri_gid = upload(h.tri_gid, o);
+    v.quad_gid = upload(h.quad_gid, o);
+    v.sphere_gid = upload(h.sphere_gid, o);
+    v.obj_gid = upload(h.obj_gid, o);
+    v.tri_mat = upload(h.tri_mat, o);
+    v.quad_mat = upload(h.quad_mat, o);
+    v.sphere_mat = upload(h.sphere_mat, o);
+    v.tri_area = upload(h.tri_area, o);
+    v.quad_area = upload(h.quad_area, o);
+    v.materials = upload(h.materials, o);
+    v.spd = upload(h.spd, o);
+    std::vector<float> ill((size_t)clv_tables::kNumIlluminants * 400);
+    std::memcpy(ill.data(), clv_tables::kIlluminants, ill.size() * sizeof(float));
+    v.illuminant = upload(ill, o);
+    std::vector<float> cmf(400 * 3);
+    for (int i = 0; i < 400; ++i) clv::wavelength_to_xyz(380 + i, &cmf[3 * i]);
+    v.cmf = upload(cmf, o);
+    v.mis_nodes = upload(h.mis_nodes, o);
+    v.root = h.root;
+    v.mis_root = h.mis_root;
+    std::memcpy(v.root_box, h.root_box, sizeof v.root_box);
+    v.background_spd = h.background_spd;
+    v.n_nodes = (uint32_t)h.nodes.size();
+    v.n_tris = (uint32_t)h.tris.size();
+    v.n_quads = (uint32_t)h.quads.size();
+    v.n_spheres = (uint32_t)(h.spheres.size() / 4);
+    v.n_objs = (uint32_t)h.objs.size();
+    v.n_materials = (uint32_t)h.materials.size();
+    v.max_depth_tree = h.tree_depth;
+    v.mis_depth = h.mis_depth;
+    v.camera = h.camera;
+    ck(cudaMalloc(&d->err, sizeof(uint32_t)), "cudaMalloc");
+    ck(cudaMemset(d->err, 0, sizeof(uint32_t)), "cudaMemset");
+    d->width = h.width;
+    d->height = h.height;
+    d->has_camera = h.width > 0 && h.mis_root != CLV_REF_EMPTY;
+    *out = d.release();
+    return CLV_OK;
+  } catch (std::exception& e) {
+    return fail(CLV_E_CUDA, e.what());
+  }
+}
+
+void clv_device_scene_free(clv_device_scene* d) { delete d; }
+
+int clv_device_status(clv_device_scene* d, uint32_t* flags_out) {
+  if (!d || !flags_out) return fail(CLV_E_INVALID, "null argument");
+  try {
+    ck(cudaMemcpy(flags_out, d->err, sizeof(uint32_t), cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
+    ck(cudaMemset(d->err, 0, sizeof(uint32_t)), "cudaMemset");
+    return CLV_OK;
+  } catch (std::exception& e) {
+    return fail(CLV_E_CUDA, e.what());
+  }
+}
+
+int clv_raycast_device(const clv_device_scene* d, const float* rays_dev, uint64_t n, uint32_t* prim_dev, float* t_dev,
+                       uint32_t* nodes_dev, uint32_t* tests_dev, void* stream) {
+  if (!d || (!rays_dev && n) || (!prim_dev && n) || (!t_dev && n)) return fail(CLV_E_INVALID, "null argument");
+  if (n == 0) return CLV_OK;
+  if ((reinterpret_cast<uintptr_t>(rays_dev) & 15u) != 0) return fail(CLV_E_INVALID, "rays must be 16-byte aligned");
+  const int block = 128;
+  raycast_kernel<<<launch_grid(n, block), block, 0, (cudaStream_t)stream>>>(
+      d->view, reinterpret_cast<const float4*>(rays_dev), n, prim_dev, t_dev, nodes_dev, tests_dev, d->err);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(CLV_E_CUDA, std::string("raycast launch: ") + cudaGetErrorString(e));
+  return CLV_OK;
+}
+
+int clv_raycast(clv_device_scene* d, const float* rays, uint64_t n, uint32_t* prim, float* t, uint32_t* nodes,
+                uint32_t* tests) {
+  if (!d || (!rays && n) || (!prim && n) || (!t && n)) return fail(CLV_E_INVALID, "null argument");
+  if (n == 0) return CLV_OK;
+  try {
+    const size_t rb = n * 32, ob = n * 4;
+    const size_t total = rb + 4 * ob;
+    char* base = static_cast<char*>(d->ensure_scratch(total));
+    float* drays = reinterpret_cast<float*>(base);
+    uint32_t* dprim = reinterpret_cast<uint32_t*>(base + rb);
+    float* dt = reinterpret_cast<float*>(base + rb + ob);
+    uint32_t* dnodes = nodes ? reinterpret_cast<uint32_t*>(base + rb + 2 * ob) : nullptr;
+    uint32_t* dtests = tests ? reinterpret_cast<uint32_t*>(base + rb + 3 * ob) : nullptr;
+    ck(cudaMemcpy(drays, rays, rb, cudaMemcpyHostToDevice), "cudaMemcpy H2D");
+    int rc = clv_raycast_device(d, drays, n, dprim, dt, dnodes, dtests, nullptr);
+    if (rc) return rc;
+    ck(cudaMemcpy(prim, dprim, ob, cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
+    ck(cudaMemcpy(t, dt, ob, cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
+    if (nodes) ck(cudaMemcpy(nodes, dnodes, ob, cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
+    if (tests) ck(cudaMemcpy(tests, dtests, ob, cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
+    uint32_t flags = 0;
+    ck(cudaMemcpy(&flags, d->err, 4, cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
+    if (flags) {
+      cudaMemset(d->err, 0, 4);
+      return fail(CLV_E_DEVICE, "kernel error flags " + std::to_string(flags));
+    }
+    return CLV_OK;
+  } catch (std::exception& e) {
+    return fail(CLV_E_CUDA, e.what());
+  }
+}
+
+int clv_render_device(clv_device_scene* d, const clv_render_opts* o, double* film_dev, void* stream) {
+  int rc = check_opts(d, o);
+  if (rc) return rc;
+  if (!film_dev) return fail(CLV_E_INVALID, "null film");
+  const RenderParams P = make_params(o);
+  const int block = 128;
+  if (o->mode == CLV_MODE_PATH_TRACING) {
+    render_kernel<<<launch_grid(P.npix * P.chunks, block), block, 0, (cudaStream_t)stream>>>(d->view, P, film_dev,
+                                                                                             d->err);
+  } else {
+    debug_kernel<<<(uint32_t)((P.npix + block - 1) / block), block, 0, (cudaStream_t)stream>>>(d->view, P, film_dev,
+                                                                                               d->err);
+  }
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(CLV_E_CUDA, std::string("render launch: ") + cudaGetErrorString(e));
+  return CLV_OK;
+}
+
+int clv_resolve_device(const double* film_dev, uint32_t width, uint32_t height, uint32_t spp, float* xyz_dev,
+                       uint8_t* rgb_dev, void* stream) {
+  if (!film_dev || spp == 0) return fail(CLV_E_INVALID, "bad argument");
+  ResolveParams R;
+  clv::m3_xyz_e_to_linsrgb(R.m);
+  R.inv_spp = 1.0 / (double)spp;
+  R.width = width;
+  R.height = height;
+  const uint64_t n = (uint64_t)width * height;
+  if (n == 0) return CLV_OK;
+  resolve_kernel<<<(uint32_t)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(R, film_dev, xyz_dev, rgb_dev);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(CLV_E_CUDA, std::string("resolve launch: ") + cudaGetErrorString(e));
+  return CLV_OK;
+}
+
+int clv_render(clv_device_scene* d, const clv_render_opts* o, float* xyz_out, clv_stats* stats) {
+  int rc = check_opts(d, o);
+  if (rc) return rc;
+  if (!xyz_out) return fail(CLV_E_INVALID, "null output");
+  try {
+    const uint64_t npix = (uint64_t)o->width * o->height;
+    const size_t film_b = npix * 3 * sizeof(double), xyz_b = npix * 3 * sizeof(float);
+    char* base = static_cast<char*>(d->ensure_scratch(film_b + xyz_b));
+    double* film = reinterpret_cast<double*>(base);
+    float* xyz = reinterpret_cast<float*>(base + film_b);
+    cudaEvent_t e0, e1;
+    ck(cudaEventCreate(&e0), "cudaEventCreate");
+    ck(cudaEventCreate(&e1), "cudaEventCreate");
+    ck(cudaMemsetAsync(film, 0, film_b, nullptr), "cudaMemset");
+    ck(cudaEventRecord(e0, nullptr), "cudaEventRecord");
+    rc = clv_render_device(d, o, film, nullptr);
+    if (rc) {
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      return rc;
+    }
+    ck(cudaEventRecord(e1, nullptr), "cudaEventRecord");
+    if (o->mode == CLV_MODE_PATH_TRACING) {
+      rc = clv_resolve_device(film, o->width, o->height, o->samples, xyz, nullptr, nullptr);
+      if (rc) return rc;
+      ck(cudaMemcpy(xyz_out, xyz, xyz_b, cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
+    } else {
+      // debug modes store linear sRGB; convert to XYZ(E) like LinSrgb::adapt_into
+      std::vector<double> tmp(npix * 3);
+      ck(cudaMemcpy(tmp.data(), film, film_b, cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
+      for (uint64_t i = 0; i < npix; ++i) {
+        const float lin[3] = {(float)tmp[3 * i], (float)tmp[3 * i + 1], (float)tmp[3 * i + 2]};
+        clv::linsrgb_to_xyz_e(lin, xyz_out + 3 * i);
+      }
+    }
+    float ms = 0.0f;
+    ck(cudaEventSynchronize(e1), "cudaEventSynchronize");
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    uint32_t flags = 0;
+    ck(cudaMemcpy(&flags, d->err, 4, cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
+    if (stats) {
+      stats->gpu_ms = ms;
+      stats->samples = npix * o->samples;
+      stats->device_errors = flags;
+      stats->kernel_launches = o->mode == CLV_MODE_PATH_TRACING ? 2 : 1;
+    }
+    if (flags) {
+      cudaMemset(d->err, 0, 4);
+      return fail(CLV_E_DEVICE, "kernel error flags " + std::to_string(flags));
+    }
+    return CLV_OK;
+  } catch (std::exception& e) {
+    return fail(CLV_E_CUDA, e.what());
+  }
+}
+
+int clv_resolve_srgb(const float* xyz, uint32_t width, uint32_t height, uint8_t* rgb) {
+  if (!xyz || !rgb) return fail(CLV_E_INVALID, "null argument");
+  try {
+    const uint64_t n = (uint64_t)width * height;
+    if (n == 0) return CLV_OK;
+    double* dfilm = nullptr;
+    uint8_t* drgb = nullptr;
+    ck(cudaMalloc(&dfilm, n * 3 * sizeof(double)), "cudaMalloc");
+    ck(cudaMalloc(&drgb, n * 3), "cudaMalloc");
+    std::vector<double> tmp(n * 3);
+    for (uint64_t i = 0; i < n * 3; ++i) tmp[i] = (double)xyz[i];
+    cudaMemcpy(dfilm, tmp.data(), n * 3 * sizeof(double), cudaMemcpyHostToDevice);
+    int rc = clv_resolve_device(dfilm, width, height, 1, nullptr, drgb, nullptr);
+    if (rc == CLV_OK) ck(cudaMemcpy(rgb, drgb, n * 3, cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
+    cudaFree(dfilm);
+    cudaFree(drgb);
+    return rc;
+  } catch (std::exception& e) {
+    return fail(CLV_E_CUDA, e.what());
+  }
+}
+
+}  // extern "C"

@@ -1,0 +1,759 @@
+// Device-side hot path of the clovers renderer on GB300 (sm_103a).
+//
+// Everything here follows the reference's f32 operation order (the file is
+// compiled with -fmad=false, so no multiply-add is fused) so that ray casts
+// return bit-identical hit ids and distances:
+//   * AABB::hit (reciprocal slabs) and AABB::distance (true divisions),
+//     clovers/src/aabb.rs:54-86 and 135-155;
+//   * BVHNode::hit's visiting order, clovers/src/bvh/hitable_trait.rs:15-81:
+//     own box first, both children's entry distances, nearer child first
+//     (left on ties), far child skipped when the near subtree's hit is closer
+//     than the far box's entry distance, the far child's hit preferred on
+//     equal distance;
+//   * Sphere/Quad/Triangle::hit, clovers/src/objects/{sphere,quad,triangle}.rs.
+// The recursion of the reference becomes an explicit per-thread stack whose
+// entries hold the deferred far child, its entry distance, its slab interval
+// (for its own-box test when it is popped) and the hit count at push time
+// (to know whether the near subtree produced a hit).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math_constants.h>
+#include <stdint.h>
+
+#include "device_types.h"
+
+namespace clvd {
+
+#define CLV_PI 3.14159265358979323846f
+#define CLV_EPS_ACNE 0.001f
+#define CLV_EPS_RECT 0.0001f
+#define CLV_EPS_MEDIUM 0.0001f
+#define CLV_FLT_MAX 3.40282347e+38f
+#define CLV_DEG2RAD (3.14159265358979323846f / 180.0f)
+#define CLV_STACK 64       // traversal stack entries (host rejects deeper trees)
+#define CLV_MIS_STACK 32   // MIS tree evaluation stack
+#define CLV_NEST 6         // wrapper nesting depth handled by the object interpreter
+
+// Device error flags (bitwise OR into a status word the host reads).
+#define CLV_ERR_STACK 1u
+#define CLV_ERR_NEST 2u
+#define CLV_ERR_MIS 4u
+
+// ------------------------------------------------------------------ vec3 --
+struct V {
+  float x, y, z;
+};
+__device__ __forceinline__ V mk(float x, float y, float z) { return V{x, y, z}; }
+__device__ __forceinline__ V add(V a, V b) { return mk(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ V sub(V a, V b) { return mk(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ V neg(V a) { return mk(-a.x, -a.y, -a.z); }
+__device__ __forceinline__ V scl(float s, V a) { return mk(s * a.x, s * a.y, s * a.z); }
+__device__ __forceinline__ V dvs(V a, float s) { return mk(a.x / s, a.y / s, a.z / s); }
+__device__ __forceinline__ float dot(V a, V b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ V cross(V a, V b) {
+  return mk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ float nsq(V a) { return dot(a, a); }
+__device__ __forceinline__ float len(V a) { return sqrtf(nsq(a)); }
+__device__ __forceinline__ V unit(V a) { return dvs(a, len(a)); }
+__device__ __forceinline__ float comp(V a, int i) { return i == 0 ? a.x : (i == 1 ? a.y : a.z); }
+__device__ __forceinline__ V ld3(const float* p) { return mk(p[0], p[1], p[2]); }
+__device__ __forceinline__ float rclamp(float x, float lo, float hi) { return x < lo ? lo : (x > hi ? hi : x); }
+
+struct Ray {
+  V o, d;
+  float time;
+  int lambda;
+};
+__device__ __forceinline__ V at(const Ray& r, float t) { return add(r.o, scl(t, r.d)); }
+
+// ------------------------------------------------------------------- rng --
+// Counter-based stream per (pixel, sample): SplitMix64 (Steele et al. 2014)
+// output function over key + k*gamma.  Conversions follow rand 0.9:
+// f32 = (u32 >> 8) * 2^-24, bool = sign bit.
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+struct Rng {
+  uint64_t key;
+  uint32_t counter;
+  __device__ void init(uint64_t seed, uint32_t pixel, uint32_t sample) {
+    key = mix64(mix64(seed) ^ (((uint64_t)pixel << 32) | (uint64_t)sample));
+    counter = 0;
+  }
+  __device__ __forceinline__ uint32_t u32() {
+    ++counter;
+    return (uint32_t)(mix64(key + (uint64_t)counter * 0x9E3779B97F4A7C15ull) >> 32);
+  }
+  __device__ __forceinline__ float f32() { return (float)(u32() >> 8) * 5.9604644775390625e-8f; }
+  __device__ __forceinline__ bool boolean() { return (int32_t)u32() < 0; }
+  __device__ __forceinline__ float sym() { return 2.0f * f32() - 1.0f; }
+};
+#define CLV_REJECT 64
+// Marsaglia 1972 point on the sphere (rand_distr UnitSphere)
+__device__ V random_unit_vector(Rng& r) {
+  for (int i = 0; i < CLV_REJECT; ++i) {
+    float x1 = r.sym(), x2 = r.sym();
+    float s = x1 * x1 + x2 * x2;
+    if (s >= 1.0f) continue;
+    float f = 2.0f * sqrtf(1.0f - s);
+    return unit(mk(x1 * f, x2 * f, 1.0f - 2.0f * s));
+  }
+  return mk(0.0f, 0.0f, 1.0f);
+}
+// rejection sampling in the unit disc (rand_distr UnitDisc)
+__device__ void random_in_unit_disk(Rng& r, float& ox, float& oy) {
+  for (int i = 0; i < CLV_REJECT; ++i) {
+    float x1 = r.sym(), x2 = r.sym();
+    if (x1 * x1 + x2 * x2 <= 1.0f) { ox = x1; oy = x2; return; }
+  }
+  ox = 0.0f; oy = 0.0f;
+}
+__device__ V random_cosine_direction(Rng& r) {  // clovers/src/random.rs:25-36
+  float r1 = r.f32();
+  float r2 = r.f32();
+  float z = sqrtf(1.0f - r2);
+  float phi = 2.0f * CLV_PI * r1;
+  float x = cosf(phi) * sqrtf(r2);
+  float y = sinf(phi) * sqrtf(r2);
+  return mk(x, y, z);
+}
+__device__ __forceinline__ int random_wavelength(Rng& r) {  // uniform integer in [380, 780)
+  return 380 + (int)(((uint64_t)r.u32() * 400ull) >> 32);
+}
+
+// ------------------------------------------------------------------ boxes --
+// Slab interval of AABB::hit for one box: the ray is inside for t in (N, F).
+__device__ __forceinline__ void slab(const float* b, V o, V inv, float& N, float& F) {
+  float n = -CLV_FLT_MAX * 2.0f, f = CLV_FLT_MAX * 2.0f;  // -inf / +inf
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    float t0 = (b[2 * a] - comp(o, a)) * comp(inv, a);
+    float t1 = (b[2 * a + 1] - comp(o, a)) * comp(inv, a);
+    float nn, ff;
+    if (t0 < t1) { nn = t0; ff = t1; } else { nn = t1; ff = t0; }
+    n = fmaxf(n, nn);  // NaN entries are skipped, as the reference's comparisons do
+    f = fminf(f, ff);
+  }
+  N = n;
+  F = f;
+}
+__device__ __forceinline__ bool slab_pass(float N, float F, float tmin, float tmax) {
+  return fminf(tmax, F) > fmaxf(tmin, N);
+}
+// AABB::distance: entry distance or false (None)
+__device__ __forceinline__ bool box_distance(const float* b, V o, V d, float& out) {
+  float tx1 = (b[0] - o.x) / d.x, tx2 = (b[1] - o.x) / d.x;
+  float tmin = fminf(tx1, tx2), tmax = fmaxf(tx1, tx2);
+  float ty1 = (b[2] - o.y) / d.y, ty2 = (b[3] - o.y) / d.y;
+  tmin = fmaxf(tmin, fminf(ty1, ty2));
+  tmax = fminf(tmax, fmaxf(ty1, ty2));
+  float tz1 = (b[4] - o.z) / d.z, tz2 = (b[5] - o.z) / d.z;
+  tmin = fmaxf(tmin, fminf(tz1, tz2));
+  tmax = fminf(tmax, fmaxf(tz1, tz2));
+  out = tmin;
+  return tmax >= tmin && tmax > 0.0f;
+}
+
+// ------------------------------------------------------------- primitives --
+// Full hit record (clovers/src/hitrecord.rs:7-33) plus the material id.
+struct Rec {
+  float t, u, v;
+  V p, n;
+  bool front;
+  uint32_t mat;
+};
+
+__device__ __forceinline__ void load_planar(const ClvPlanar* arr, uint32_t i, float f[16]) {
+  const float4* p = reinterpret_cast<const float4*>(arr + i);
+  float4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2), e = __ldg(p + 3);
+  f[0] = a.x; f[1] = a.y; f[2] = a.z; f[3] = a.w;
+  f[4] = b.x; f[5] = b.y; f[6] = b.z; f[7] = b.w;
+  f[8] = c.x; f[9] = c.y; f[10] = c.z; f[11] = c.w;
+  f[12] = e.x; f[13] = e.y; f[14] = e.z; f[15] = e.w;
+}
+// Quad::hit / Triangle::hit up to the inside test: distance t and plane coordinates.
+__device__ __forceinline__ bool planar_test(const float f[16], bool tri, const Ray& r, float tmin, float tmax,
+                                            float& t, float& alpha, float& beta) {
+  V q = mk(f[0], f[1], f[2]), u = mk(f[3], f[4], f[5]), v = mk(f[6], f[7], f[8]);
+  V n = mk(f[9], f[10], f[11]), w = mk(f[13], f[14], f[15]);
+  float d = f[12];
+  float denom = dot(n, r.d);
+  if (fabsf(denom) < CLV_EPS_RECT) return false;
+  t = (-d - dot(n, r.o)) / denom;
+  if (t < tmin || t > tmax) return false;
+  V ph = sub(at(r, t), q);
+  alpha = dot(w, cross(ph, v));
+  beta = dot(w, cross(u, ph));
+  bool in = (alpha >= 0.0f && alpha <= 1.0f) && (beta >= 0.0f && beta <= 1.0f);
+  if (tri) in = in && (alpha + beta <= 1.0f);
+  return in;
+}
+__device__ __forceinline__ void face(Rec& rec, const Ray& r, V outward) {
+  rec.front = dot(r.d, outward) < 0.0f;
+  rec.n = rec.front ? outward : neg(outward);
+}
+__device__ __forceinline__ void planar_record(const float f[16], const Ray& r, float t, float alpha, float beta,
+                                              Rec& rec) {
+  rec.t = t;
+  rec.p = at(r, t);
+  rec.u = alpha;
+  rec.v = beta;
+  face(rec, r, mk(f[9], f[10], f[11]));
+}
+// Sphere::hit: roots strictly inside (tmin, tmax)
+__device__ __forceinline__ bool sphere_test(float4 s, const Ray& r, float tmin, float tmax, float& t) {
+  V c = mk(s.x, s.y, s.z);
+  V oc = sub(r.o, c);
+  float a = nsq(r.d);
+  float hb = dot(oc, r.d);
+  float cc = nsq(oc) - s.w * s.w;
+  float disc = hb * hb - a * cc;
+  if (!(disc > 0.0f)) return false;
+  float root = sqrtf(disc);
+  float d0 = (-hb - root) / a;
+  if (d0 < tmax && d0 > tmin) { t = d0; return true; }
+  float d1 = (-hb + root) / a;
+  if (d1 < tmax && d1 > tmin) { t = d1; return true; }
+  return false;
+}
+__device__ __forceinline__ void sphere_record(V c, float radius, const Ray& r, float t, Rec& rec) {
+  rec.t = t;
+  rec.p = at(r, t);
+  V outward = unit(dvs(sub(rec.p, c), radius));
+  V tr = dvs(sub(rec.p, c), radius);  // get_uv, sphere.rs:58-65
+  float phi = atan2f(tr.z, tr.x);
+  float theta = asinf(tr.y);
+  rec.u = 1.0f - (phi + CLV_PI) / (2.0f * CLV_PI);
+  rec.v = (theta + CLV_PI / 2.0f) / CLV_PI;
+  face(rec, r, outward);
+}
+__device__ __forceinline__ float4 load_sphere(const ClvDeviceScene& S, uint32_t i) {
+  return __ldg(reinterpret_cast<const float4*>(S.spheres) + i);
+}
+
+// ----------------------------------------------- compound object interpreter --
+// Evaluates any ref (primitive or ClvObj) into a full record, recursing
+// through wrappers up to CLV_NEST levels (host validates the nesting).
+struct Counters {
+  uint32_t nodes, prims;
+};
+
+template <int LEVEL>
+struct ObjEval {
+  static __device__ bool hit(const ClvDeviceScene& S, uint32_t ref, const Ray& r, float tmin, float tmax, Rng* rng,
+                             Rec& rec, Counters* cnt, uint32_t* err);
+  static __device__ float pdf(const ClvDeviceScene& S, uint32_t ref, V origin, V dir, int lambda, float time);
+};
+template <>
+struct ObjEval<CLV_NEST> {
+  static __device__ bool hit(const ClvDeviceScene&, uint32_t, const Ray&, float, float, Rng*, Rec&, Counters*,
+                             uint32_t* err) {
+    if (err) atomicOr(err, CLV_ERR_NEST);
+    return false;
+  }
+  static __device__ float pdf(const ClvDeviceScene&, uint32_t, V, V, int, float) { return 0.0f; }
+};
+
+template <int LEVEL>
+__device__ __noinline__ bool ObjEval<LEVEL>::hit(const ClvDeviceScene& S, uint32_t ref, const Ray& r, float tmin, float tmax,
+                                    Rng* rng, Rec& rec, Counters* cnt, uint32_t* err) {
+  const uint32_t kind = CLV_REF_KIND(ref), idx = CLV_REF_INDEX(ref);
+  if (kind == CLV_REF_TRI || kind == CLV_REF_QUAD) {
+    if (cnt) cnt->prims++;
+    float f[16], t, a, b;
+    load_planar(kind == CLV_REF_TRI ? S.tris : S.quads, idx, f);
+    if (!planar_test(f, kind == CLV_REF_TRI, r, tmin, tmax, t, a, b)) return false;
+    planar_record(f, r, t, a, b, rec);
+    rec.mat = kind == CLV_REF_TRI ? S.tri_mat[idx] : S.quad_mat[idx];
+    return true;
+  }
+  if (kind == CLV_REF_SPHERE) {
+    if (cnt) cnt->prims++;
+    float4 s = load_sphere(S, idx);
+    float t;
+    if (!sphere_test(s, r, tmin, tmax, t)) return false;
+    sphere_record(mk(s.x, s.y, s.z), s.w, r, t, rec);
+    rec.mat = S.sphere_mat[idx];
+    return true;
+  }
+  if (kind != CLV_REF_OBJ) return false;
+  const ClvObj& o = S.objs[idx];
+  switch (o.kind) {
+    case CLV_OBJ_BOXY: {  // boxy.rs:76-94: closest of 6 quads, tmax narrowing
+      bool any = false;
+      float closest = tmax;
+      for (int k = 0; k < 6; ++k) {
+        Rec h;
+        if (ObjEval<LEVEL + 1>::hit(S, CLV_MAKE_REF(CLV_REF_QUAD, o.a + k), r, tmin, closest, rng, h, cnt, err)) {
+          closest = h.t;
+          rec = h;
+          any = true;
+        }
+      }
+      return any;
+    }
+    case CLV_OBJ_LIST: {  // hitable.rs:148-166: None as soon as one member misses
+      float best = CLV_FLT_MAX * 2.0f;
+      bool any = false;
+      for (uint32_t k = 0; k < o.b; ++k) {
+        Rec h;
+        if (!ObjEval<LEVEL + 1>::hit(S, S.obj_children[o.a + k], r, tmin, tmax, rng, h, cnt, err)) return false;
+        if (h.t < best) {
+          best = h.t;
+          rec = h;
+          any = true;
+        }
+      }
+      return any;
+    }
+    case CLV_OBJ_TRANSLATE: {  // translate.rs:41-78
+      V off = mk(o.p[0], o.p[1], o.p[2]);
+      Ray moved{sub(r.o, off), r.d, r.time, r.lambda};
+      Rec h;
+      if (!ObjEval<LEVEL + 1>::hit(S, o.a, moved, tmin, tmax, rng, h, cnt, err)) return false;
+      rec = h;
+      rec.p = add(h.p, off);
+      face(rec, moved, h.n);
+      return true;
+    }
+    case CLV_OBJ_ROTATEY: {  // rotate.rs:82-159
+      float s = o.p[0], c = o.p[1];
+      V ro = r.o, rd = r.d;
+      ro.x = c * r.o.x - s * r.o.z;
+      ro.z = s * r.o.x + c * r.o.z;
+      rd.x = c * r.d.x - s * r.d.z;
+      rd.z = s * r.d.x + c * r.d.z;
+      Ray rr{ro, unit(rd), r.time, r.lambda};
+      Rec h;
+      if (!ObjEval<LEVEL + 1>::hit(S, o.a, rr, tmin, tmax, rng, h, cnt, err)) return false;
+      V p = h.p, n = h.n;
+      p.x = c * h.p.x + s * h.p.z;
+      p.z = -s * h.p.x + c * h.p.z;
+      n.x = c * h.n.x + s * h.n.z;
+      n.z = -s * h.n.x + c * h.n.z;
+      rec = h;
+      rec.p = p;
+      face(rec, rr, unit(n));
+      return true;
+    }
+    case CLV_OBJ_MEDIUM: {  // constant_medium.rs:65-126
+      Rec r1, r2;
+      const float inf = CLV_FLT_MAX * 2.0f;
+      if (!ObjEval<LEVEL + 1>::hit(S, o.a, r, -inf, inf, rng, r1, cnt, err)) return false;
+      if (!ObjEval<LEVEL + 1>::hit(S, o.a, r, r1.t + CLV_EPS_MEDIUM, inf, rng, r2, cnt, err)) return false;
+      if (r1.t < tmin) r1.t = tmin;
+      if (r2.t > tmax) r2.t = tmax;
+      if (r1.t >= r2.t) return false;
+      if (r1.t < 0.0f) r1.t = 0.0f;
+      float rl = len(r.d);
+      float inside = (r2.t - r1.t) * rl;
+      float hd = o.p[0] * logf(rng->f32());
+      if (hd > inside) return false;
+      rec.t = r1.t + hd / rl;
+      rec.p = at(r, rec.t);
+      rec.n = random_unit_vector(*rng);
+      rec.front = true;
+      rec.u = r1.u;
+      rec.v = r1.v;
+      rec.mat = o.b;
+      return true;
+    }
+    case CLV_OBJ_MOVING: {  // moving_sphere.rs:104-160
+      if (cnt) cnt->prims++;
+      V c0 = mk(o.p[0], o.p[1], o.p[2]), c1 = mk(o.p[3], o.p[4], o.p[5]);
+      float t0 = o.p[6], t1 = o.p[7], radius = o.p[8];
+      V c = add(c0, scl((r.time - t0) / (t1 - t0), sub(c1, c0)));
+      float t;
+      if (!sphere_test(make_float4(c.x, c.y, c.z, radius), r, tmin, tmax, t)) return false;
+      sphere_record(c, radius, r, t, rec);
+      rec.mat = o.b;
+      return true;
+    }
+  }
+  return false;
+}
+
+// pdf_value of one MIS leaf object (HitableTrait::pdf_value of each type).
+__device__ __forceinline__ float planar_pdf(const ClvDeviceScene& S, bool tri, uint32_t idx, V origin, V dir) {
+  float f[16], t, a, b;
+  load_planar(tri ? S.tris : S.quads, idx, f);
+  Ray r{origin, dir, 0.0f, 0};
+  if (!planar_test(f, tri, r, CLV_EPS_ACNE, CLV_FLT_MAX * 2.0f, t, a, b)) return 0.0f;
+  Rec rec;
+  planar_record(f, r, t, a, b, rec);
+  float dist2 = t * t * nsq(dir);
+  float cosine = fabsf(dot(dir, rec.n)) / len(dir);
+  return dist2 / (cosine * (tri ? S.tri_area[idx] : S.quad_area[idx]));
+}
+__device__ __forceinline__ float sphere_pdf(float4 s, V origin, V dir) {
+  Ray r{origin, dir, 0.0f, 0};
+  float t;
+  if (!sphere_test(s, r, CLV_EPS_ACNE, CLV_FLT_MAX * 2.0f, t)) return 0.0f;
+  V c = mk(s.x, s.y, s.z);
+  float ctm = sqrtf(1.0f - s.w * s.w / nsq(sub(c, origin)));
+  float sa = 2.0f * CLV_PI * (1.0f - ctm);
+  return 1.0f / sa;
+}
+template <int LEVEL>
+__device__ __noinline__ float ObjEval<LEVEL>::pdf(const ClvDeviceScene& S, uint32_t ref, V origin, V dir, int lambda, float time) {
+  const uint32_t kind = CLV_REF_KIND(ref), idx = CLV_REF_INDEX(ref);
+  if (kind == CLV_REF_TRI || kind == CLV_REF_QUAD) return planar_pdf(S, kind == CLV_REF_TRI, idx, origin, dir);
+  if (kind == CLV_REF_SPHERE) return sphere_pdf(load_sphere(S, idx), origin, dir);
+  if (kind != CLV_REF_OBJ) return 0.0f;
+  const ClvObj& o = S.objs[idx];
+  switch (o.kind) {
+    case CLV_OBJ_BOXY: {  // boxy.rs:113-128
+      float sum = 0.0f;
+      for (int k = 0; k < 6; ++k) sum += planar_pdf(S, false, o.a + k, origin, dir) / 6.0f;
+      return sum;
+    }
+    case CLV_OBJ_TRANSLATE:  // translate.rs:81-98 (adds the offset)
+      return ObjEval<LEVEL + 1>::pdf(S, o.a, add(origin, mk(o.p[0], o.p[1], o.p[2])), dir, lambda, time);
+    case CLV_OBJ_MEDIUM:
+      return ObjEval<LEVEL + 1>::pdf(S, o.a, origin, dir, lambda, time);
+    default:  // RotateY, MovingSphere, HitableList: 0
+      return 0.0f;
+  }
+}
+
+// ------------------------------------------------------------- traversal --
+// Closest-hit state.  For triangles/quads/spheres only (t, ref, u, v) are kept
+// and the full record is rebuilt afterwards (deterministic); compound objects
+// keep their full record since media consume randomness.
+struct Hit {
+  float t;
+  uint32_t ref;  // leaf ref that produced the hit, CLV_REF_EMPTY if none
+  float a, b;    // plane coordinates (triangle / quad)
+  Rec full;      // compound objects only
+};
+
+struct StackEntry {
+  uint32_t ref;
+  uint32_t hits;
+  float far_d, N, F;
+};
+
+// Tests one BVH leaf with the current tmax; on acceptance updates hit/tmax.
+__device__ __forceinline__ bool leaf_test(const ClvDeviceScene& S, uint32_t ref, const Ray& r, float tmin,
+                                          float tmax, Rng* rng, Hit& hit, Counters* cnt, uint32_t* err) {
+  const uint32_t kind = CLV_REF_KIND(ref), idx = CLV_REF_INDEX(ref);
+  if (kind == CLV_REF_TRI || kind == CLV_REF_QUAD) {
+    if (cnt) cnt->prims++;
+    float f[16], t, a, b;
+    load_planar(kind == CLV_REF_TRI ? S.tris : S.quads, idx, f);
+    if (!planar_test(f, kind == CLV_REF_TRI, r, tmin, tmax, t, a, b)) return false;
+    hit.t = t;
+    hit.ref = ref;
+    hit.a = a;
+    hit.b = b;
+    return true;
+  }
+  if (kind == CLV_REF_SPHERE) {
+    if (cnt) cnt->prims++;
+    float t;
+    if (!sphere_test(load_sphere(S, idx), r, tmin, tmax, t)) return false;
+    hit.t = t;
+    hit.ref = ref;
+    return true;
+  }
+  Rec rec;
+  if (!ObjEval<0>::hit(S, ref, r, tmin, tmax, rng, rec, cnt, err)) return false;
+  hit.t = rec.t;
+  hit.ref = ref;
+  hit.full = rec;
+  return true;
+}
+
+// BVHNode::hit over the flattened tree.  Returns true with `hit` filled.
+__device__ bool closest_hit(const ClvDeviceScene& S, const Ray& r, float tmin, float tmax, Rng* rng, Hit& hit,
+                            Counters* cnt, uint32_t* err) {
+  hit.ref = CLV_REF_EMPTY;
+  const V inv = mk(1.0f / r.d.x, 1.0f / r.d.y, 1.0f / r.d.z);
+  uint32_t hits = 0;
+  StackEntry stack[CLV_STACK];
+  int sp = 0;
+  uint32_t cur = S.root;
+  {  // the root is always a node (BVHNode::from_list)
+    if (cnt) cnt->nodes++;
+    float N, F;
+    slab(S.root_box, r.o, inv, N, F);
+    if (!slab_pass(N, F, tmin, tmax)) return false;
+  }
+  while (true) {
+    // `cur` is a node whose own box test passed
+    const ClvNode* np = S.nodes + CLV_REF_INDEX(cur);
+    const float4* p4 = reinterpret_cast<const float4*>(np);
+    const float4 q0 = __ldg(p4), q1 = __ldg(p4 + 1), q2 = __ldg(p4 + 2), q3 = __ldg(p4 + 3);
+    const float lb[6] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y};
+    const float rb[6] = {q1.z, q1.w, q2.x, q2.y, q2.z, q2.w};
+    const uint32_t L = __float_as_uint(q3.x), R = __float_as_uint(q3.y);
+    uint32_t next = CLV_REF_EMPTY;
+    const float* nbox = nullptr;
+    if (L != CLV_REF_EMPTY && R != CLV_REF_EMPTY) {
+      float ld, rd;
+      const bool lh = box_distance(lb, r.o, r.d, ld), rh = box_distance(rb, r.o, r.d, rd);
+      if (lh && rh) {
+        const float far_d = fmaxf(ld, rd);
+        const bool left_first = ld < rd;
+        next = left_first ? L : R;
+        nbox = left_first ? lb : rb;
+        const uint32_t far = left_first ? R : L;
+        const float* fbox = left_first ? rb : lb;
+        if (sp >= CLV_STACK) {
+          if (err) atomicOr(err, CLV_ERR_STACK);
+          return hit.ref != CLV_REF_EMPTY;
+        }
+        StackEntry& e = stack[sp++];
+        e.ref = far;
+        e.hits = hits;
+        e.far_d = far_d;
+        if (CLV_REF_KIND(far) == CLV_REF_NODE) slab(fbox, r.o, inv, e.N, e.F);
+      } else if (lh) {
+        next = L;
+        nbox = lb;
+      } else if (rh) {
+        next = R;
+        nbox = rb;
+      }
+    } else if (L != CLV_REF_EMPTY) {
+      next = L;
+      nbox = lb;
+    } else if (R != CLV_REF_EMPTY) {
+      next = R;
+      nbox = rb;
+    }
+    // descend into `next` (or pop deferred far children)
+    while (true) {
+      if (next != CLV_REF_EMPTY) {
+        if (CLV_REF_KIND(next) == CLV_REF_NODE) {
+          if (cnt) cnt->nodes++;
+          float N, F;
+          if (nbox) slab(nbox, r.o, inv, N, F);
+          else { N = stack[sp].N; F = stack[sp].F; }
+          if (slab_pass(N, F, tmin, tmax)) break;  // continue at node `next`
+        } else if (leaf_test(S, next, r, tmin, tmax, rng, hit, cnt, err)) {
+          tmax = hit.t;
+          ++hits;
+        }
+      }
+      // pop
+      next = CLV_REF_EMPTY;
+      while (sp > 0) {
+        const StackEntry& e = stack[--sp];
+        if (hits > e.hits && hit.t < e.far_d) continue;  // near subtree hit closer than far box
+        next = e.ref;
+        nbox = nullptr;  // own-box slab of a popped node is stack[sp]
+        break;
+      }
+      if (next == CLV_REF_EMPTY) return hit.ref != CLV_REF_EMPTY;
+    }
+    cur = next;
+  }
+}
+
+// Full record of the closest hit (deterministic rebuild for primitives).
+__device__ __forceinline__ void hit_record(const ClvDeviceScene& S, const Ray& r, const Hit& h, Rec& rec) {
+  const uint32_t kind = CLV_REF_KIND(h.ref), idx = CLV_REF_INDEX(h.ref);
+  if (kind == CLV_REF_TRI || kind == CLV_REF_QUAD) {
+    float f[16];
+    load_planar(kind == CLV_REF_TRI ? S.tris : S.quads, idx, f);
+    planar_record(f, r, h.t, h.a, h.b, rec);
+    rec.mat = kind == CLV_REF_TRI ? S.tri_mat[idx] : S.quad_mat[idx];
+  } else if (kind == CLV_REF_SPHERE) {
+    float4 s = load_sphere(S, idx);
+    sphere_record(mk(s.x, s.y, s.z), s.w, r, h.t, rec);
+    rec.mat = S.sphere_mat[idx];
+  } else {
+    rec = h.full;
+  }
+}
+__device__ __forceinline__ uint32_t hit_gid(const ClvDeviceScene& S, uint32_t ref) {
+  const uint32_t kind = CLV_REF_KIND(ref), idx = CLV_REF_INDEX(ref);
+  switch (kind) {
+    case CLV_REF_TRI: return S.tri_gid[idx];
+    case CLV_REF_QUAD: return S.quad_gid[idx];
+    case CLV_REF_SPHERE: return S.sphere_gid[idx];
+    case CLV_REF_OBJ: return S.obj_gid[idx];
+  }
+  return 0xFFFFFFFFu;
+}
+
+// ------------------------------------------------------ MIS (priority) tree --
+// BVHNode::pdf_value (bvh/hitable_trait.rs:89-111): midpoint of both children
+// (f32::midpoint = f64 sum halved, rounded once), single child passed through.
+__device__ float mis_pdf(const ClvDeviceScene& S, V origin, V dir, int lambda, float time, uint32_t* err) {
+  struct Frame {
+    uint32_t node;
+    uint32_t stage;  // 0 start, 1 left evaluated
+    float lval;
+  };
+  Frame st[CLV_MIS_STACK];
+  int sp = 0;
+  uint32_t ref = S.mis_root;
+  float val = 0.0f;
+  while (true) {
+    // descend from `ref` until a leaf value is produced
+    while (CLV_REF_KIND(ref) == CLV_REF_NODE && ref != CLV_REF_EMPTY) {
+      const ClvMisNode n = S.mis_nodes[CLV_REF_INDEX(ref)];
+      if (n.right == CLV_REF_EMPTY) { ref = n.left; continue; }
+      if (n.left == CLV_REF_EMPTY) { ref = n.right; continue; }
+      if (sp >= CLV_MIS_STACK) {
+        if (err) atomicOr(err, CLV_ERR_MIS);
+        return 0.0f;
+      }
+      st[sp++] = Frame{CLV_REF_INDEX(ref), 0u, 0.0f};
+      ref = n.left;
+    }
+    val = ref == CLV_REF_EMPTY ? 0.0f : ObjEval<0>::pdf(S, ref, origin, dir, lambda, time);
+    // ascend: combine finished values
+    while (true) {
+      if (sp == 0) return val;
+      Frame& f = st[sp - 1];
+      if (f.stage == 0) {
+        f.stage = 1;
+        f.lval = val;
+        ref = S.mis_nodes[f.node].right;
+        break;
+      }
+      val = (float)(((double)f.lval + (double)val) / 2.0);
+      --sp;
+    }
+  }
+}
+// leaf random(): Sphere (sphere.rs:160-187), Quad (quad.rs:166-172), Triangle (triangle.rs:203-220)
+__device__ V leaf_random(const ClvDeviceScene& S, uint32_t ref, V origin, Rng& rng) {
+  const uint32_t kind = CLV_REF_KIND(ref), idx = CLV_REF_INDEX(ref);
+  if (kind == CLV_REF_SPHERE) {
+    float4 s = load_sphere(S, idx);
+    V offset = sub(mk(s.x, s.y, s.z), origin);
+    float d2 = nsq(offset);
+    V w = unit(offset);
+    V a = fabsf(w.x) > 0.9f ? unit(mk(0.0f, 1.0f, 0.0f)) : unit(mk(1.0f, 0.0f, 0.0f));
+    V vv = unit(cross(w, a));
+    V uu = unit(cross(w, vv));
+    float r1 = rng.f32();
+    float r2 = rng.f32();
+    float z = 1.0f + r2 * (sqrtf(1.0f - s.w * s.w / d2) - 1.0f);
+    float phi = 2.0f * CLV_PI * r1;
+    float x = cosf(phi) * sqrtf(1.0f - z * z);
+    float y = sinf(phi) * sqrtf(1.0f - z * z);
+    V l = unit(mk(x, y, z));
+    return unit(add(add(scl(l.x, uu), scl(l.y, vv)), scl(l.z, w)));
+  }
+  float f[16];
+  load_planar(kind == CLV_REF_TRI ? S.tris : S.quads, idx, f);
+  V q = mk(f[0], f[1], f[2]), u = mk(f[3], f[4], f[5]), v = mk(f[6], f[7], f[8]);
+  if (kind == CLV_REF_QUAD) {
+    float a = rng.f32();
+    V pa = add(q, scl(a, u));
+    float b = rng.f32();
+    return sub(add(pa, scl(b, v)), origin);
+  }
+  float a = rng.f32(), b = rng.f32();
+  if (a + b > 1.0f) { a = 1.0f - a; b = 1.0f - b; }
+  return sub(add(add(q, scl(a, u)), scl(b, v)), origin);
+}
+// BVHNode::random (hitable_trait.rs:115-127): coin flips down to a leaf
+__device__ V mis_random(const ClvDeviceScene& S, V origin, Rng& rng) {
+  uint32_t ref = S.mis_root;
+  for (int guard = 0; guard < 4096 && CLV_REF_KIND(ref) == CLV_REF_NODE && ref != CLV_REF_EMPTY; ++guard) {
+    const ClvMisNode n = S.mis_nodes[CLV_REF_INDEX(ref)];
+    if (n.right == CLV_REF_EMPTY) ref = n.left;
+    else if (n.left == CLV_REF_EMPTY) ref = n.right;
+    else ref = rng.boolean() ? n.left : n.right;
+  }
+  return leaf_random(S, ref, origin, rng);
+}
+
+// -------------------------------------------------------------- materials --
+__device__ __forceinline__ float spd_get(const ClvDeviceScene& S, uint32_t table, int lambda) {
+  return __ldg(S.spd + (size_t)table * 400 + (lambda - 380));
+}
+__device__ __forceinline__ float tex_color(const ClvDeviceScene& S, const ClvMaterial& m, int lambda, const Rec& rec) {
+  switch (m.tex_kind) {
+    case CLV_TEX_SOLID: return spd_get(S, m.spd_even, lambda);
+    case CLV_TEX_SPATIAL: {
+      float d = m.density * CLV_PI;
+      float s = 1.0f * sinf(d * rec.p.x) * sinf(d * rec.p.y) * sinf(d * rec.p.z);
+      return spd_get(S, s < 0.0f ? m.spd_odd : m.spd_even, lambda);
+    }
+    case CLV_TEX_SURFACE: {
+      float d = m.density * CLV_PI;
+      float s = 1.0f * sinf(d * rec.u) * sinf(d * rec.v);
+      return spd_get(S, s < 0.0f ? m.spd_odd : m.spd_even, lambda);
+    }
+    default:
+      return rclamp(__ldg(S.illuminant + (size_t)m.illuminant * 400 + (lambda - 380)) * m.intensity, 0.0f, 1.0f);
+  }
+}
+__device__ __forceinline__ float tex_emit(const ClvDeviceScene& S, const ClvMaterial& m, int lambda, const Rec& rec) {
+  if (m.tex_kind == CLV_TEX_ILLUMINANT)
+    return __ldg(S.illuminant + (size_t)m.illuminant * 400 + (lambda - 380)) * m.intensity;
+  return tex_color(S, m, lambda, rec);  // non-illuminant textures emit their colour, unclamped
+}
+// Material::emit (diffuse_light.rs:41-53, cone_light.rs:43-66)
+__device__ __forceinline__ float mat_emit(const ClvDeviceScene& S, const ClvMaterial& m, const Ray& r, int lambda,
+                                          const Rec& rec) {
+  if (m.kind == CLV_MAT_DIFFUSELIGHT) {
+    if (!rec.front) return 0.0f;
+    return tex_emit(S, m, lambda, rec);
+  }
+  if (m.kind == CLV_MAT_CONELIGHT) {
+    if (!rec.front) return 0.0f;
+    float spread = m.spread * CLV_DEG2RAD;
+    float angle = acosf(-dot(r.d, rec.n) / (len(r.d) * len(rec.n)));
+    if (angle > spread) return 0.0f;
+    return tex_emit(S, m, lambda, rec);
+  }
+  return 0.0f;
+}
+// Material::color with the optional thin-film factor (materials.rs:95-102, thin_film.rs:31-54)
+__device__ __forceinline__ float mat_color(const ClvDeviceScene& S, const ClvMaterial& m, const Ray& r, int lambda,
+                                           const Rec& rec) {
+  float tf = 1.0f;
+  if (m.thin_film) {
+    float n_ratio = 1.0f / m.tf_ior;
+    float c1 = -dot(r.d, rec.n);
+    float s1 = sqrtf(1.0f - c1 * c1);
+    float s2 = n_ratio * s1;
+    float c2 = sqrtf(1.0f - (s2 * s2));
+    float opd = 2.0f * m.tf_ior * m.tf_thickness * c2;
+    float mm = opd / (float)lambda;
+    tf = 1.0f + cosf(mm * 2.0f * CLV_PI);
+  }
+  float k;
+  switch (m.kind) {
+    case CLV_MAT_DIELECTRIC: k = spd_get(S, m.spd_even, lambda); break;
+    case CLV_MAT_DISPERSIVE: k = 1.0f; break;
+    case CLV_MAT_CONELIGHT:
+    case CLV_MAT_DIFFUSELIGHT: k = rclamp(tex_color(S, m, lambda, rec), 0.0f, 1.0f); break;
+    default: k = tex_color(S, m, lambda, rec); break;
+  }
+  return k * tf;
+}
+__device__ __forceinline__ V reflect(V v, V n) { return unit(sub(v, scl(2.0f * dot(v, n), n))); }
+__device__ __forceinline__ V refract(V v, V n, float ratio) {
+  float ct = fminf(-dot(v, n), 1.0f);
+  V par = scl(ratio, add(v, scl(ct, n)));
+  V perp = scl(-sqrtf(1.0f - nsq(par)), n);
+  return unit(add(par, perp));
+}
+__device__ __forceinline__ float schlick(float cosine, float ri) {
+  float r0 = (1.0f - ri) / (1.0f + ri);
+  r0 = r0 * r0;
+  return r0 + (1.0f - r0) * powf(1.0f - cosine, 5.0f);
+}
+__device__ __forceinline__ float dispersive_index(const ClvMaterial& m, int lambda) {
+  float wm = (float)lambda / 1000.0f;
+  if (!m.sellmeier) return m.cauchy_a + (m.cauchy_b / (wm * wm));
+  float l2 = wm * wm;  // Sellmeier: n^2 = 1 + sum B_i l^2 / (l^2 - C_i)
+  float s = 1.0f;
+  for (int i = 0; i < 3; ++i) s = s + m.sell_b[i] * l2 / (l2 - m.sell_c[i]);
+  return sqrtf(s);
+}
+
+}  // namespace clvd

@@ -1,0 +1,149 @@
+/* clovers_gpu.h -- C ABI of the GB300 (sm_103a) render path of clovers.
+ *
+ * This library replaces the reference's CPU render driver
+ * (clovers-cli/src/draw_cpu.rs:26-31, `draw(global, render_options, scene,
+ * sampler) -> Vec<Xyz<E>>`) and the scene it consumes
+ * (clovers-cli/src/json_scene.rs:12-27, `initialize(path, bvh, w, h) ->
+ * Scene`).  The reference has no FFI of its own (it is one Rust binary); these
+ * are the entry points a Rust `extern "C"` block in clovers-cli would bind.
+ *
+ * Conventions: every function returns 0 on success or a negative CLV_E*
+ * status; clv_last_error() then holds a message (per thread).  No exception
+ * crosses this boundary.  Output buffers are owned by the caller.  Handles are
+ * opaque; one handle must not be used by two threads at the same time.
+ * Functions named *_device take device pointers and a cudaStream_t passed as
+ * void*, and are asynchronous with respect to the host.
+ */
+#ifndef CLOVERS_GPU_H
+#define CLOVERS_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CLV_OK 0
+#define CLV_E_INVALID -1   /* bad argument or unsupported option            */
+#define CLV_E_SCENE -2     /* scene file / mesh cannot be loaded            */
+#define CLV_E_CUDA -3      /* CUDA runtime error (message has the details)  */
+#define CLV_E_DEVICE -4    /* a kernel reported an error flag (stack, nesting) */
+
+#define CLV_BVH_LAM 0 /* BvhAlgorithm::Lam -- not supported (returns CLV_E_INVALID) */
+#define CLV_BVH_SAH 1 /* BvhAlgorithm::Sah (the clovers-cli default, render.rs:43-44) */
+
+/* RenderMode, clovers-cli/src/render.rs:51-61 */
+#define CLV_MODE_PATH_TRACING 0
+#define CLV_MODE_NORMAL_MAP 1
+#define CLV_MODE_BVH_TEST_COUNT 2
+#define CLV_MODE_PRIMITIVE_TEST_COUNT 3
+
+typedef struct clv_scene clv_scene;               /* host-side flattened scene */
+typedef struct clv_device_scene clv_device_scene; /* scene resident in GPU memory */
+
+/* RenderOptions (clovers-cli/src/render.rs:16-49) minus the file options,
+ * plus the seed of the counter-based random streams. */
+typedef struct clv_render_opts {
+  uint32_t width;               /* -w, default 1024 */
+  uint32_t height;              /* -h, default 1024 */
+  uint32_t samples;             /* -s, samples per pixel, default 64 */
+  uint32_t max_depth;           /* -d, default 64 */
+  uint32_t mode;                /* CLV_MODE_*, default path tracing */
+  uint32_t sampler;             /* 0 = random (default); 1 = blue noise: unsupported */
+  uint64_t seed;                /* stream seed; identical seeds give identical images */
+  uint32_t sample_offset;       /* index of the first sample (progressive rendering) */
+  uint32_t samples_per_thread;  /* 0 = automatic */
+} clv_render_opts;
+
+typedef struct clv_scene_info {
+  uint64_t objects;     /* top-level objects after list flattening */
+  uint32_t nodes;       /* BVH nodes */
+  uint32_t triangles, quads, spheres, compound;
+  uint32_t materials;
+  uint32_t tree_depth;  /* BVH depth (root = 1) */
+  uint32_t mis_nodes;
+  uint32_t width, height;
+} clv_scene_info;
+
+typedef struct clv_stats {
+  double gpu_ms;           /* device time of the render kernels */
+  uint64_t samples;        /* width * height * spp */
+  uint32_t device_errors;  /* CLV_ERR_* bits reported by kernels (0 = none) */
+  uint32_t kernel_launches;
+} clv_stats;
+
+/* ---- scenes ------------------------------------------------------------ */
+
+/* json_scene::initialize (clovers-cli/src/json_scene.rs:12-27): parse a
+ * clovers scene file, build the SAH BVH and the MIS (priority) BVH on the
+ * host.  width/height fix the camera aspect ratio. */
+int clv_scene_load_json(const char* path, uint32_t width, uint32_t height, int bvh_alg, clv_scene** out);
+
+/* Same, from the JSON text itself; relative STL paths resolve against base_dir. */
+int clv_scene_load_json_text(const char* json, const char* base_dir, uint32_t width, uint32_t height, int bvh_alg,
+                             clv_scene** out);
+
+/* A triangle-only scene: Triangle::from_coordinates per index triple
+ * (clovers/src/objects/triangle.rs:106-117), all with the default material.
+ * Used for ray-cast workloads; it has no camera and no priority objects. */
+int clv_scene_from_mesh(const float* verts, uint32_t nverts, const uint32_t* indices, uint32_t ntris,
+                        clv_scene** out);
+
+int clv_scene_info_get(const clv_scene* scene, clv_scene_info* out);
+void clv_scene_free(clv_scene* scene);
+
+/* Copies the flattened scene to GPU memory (BVH nodes, primitive records,
+ * materials, spectral tables, MIS tree). */
+int clv_scene_upload(const clv_scene* scene, clv_device_scene** out);
+void clv_device_scene_free(clv_device_scene* dscene);
+
+/* ---- render: the draw() replacement ------------------------------------ */
+
+/* draw_cpu::draw (clovers-cli/src/draw_cpu.rs:26-146): renders and writes the
+ * mean XYZ(E) per pixel, row-major with row 0 at the top of the image (the
+ * reference's pixelbuffer order), xyz_out = width*height*3 floats on the host.
+ * opts->width/height must match the scene's.  Blocks until done. */
+int clv_render(clv_device_scene* dscene, const clv_render_opts* opts, float* xyz_out, clv_stats* stats);
+
+/* Device variant: ADDS the per-pixel sums of film deposits (f64, not divided
+ * by spp) into film_dev (width*height*3 doubles, caller-zeroed), on `stream`. */
+int clv_render_device(clv_device_scene* dscene, const clv_render_opts* opts, double* film_dev, void* stream);
+
+/* Film resolve (clovers-cli/src/write.rs:39-44): mean = film / spp (f64) ->
+ * f32 XYZ(E) -> D65 -> sRGB -> u8.  xyz_out_dev (optional) receives the f32
+ * means.  Device pointers. */
+int clv_resolve_device(const double* film_dev, uint32_t width, uint32_t height, uint32_t spp, float* xyz_out_dev,
+                       uint8_t* rgb_out_dev, void* stream);
+
+/* Host variant of the resolve for XYZ(E) means already on the host. */
+int clv_resolve_srgb(const float* xyz, uint32_t width, uint32_t height, uint8_t* rgb_out);
+
+/* ---- ray casts --------------------------------------------------------- */
+
+/* Closest hit of each ray with BVHNode::hit's exact decision order
+ * (clovers/src/bvh/hitable_trait.rs:15-81).  rays = n x {ox,oy,oz,tmin,
+ * dx,dy,dz,tmax} (32 bytes each, directions unit length); prim_id = index of
+ * the top-level object hit (0xFFFFFFFF on a miss), t = hit distance.
+ * node_visits / prim_tests (optional, may be NULL) count BVHNode::hit calls
+ * (clovers/src/bvh/testcount.rs:23) and primitive tests per ray.  Host buffers;
+ * blocks until done. */
+int clv_raycast(clv_device_scene* dscene, const float* rays, uint64_t n, uint32_t* prim_id, float* t,
+                uint32_t* node_visits, uint32_t* prim_tests);
+
+/* Device variant, asynchronous on `stream`. */
+int clv_raycast_device(const clv_device_scene* dscene, const float* rays_dev, uint64_t n, uint32_t* prim_id_dev,
+                       float* t_dev, uint32_t* node_visits_dev, uint32_t* prim_tests_dev, void* stream);
+
+/* ---- status ------------------------------------------------------------ */
+
+/* Error bits raised by kernels since the last call (clears them). */
+int clv_device_status(clv_device_scene* dscene, uint32_t* flags_out);
+
+const char* clv_last_error(void);
+const char* clv_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CLOVERS_GPU_H */

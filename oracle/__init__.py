@@ -1,0 +1,223 @@
+"""CPU oracle of the clovers render path -- TEST INFRASTRUCTURE ONLY.
+
+A ctypes wrapper over ``oracle.cpp`` (a C++ restatement of the reference's
+Rust algorithm).  Only the test suite, ``__graft_entry__.smoke()`` and the
+CPU-baseline leg of ``bench.py`` may use it, and only as the checker or the
+CPU baseline -- never as the product path.
+"""
+
+import ctypes
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "liboracle.so")
+_SRC = [os.path.join(HERE, "oracle.cpp"), os.path.join(HERE, "..", "clovers_gb300", "csrc", "json.hpp"),
+        os.path.join(HERE, "..", "clovers_gb300", "csrc", "spectral_tables.h")]
+_L = None
+_LOCK = threading.Lock()
+
+
+def build(force=False):
+    stale = force or not os.path.exists(LIB) or any(os.path.getmtime(s) > os.path.getmtime(LIB) for s in _SRC)
+    if stale:
+        p = subprocess.run(["make", "-C", HERE, "-B" if force else "all"], stdout=subprocess.PIPE,
+                           stderr=subprocess.STDOUT, text=True)
+        if p.returncode != 0:
+            raise RuntimeError("oracle build failed:\n" + p.stdout)
+    return LIB
+
+
+def lib():
+    global _L
+    with _LOCK:
+        if _L is None:
+            build()
+            L = ctypes.CDLL(LIB)
+            vp, u32, u64, i32, f32 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int, ctypes.c_float
+            sig = {
+                "orc_last_error": (ctypes.c_char_p, []),
+                "orc_spectral_power": (i32, [f32, f32, f32, i32, ctypes.POINTER(f32)]),
+                "orc_wavelength_into_xyz": (None, [i32, vp]),
+                "orc_rotate_wavelength": (None, [i32, vp]),
+                "orc_srgb_to_xyz_e": (None, [vp, vp]),
+                "orc_xyz_e_to_srgb8": (None, [vp, u64, vp]),
+                "orc_aabb_area": (f32, [vp]),
+                "orc_aabb_centroid": (None, [vp, vp]),
+                "orc_aabb_combine": (None, [vp, vp, vp]),
+                "orc_aabb_hit": (i32, [vp, vp]),
+                "orc_interval": (None, [f32, f32, vp]),
+                "orc_prim_hit": (i32, [i32, vp, vp, vp, vp, vp, vp]),
+                "orc_scene_load_json": (vp, [ctypes.c_char_p, u32, u32]),
+                "orc_scene_from_mesh": (vp, [vp, u32, vp, u32]),
+                "orc_scene_free": (None, [vp]),
+                "orc_scene_object_count": (u64, [vp]),
+                "orc_scene_tree_stats": (None, [vp, vp]),
+                "orc_camera_ray": (None, [vp, f32, f32, f32, f32, vp]),
+                "orc_scene_background_xyz": (None, [vp, vp]),
+                "orc_raycast": (i32, [vp, vp, u64, vp, vp, vp, vp, i32]),
+                "orc_render": (i32, [vp, u32, u32, u32, u32, u64, u32, u32, u32, u32, u32, vp, i32]),
+                "orc_trace_sample": (i32, [vp, u32, u32, u32, u32, u32, u32, u64, vp, vp, vp]),
+            }
+            for name, (res, args) in sig.items():
+                fn = getattr(L, name)
+                fn.restype = res
+                fn.argtypes = args
+            _L = L
+        return _L
+
+
+def _err():
+    return lib().orc_last_error().decode()
+
+
+def _buf(a):
+    return a.ctypes.data
+
+
+def spectral_power(xyz, lam):
+    out = ctypes.c_float()
+    if lib().orc_spectral_power(float(xyz[0]), float(xyz[1]), float(xyz[2]), int(lam), ctypes.byref(out)) != 0:
+        raise ValueError(_err())
+    return np.float32(out.value)
+
+
+def wavelength_into_xyz(lam):
+    o = np.zeros(3, np.float32)
+    lib().orc_wavelength_into_xyz(int(lam), _buf(o))
+    return o
+
+
+def rotate_wavelength(hero):
+    o = np.zeros(4, np.int32)
+    lib().orc_rotate_wavelength(int(hero), _buf(o))
+    return o
+
+
+def srgb_to_xyz_e(rgb):
+    i = np.asarray(rgb, np.float32)
+    o = np.zeros(3, np.float32)
+    lib().orc_srgb_to_xyz_e(_buf(i), _buf(o))
+    return o
+
+
+def xyz_e_to_srgb8(xyz):
+    x = np.ascontiguousarray(xyz, np.float32).reshape(-1, 3)
+    o = np.zeros_like(x, dtype=np.uint8)
+    lib().orc_xyz_e_to_srgb8(_buf(x), x.shape[0], _buf(o))
+    return o
+
+
+def aabb_area(box):
+    b = np.asarray(box, np.float32)
+    return np.float32(lib().orc_aabb_area(_buf(b)))
+
+
+def aabb_centroid(box):
+    b = np.asarray(box, np.float32)
+    o = np.zeros(3, np.float32)
+    lib().orc_aabb_centroid(_buf(b), _buf(o))
+    return o
+
+
+def aabb_combine(a, b):
+    x, y = np.asarray(a, np.float32), np.asarray(b, np.float32)
+    o = np.zeros(6, np.float32)
+    lib().orc_aabb_combine(_buf(x), _buf(y), _buf(o))
+    return o
+
+
+def aabb_hit(box, ray):
+    b, r = np.asarray(box, np.float32), np.asarray(ray, np.float32)
+    return bool(lib().orc_aabb_hit(_buf(b), _buf(r)))
+
+
+def interval(a, b):
+    o = np.zeros(4, np.float32)
+    lib().orc_interval(float(a), float(b), _buf(o))
+    return o  # min, max, size, center
+
+
+def prim_hit(kind, q, u, v, ray):
+    """kind 1 triangle, 2 quad, 3 sphere (q = center, u[0] = radius).  -> (hit, record[10], box[6])"""
+    qa, ua, va = (np.asarray(x, np.float32) for x in (q, u, v))
+    r = np.asarray(ray, np.float32)
+    rec = np.zeros(10, np.float32)
+    box = np.zeros(6, np.float32)
+    h = lib().orc_prim_hit(kind, _buf(qa), _buf(ua), _buf(va), _buf(r), _buf(rec), _buf(box))
+    return bool(h), rec, box
+
+
+class Scene:
+    def __init__(self, handle):
+        if not handle:
+            raise ValueError(_err())
+        self.h = ctypes.c_void_p(handle)
+
+    @classmethod
+    def from_json(cls, path, width, height):
+        return cls(lib().orc_scene_load_json(os.fsencode(path), width, height))
+
+    @classmethod
+    def from_mesh(cls, verts, idx):
+        v = np.ascontiguousarray(verts, np.float32).reshape(-1, 3)
+        i = np.ascontiguousarray(idx, np.uint32).reshape(-1, 3)
+        return cls(lib().orc_scene_from_mesh(_buf(v), v.shape[0], _buf(i), i.shape[0]))
+
+    def __del__(self):
+        try:
+            if self.h and self.h.value:
+                lib().orc_scene_free(self.h)
+        except Exception:
+            pass
+
+    def object_count(self):
+        return lib().orc_scene_object_count(self.h)
+
+    def tree_stats(self):
+        o = np.zeros(3, np.uint64)
+        lib().orc_scene_tree_stats(self.h, _buf(o))
+        return {"nodes": int(o[0]), "tree_depth": int(o[1]), "mis_nodes": int(o[2])}
+
+    def camera_ray(self, pu, pv, lx=0.0, ly=0.0):
+        o = np.zeros(6, np.float32)
+        lib().orc_camera_ray(self.h, pu, pv, lx, ly, _buf(o))
+        return o
+
+    def background_xyz(self):
+        o = np.zeros(3, np.float32)
+        lib().orc_scene_background_xyz(self.h, _buf(o))
+        return o
+
+    def raycast(self, rays, threads=None, with_counts=False):
+        r = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+        n = r.shape[0]
+        prim = np.empty(n, np.uint32)
+        t = np.empty(n, np.float32)
+        nodes = np.empty(n, np.uint32) if with_counts else None
+        tests = np.empty(n, np.uint32) if with_counts else None
+        lib().orc_raycast(self.h, _buf(r), n, _buf(prim), _buf(t), _buf(nodes) if with_counts else None,
+                          _buf(tests) if with_counts else None, threads or os.cpu_count() or 1)
+        return (prim, t, nodes, tests) if with_counts else (prim, t)
+
+    def render(self, width, height, spp, max_depth, seed, window=None, sample_offset=0, threads=None):
+        """Per-pixel SUM of film deposits (f64), window = (x0, r0, x1, r1) in buffer coordinates."""
+        x0, r0, x1, r1 = window or (0, 0, width, height)
+        out = np.zeros(((r1 - r0) * (x1 - x0), 3), np.float64)
+        rc = lib().orc_render(self.h, width, height, spp, max_depth, seed, x0, r0, x1, r1, sample_offset, _buf(out),
+                              threads or os.cpu_count() or 1)
+        if rc != 0:
+            raise RuntimeError(_err())
+        return out
+
+    def trace_sample(self, width, height, x, r, sample, max_depth, seed):
+        p = np.zeros(4, np.float32)
+        w = np.zeros(4, np.int32)
+        ray = np.zeros(6, np.float32)
+        if lib().orc_trace_sample(self.h, width, height, x, r, sample, max_depth, seed, _buf(p), _buf(w),
+                                  _buf(ray)) != 0:
+            raise RuntimeError(_err())
+        return p, w, ray

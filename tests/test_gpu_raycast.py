@@ -1,0 +1,91 @@
+"""GPU closest-hit ray casts against the oracle: bit-exact hit ids and
+distances, and identical traversal counts (BVHNode::hit calls and primitive
+tests per ray), through the C ABI."""
+
+import numpy as np
+import pytest
+
+import clovers_gb300 as cg
+import oracle
+from clovers_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def _compare(dscene, oscene, rays):
+    prim, t, nodes, tests = cg.raycast(dscene, rays, with_counts=True)
+    oprim, ot, onodes, otests = oscene.raycast(rays, with_counts=True)
+    assert np.array_equal(prim, oprim), "hit ids differ on %d rays" % int((prim != oprim).sum())
+    hit = oprim != 0xFFFFFFFF
+    assert np.array_equal(t[hit].view(np.uint32), ot[hit].view(np.uint32)), "hit distances differ"
+    assert np.array_equal(nodes, onodes), "BVH node visit counts differ"
+    assert np.array_equal(tests, otests), "primitive test counts differ"
+    assert dscene.status() == 0
+    return hit.mean()
+
+
+@pytest.mark.parametrize("ntris,nrays", [(1, 4096), (2, 4096), (7, 4096), (4096, 65536), (65536, 262144)])
+def test_triangle_soup_parity(ntris, nrays):
+    v, i = scenes.triangle_soup(ntris, seed=5)
+    rays = scenes.random_rays(nrays, seed=6)
+    d = cg.Scene.from_mesh(v, i).upload()
+    frac = _compare(d, oracle.Scene.from_mesh(v, i), rays)
+    if ntris >= 4096:
+        assert frac > 0.1
+
+
+def test_shared_edges_and_grid_rays():
+    # a regular grid mesh: many rays hit edges and vertices shared by two or more triangles
+    n = 64
+    xs = np.linspace(0, 1, n + 1, dtype=np.float32)
+    gx, gy = np.meshgrid(xs, xs)
+    verts = np.stack([gx.ravel(), gy.ravel(), np.zeros(gx.size, np.float32)], 1).astype(np.float32)
+    idx = []
+    for r in range(n):
+        for c in range(n):
+            a = r * (n + 1) + c
+            idx += [[a, a + 1, a + n + 1], [a + 1, a + n + 2, a + n + 1]]
+    idx = np.array(idx, np.uint32)
+    g = np.linspace(0, 1, 257, dtype=np.float32)
+    ox, oy = np.meshgrid(g, g)
+    rays = np.zeros((ox.size, 8), np.float32)
+    rays[:, 0], rays[:, 1], rays[:, 2] = ox.ravel(), oy.ravel(), -1.0
+    rays[:, 3], rays[:, 6], rays[:, 7] = 0.001, 1.0, np.float32(3.4e38)
+    d = cg.Scene.from_mesh(verts, idx).upload()
+    assert _compare(d, oracle.Scene.from_mesh(verts, idx), rays) > 0.9
+
+
+def test_axis_aligned_and_degenerate_rays():
+    v, i = scenes.triangle_soup(2048, seed=8)
+    rng = np.random.default_rng(9)
+    rays = np.zeros((6 * 2048, 8), np.float32)
+    rays[:, 0:3] = rng.random((rays.shape[0], 3))
+    for k in range(6):  # +-x, +-y, +-z directions: zero components give inf/NaN slabs
+        rays[k * 2048:(k + 1) * 2048, 4 + k // 2] = 1.0 if k % 2 == 0 else -1.0
+    rays[:, 3], rays[:, 7] = 0.001, np.float32(3.4e38)
+    d = cg.Scene.from_mesh(v, i).upload()
+    _compare(d, oracle.Scene.from_mesh(v, i), rays)
+
+
+def test_box_scene_parity(box_scene_path):
+    w = h = 96
+    d = cg.Scene.from_json(box_scene_path, w, h).upload()
+    o = oracle.Scene.from_json(box_scene_path, w, h)
+    cam = scenes.camera_rays(w, h, lambda pu, pv: o.camera_ray(pu, pv))
+    rays = np.concatenate([cam, scenes.random_rays(20000, seed=4) * np.array([555] * 3 + [1] * 5, np.float32)])
+    assert _compare(d, o, rays) > 0.5
+
+
+def test_spheres_scene_parity(spheres_scene_path):
+    w, h = 80, 45
+    d = cg.Scene.from_json(spheres_scene_path, w, h).upload()
+    o = oracle.Scene.from_json(spheres_scene_path, w, h)
+    cam = scenes.camera_rays(w, h, lambda pu, pv: o.camera_ray(pu, pv))
+    _compare(d, o, cam)
+
+
+def test_empty_ray_batch():
+    v, i = scenes.triangle_soup(16, seed=1)
+    d = cg.Scene.from_mesh(v, i).upload()
+    prim, t = cg.raycast(d, np.zeros((0, 8), np.float32))
+    assert prim.size == 0 and t.size == 0
