@@ -20,30 +20,34 @@
 #include "../../include/clovers_gpu.h"
 #include "clv_device.cuh"
 #include "scene.hpp"
+#include "wavefront.cuh"
 #include "spectral.hpp"
 
 using namespace clvd;
 
 // ------------------------------------------------------------------ kernels --
 
+template <bool COMPLEX>
 __global__ void __launch_bounds__(128) raycast_kernel(ClvDeviceScene S, const float4* __restrict__ rays, uint64_t n,
                                                       uint32_t* __restrict__ prim, float* __restrict__ tout,
                                                       uint32_t* __restrict__ nodes, uint32_t* __restrict__ tests,
                                                       uint32_t* err) {
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const bool want = nodes != nullptr || tests != nullptr;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
     const float4 a = __ldcs(rays + 2 * i), b = __ldcs(rays + 2 * i + 1);
-    Ray r{mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), 0.0f, 600};
+    const Ray r{mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), 0.0f, 600};
     Hit h;
     Counters c{0u, 0u};
     Rng rng;
     rng.init(0, (uint32_t)i, 0);
-    const bool want = nodes != nullptr || tests != nullptr;
-    const bool any = closest_hit(S, r, a.w, b.w, &rng, h, want ? &c : nullptr, err);
+    const bool any = closest_hit<COMPLEX>(S, r, a.w, b.w, &rng, h, nullptr, want ? &c : nullptr, err);
     __stcs(prim + i, any ? hit_gid(S, h.ref) : 0xFFFFFFFFu);
     __stcs(tout + i, any ? h.t : 0.0f);
-    if (nodes) nodes[i] = c.nodes;
-    if (tests) tests[i] = c.prims;
+    if (want) {
+      if (nodes) nodes[i] = c.nodes;
+      if (tests) tests[i] = c.prims;
+    }
   }
 }
 
@@ -91,13 +95,14 @@ __device__ void trace_path(const ClvDeviceScene& S, Ray ray, uint32_t max_depth,
   for (uint32_t depth = 0;; ++depth) {
     if (depth > max_depth) break;
     Hit h;
-    if (!closest_hit(S, ray, CLV_EPS_ACNE, CLV_FLT_MAX, &rng, h, nullptr, err)) {
+    Rec full;
+    if (!closest_hit<true>(S, ray, CLV_EPS_ACNE, CLV_FLT_MAX, &rng, h, &full, nullptr, err)) {
 #pragma unroll
       for (int i = 0; i < 4; ++i) L[i] += beta[i] * spd_get(S, S.background_spd, waves[i]);
       break;
     }
     Rec rec;
-    hit_record(S, ray, h, rec);
+    hit_record(S, ray, h, full, rec);
     const ClvMaterial& m = S.materials[rec.mat];
     const uint32_t kind = m.kind;
     if (kind == CLV_MAT_DIFFUSELIGHT || kind == CLV_MAT_CONELIGHT) {  // no scatter: emitted only
@@ -252,12 +257,13 @@ __global__ void debug_kernel(ClvDeviceScene S, RenderParams P, double* __restric
   Ray r{ld3(C.origin), unit(dir), 0.0f, lambda};
   float rgb[3] = {0.0f, 0.0f, 0.0f};  // linear sRGB
   Hit h;
+  Rec full;
   Counters c{0u, 0u};
-  const bool any = closest_hit(S, r, CLV_EPS_ACNE, CLV_FLT_MAX, &rng, h, &c, err);
+  const bool any = closest_hit<true>(S, r, CLV_EPS_ACNE, CLV_FLT_MAX, &rng, h, &full, &c, err);
   if (P.mode == CLV_MODE_NORMAL_MAP) {  // normals.rs:11-37
     if (any) {
       Rec rec;
-      hit_record(S, r, h, rec);
+      hit_record(S, r, h, full, rec);
       const V n = mk(-rec.n.x, rec.n.y, -rec.n.z);
       rgb[0] = 0.5f + 0.5f * n.x;
       rgb[1] = 0.5f + 0.5f * n.y;
@@ -304,6 +310,32 @@ __global__ void resolve_kernel(ResolveParams R, const double* __restrict__ film,
       rgb[3 * i + r] = (uint8_t)v;
     }
   }
+}
+
+// Self-test of div_rn against IEEE division on random operands: a spans
+// magnitudes 2^-40..2^40 with random signs, d spans 2^-70..2^70 including
+// values outside div_rn's fast range, zeros and infinities.
+__global__ void selftest_division_kernel(uint64_t n, uint64_t seed, unsigned long long* bad) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  unsigned long long local = 0;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const uint64_t h1 = mix64(seed ^ (i * 0x9E3779B97F4A7C15ull)), h2 = mix64(h1 + 0x632BE59BD9B4E019ull);
+    float a = __uint_as_float((uint32_t)(h1 & 0x807FFFFFu) | ((uint32_t)(87 + (h1 >> 32) % 81) << 23));
+    float d = __uint_as_float((uint32_t)(h2 & 0x807FFFFFu) | ((uint32_t)(57 + (h2 >> 32) % 141) << 23));
+    const uint32_t sel = (uint32_t)(h2 >> 56);
+    if (sel == 0) d = 0.0f;
+    if (sel == 1) d = -0.0f;
+    if (sel == 2) a = 0.0f;
+    if (sel == 3) d = __uint_as_float(0x7F800000u);
+    if (sel == 4) d = __uint_as_float((uint32_t)(h2 & 0x807FFFFFu));  // subnormal
+    const float inv = 1.0f / d;
+    const float ad = fabsf(d);
+    const bool fast = ad >= 8.67361738e-19f && ad <= 1.15292150e18f;
+    const float q = fast ? div_rn(a, d, inv) : a / d;
+    const float e = a / d;
+    if (__float_as_uint(q) != __float_as_uint(e) && !(q != q && e != e)) ++local;
+  }
+  if (local) atomicAdd(bad, local);
 }
 
 // --------------------------------------------------------------- host side --
@@ -360,11 +392,44 @@ struct clv_device_scene {
   // scratch reused by the host-buffer entry points
   void* scratch = nullptr;
   size_t scratch_bytes = 0;
+  // wavefront path state, sized on first use
+  void* wf_mem = nullptr;
+  uint32_t wf_slots = 0;
+  WfCounters* wf_counters = nullptr;
+  unsigned int* wf_live_host = nullptr;  // pinned
   ~clv_device_scene() {
     for (void* p : owned) cudaFree(p);
     if (err) cudaFree(err);
     if (scratch) cudaFree(scratch);
+    if (wf_mem) cudaFree(wf_mem);
+    if (wf_counters) cudaFree(wf_counters);
+    if (wf_live_host) cudaFreeHost(wf_live_host);
   }
+  WfState wavefront_state(uint32_t q) {
+    if (q > wf_slots) {
+      if (wf_mem) cudaFree(wf_mem);
+      wf_mem = nullptr;
+      wf_slots = 0;
+      ck(cudaMalloc(&wf_mem, (size_t)q * kWfSlotBytes), "cudaMalloc path state");
+      wf_slots = q;
+    }
+    if (!wf_counters) ck(cudaMalloc(&wf_counters, sizeof(WfCounters)), "cudaMalloc");
+    if (!wf_live_host) ck(cudaMallocHost(&wf_live_host, sizeof(unsigned int)), "cudaMallocHost");
+    char* p = static_cast<char*>(wf_mem);
+    const size_t n = wf_slots;
+    WfState W;
+    W.o_time = reinterpret_cast<float4*>(p); p += n * 16;
+    W.d_lambda = reinterpret_cast<float4*>(p); p += n * 16;
+    W.beta = reinterpret_cast<float4*>(p); p += n * 16;
+    W.L = reinterpret_cast<float4*>(p); p += n * 16;
+    W.meta = reinterpret_cast<uint4*>(p); p += n * 16;
+    W.hit = reinterpret_cast<float4*>(p); p += n * 16;
+    W.full = reinterpret_cast<float4*>(p); p += n * 48;
+    W.key = reinterpret_cast<uint2*>(p);
+    W.Q = q;
+    return W;
+  }
+  static constexpr size_t kWfSlotBytes = 16 * 6 + 48 + 8;
   void* ensure_scratch(size_t bytes) {
     if (bytes > scratch_bytes) {
       if (scratch) cudaFree(scratch);
@@ -391,6 +456,7 @@ static int check_opts(const clv_device_scene* d, const clv_render_opts* o) {
   if (o->samples == 0) return fail(CLV_E_INVALID, "samples must be positive");
   if (o->sampler != 0) return fail(CLV_E_INVALID, "only the random sampler is supported (blue-noise tables are absent)");
   if (o->mode > CLV_MODE_PRIMITIVE_TEST_COUNT) return fail(CLV_E_INVALID, "unknown render mode");
+  if (o->engine > 1) return fail(CLV_E_INVALID, "unknown render engine");
   if ((uint64_t)o->width * o->height > 0x1FFFFFFFull) return fail(CLV_E_INVALID, "image too large");
   return CLV_OK;
 }
@@ -421,6 +487,24 @@ extern "C" {
 
 const char* clv_last_error(void) { return g_error.c_str(); }
 const char* clv_version(void) { return "clovers_gb300 0.1 (sm_103a)"; }
+
+int clv_selftest_division(uint64_t n, uint64_t seed, uint64_t* mismatches) {
+  if (!mismatches) return fail(CLV_E_INVALID, "null argument");
+  try {
+    unsigned long long* bad = nullptr;
+    ck(cudaMalloc(&bad, sizeof(unsigned long long)), "cudaMalloc");
+    ck(cudaMemset(bad, 0, sizeof(unsigned long long)), "cudaMemset");
+    selftest_division_kernel<<<launch_grid(n, 256), 256>>>(n, seed, bad);
+    unsigned long long h = 0;
+    const cudaError_t e = cudaMemcpy(&h, bad, sizeof h, cudaMemcpyDeviceToHost);
+    cudaFree(bad);
+    ck(e, "selftest");
+    *mismatches = h;
+    return CLV_OK;
+  } catch (std::exception& e) {
+    return fail(CLV_E_CUDA, e.what());
+  }
+}
 
 int clv_scene_load_json_text(const char* json, const char* base_dir, uint32_t width, uint32_t height, int bvh_alg,
                              clv_scene** out) {
@@ -561,8 +645,12 @@ int clv_raycast_device(const clv_device_scene* d, const float* rays_dev, uint64_
   if (n == 0) return CLV_OK;
   if ((reinterpret_cast<uintptr_t>(rays_dev) & 15u) != 0) return fail(CLV_E_INVALID, "rays must be 16-byte aligned");
   const int block = 128;
-  raycast_kernel<<<launch_grid(n, block), block, 0, (cudaStream_t)stream>>>(
-      d->view, reinterpret_cast<const float4*>(rays_dev), n, prim_dev, t_dev, nodes_dev, tests_dev, d->err);
+  if (d->view.n_objs)
+    raycast_kernel<true><<<launch_grid(n, block), block, 0, (cudaStream_t)stream>>>(
+        d->view, reinterpret_cast<const float4*>(rays_dev), n, prim_dev, t_dev, nodes_dev, tests_dev, d->err);
+  else
+    raycast_kernel<false><<<launch_grid(n, block), block, 0, (cudaStream_t)stream>>>(
+        d->view, reinterpret_cast<const float4*>(rays_dev), n, prim_dev, t_dev, nodes_dev, tests_dev, d->err);
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail(CLV_E_CUDA, std::string("raycast launch: ") + cudaGetErrorString(e));
   return CLV_OK;
@@ -600,12 +688,56 @@ int clv_raycast(clv_device_scene* d, const float* rays, uint64_t n, uint32_t* pr
   }
 }
 
+static int render_wavefront(clv_device_scene* d, const clv_render_opts* o, double* film, cudaStream_t st) {
+  try {
+    WfParams P;
+    P.width = o->width;
+    P.height = o->height;
+    P.max_depth = o->max_depth;
+    P.sample_offset = o->sample_offset;
+    P.npix = (uint64_t)o->width * o->height;
+    P.total = P.npix * o->samples;
+    P.seed = o->seed;
+    uint64_t q = o->path_slots ? o->path_slots : (uint64_t)sm_count() * 2048 * 4;
+    q = std::min<uint64_t>(q, P.total);
+    q = (q + 127) / 128 * 128;
+    WfState W = d->wavefront_state((uint32_t)q);
+    WfCounters c0{std::min<uint64_t>(q, P.total), 0u, 0u};
+    ck(cudaMemcpyAsync(d->wf_counters, &c0, sizeof c0, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync");
+    const int block = 128;
+    const uint32_t grid = (uint32_t)((q + block - 1) / block);
+    wf_init<<<grid, block, 0, st>>>(d->view, P, W);
+    const bool complex = d->view.n_objs != 0;
+    // a path lives at most max_depth + 1 bounces; the live counter is polled every `batch` bounces
+    const int batch = 8;
+    for (uint64_t it = 0;; it += batch) {
+      for (int k = 0; k < batch; ++k) {
+        cudaMemsetAsync(&d->wf_counters->live, 0, sizeof(unsigned int), st);
+        if (complex) wf_intersect<true><<<grid, block, 0, st>>>(d->view, W, d->err);
+        else wf_intersect<false><<<grid, block, 0, st>>>(d->view, W, d->err);
+        wf_shade<<<grid, block, 0, st>>>(d->view, P, W, d->wf_counters, film, d->err);
+      }
+      ck(cudaGetLastError(), "wavefront launch");
+      ck(cudaMemcpyAsync(d->wf_live_host, &d->wf_counters->live, sizeof(unsigned int), cudaMemcpyDeviceToHost, st),
+         "cudaMemcpyAsync");
+      ck(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+      if (*d->wf_live_host == 0) break;
+      if (it > (uint64_t)4 * (P.total / q + 1) * (o->max_depth + 2) + 64)
+        throw std::runtime_error("wavefront did not drain");  // unreachable unless a kernel misbehaves
+    }
+    return CLV_OK;
+  } catch (std::exception& e) {
+    return fail(CLV_E_CUDA, e.what());
+  }
+}
+
 int clv_render_device(clv_device_scene* d, const clv_render_opts* o, double* film_dev, void* stream) {
   int rc = check_opts(d, o);
   if (rc) return rc;
   if (!film_dev) return fail(CLV_E_INVALID, "null film");
-  const RenderParams P = make_params(o);
   const int block = 128;
+  if (o->mode == CLV_MODE_PATH_TRACING && o->engine == 0) return render_wavefront(d, o, film_dev, (cudaStream_t)stream);
+  const RenderParams P = make_params(o);
   if (o->mode == CLV_MODE_PATH_TRACING) {
     render_kernel<<<launch_grid(P.npix * P.chunks, block), block, 0, (cudaStream_t)stream>>>(d->view, P, film_dev,
                                                                                              d->err);

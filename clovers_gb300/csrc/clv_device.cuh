@@ -423,23 +423,56 @@ __device__ __noinline__ float ObjEval<LEVEL>::pdf(const ClvDeviceScene& S, uint3
 // ------------------------------------------------------------- traversal --
 // Closest-hit state.  For triangles/quads/spheres only (t, ref, u, v) are kept
 // and the full record is rebuilt afterwards (deterministic); compound objects
-// keep their full record since media consume randomness.
+// write their full record to `full` since media consume randomness.
 struct Hit {
   float t;
   uint32_t ref;  // leaf ref that produced the hit, CLV_REF_EMPTY if none
   float a, b;    // plane coordinates (triangle / quad)
-  Rec full;      // compound objects only
 };
 
-struct StackEntry {
-  uint32_t ref;
-  uint32_t hits;
-  float far_d, N, F;
-};
+// a / d for the slab divisions of AABB::distance, given inv = RN(1/d).
+// q0 = RN(a*inv); the residual a - q0*d is exact with an FMA and one
+// correction step q0 + residual*inv rounds to the correctly rounded quotient
+// (Markstein's theorem; Muller et al., Handbook of Floating-Point Arithmetic,
+// ch. 8) while no intermediate overflows or underflows.  Outside the guarded
+// range the IEEE division is used, so every result equals a / d exactly.
+__device__ __forceinline__ float div_rn(float a, float d, float inv) {
+  const float q0 = a * inv;
+  const float aq = fabsf(q0);
+  if (aq >= 8.67361738e-19f && aq <= 1.15292150e18f) {  // 2^-60 .. 2^60
+    const float r = __fmaf_rn(-q0, d, a);
+    return __fmaf_rn(r, inv, q0);
+  }
+  return a / d;
+}
 
-// Tests one BVH leaf with the current tmax; on acceptance updates hit/tmax.
+// Per-ray constants of the traversal.
+struct RayPre {
+  V o, d, inv;
+  bool fast;  // all |d| in [2^-60, 2^60]: div_rn's guard suffices
+};
+__device__ __forceinline__ float divc(const RayPre& R, float a, int axis) {
+  const float d = comp(R.d, axis), inv = comp(R.inv, axis);
+  return R.fast ? div_rn(a, d, inv) : a / d;
+}
+// AABB::distance with div_rn
+__device__ __forceinline__ bool box_distance_pre(const float* b, const RayPre& R, float& out) {
+  float tx1 = divc(R, b[0] - R.o.x, 0), tx2 = divc(R, b[1] - R.o.x, 0);
+  float tmin = fminf(tx1, tx2), tmax = fmaxf(tx1, tx2);
+  float ty1 = divc(R, b[2] - R.o.y, 1), ty2 = divc(R, b[3] - R.o.y, 1);
+  tmin = fmaxf(tmin, fminf(ty1, ty2));
+  tmax = fminf(tmax, fmaxf(ty1, ty2));
+  float tz1 = divc(R, b[4] - R.o.z, 2), tz2 = divc(R, b[5] - R.o.z, 2);
+  tmin = fmaxf(tmin, fminf(tz1, tz2));
+  tmax = fminf(tmax, fmaxf(tz1, tz2));
+  out = tmin;
+  return tmax >= tmin && tmax > 0.0f;
+}
+
+// Tests one BVH leaf with the current tmax.
+template <bool COMPLEX>
 __device__ __forceinline__ bool leaf_test(const ClvDeviceScene& S, uint32_t ref, const Ray& r, float tmin,
-                                          float tmax, Rng* rng, Hit& hit, Counters* cnt, uint32_t* err) {
+                                          float tmax, Rng* rng, Hit& hit, Rec* full, Counters* cnt, uint32_t* err) {
   const uint32_t kind = CLV_REF_KIND(ref), idx = CLV_REF_INDEX(ref);
   if (kind == CLV_REF_TRI || kind == CLV_REF_QUAD) {
     if (cnt) cnt->prims++;
@@ -460,103 +493,130 @@ __device__ __forceinline__ bool leaf_test(const ClvDeviceScene& S, uint32_t ref,
     hit.ref = ref;
     return true;
   }
-  Rec rec;
-  if (!ObjEval<0>::hit(S, ref, r, tmin, tmax, rng, rec, cnt, err)) return false;
-  hit.t = rec.t;
-  hit.ref = ref;
-  hit.full = rec;
-  return true;
+  if (COMPLEX) {
+    Rec rec;
+    if (!ObjEval<0>::hit(S, ref, r, tmin, tmax, rng, rec, cnt, err)) return false;
+    hit.t = rec.t;
+    hit.ref = ref;
+    if (full) *full = rec;
+    return true;
+  }
+  return false;
 }
 
-// BVHNode::hit over the flattened tree.  Returns true with `hit` filled.
+// BVHNode::hit over the flattened tree, one "call" (node or leaf) per loop
+// iteration so that warps reconverge every iteration.
+//
+// Stack entries are the deferred far children of the nodes on the current
+// path (ref, entry distance, slab interval).  Whether a node's near subtree
+// produced a hit is tracked without per-entry counters: every entry on the
+// stack belongs to an ancestor whose near subtree is being traversed, so when
+// a hit is accepted all current entries are marked, which keeps the marked
+// entries a prefix [0, marked) of the stack.
+template <bool COMPLEX>
 __device__ bool closest_hit(const ClvDeviceScene& S, const Ray& r, float tmin, float tmax, Rng* rng, Hit& hit,
-                            Counters* cnt, uint32_t* err) {
+                            Rec* full, Counters* cnt, uint32_t* err) {
   hit.ref = CLV_REF_EMPTY;
-  const V inv = mk(1.0f / r.d.x, 1.0f / r.d.y, 1.0f / r.d.z);
-  uint32_t hits = 0;
-  StackEntry stack[CLV_STACK];
-  int sp = 0;
-  uint32_t cur = S.root;
-  {  // the root is always a node (BVHNode::from_list)
-    if (cnt) cnt->nodes++;
-    float N, F;
-    slab(S.root_box, r.o, inv, N, F);
-    if (!slab_pass(N, F, tmin, tmax)) return false;
+  hit.t = 0.0f;
+  RayPre R;
+  R.o = r.o;
+  R.d = r.d;
+  R.inv = mk(1.0f / r.d.x, 1.0f / r.d.y, 1.0f / r.d.z);
+  {
+    const float ax = fabsf(r.d.x), ay = fabsf(r.d.y), az = fabsf(r.d.z);
+    const float lo = 8.67361738e-19f, hi = 1.15292150e18f;
+    R.fast = ax >= lo && ax <= hi && ay >= lo && ay <= hi && az >= lo && az <= hi;
   }
+  float4 stack[CLV_STACK];
+  int sp = 0, marked = 0;
+  uint32_t ref = S.root;
+  float N, F;
+  slab(S.root_box, r.o, R.inv, N, F);
+  bool found = false;
   while (true) {
-    // `cur` is a node whose own box test passed
-    const ClvNode* np = S.nodes + CLV_REF_INDEX(cur);
-    const float4* p4 = reinterpret_cast<const float4*>(np);
-    const float4 q0 = __ldg(p4), q1 = __ldg(p4 + 1), q2 = __ldg(p4 + 2), q3 = __ldg(p4 + 3);
-    const float lb[6] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y};
-    const float rb[6] = {q1.z, q1.w, q2.x, q2.y, q2.z, q2.w};
-    const uint32_t L = __float_as_uint(q3.x), R = __float_as_uint(q3.y);
-    uint32_t next = CLV_REF_EMPTY;
-    const float* nbox = nullptr;
-    if (L != CLV_REF_EMPTY && R != CLV_REF_EMPTY) {
-      float ld, rd;
-      const bool lh = box_distance(lb, r.o, r.d, ld), rh = box_distance(rb, r.o, r.d, rd);
-      if (lh && rh) {
-        const float far_d = fmaxf(ld, rd);
-        const bool left_first = ld < rd;
-        next = left_first ? L : R;
-        nbox = left_first ? lb : rb;
-        const uint32_t far = left_first ? R : L;
-        const float* fbox = left_first ? rb : lb;
-        if (sp >= CLV_STACK) {
-          if (err) atomicOr(err, CLV_ERR_STACK);
-          return hit.ref != CLV_REF_EMPTY;
+    bool descend = false;
+    if (CLV_REF_KIND(ref) == CLV_REF_NODE) {
+      if (cnt) cnt->nodes++;
+      if (slab_pass(N, F, tmin, tmax)) {
+        const float4* p4 = reinterpret_cast<const float4*>(S.nodes + CLV_REF_INDEX(ref));
+        const float4 q0 = __ldg(p4), q1 = __ldg(p4 + 1), q2 = __ldg(p4 + 2), q3 = __ldg(p4 + 3);
+        const float lb[6] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y};
+        const float rb[6] = {q1.z, q1.w, q2.x, q2.y, q2.z, q2.w};
+        const uint32_t L = __float_as_uint(q3.x), Rr = __float_as_uint(q3.y);
+        uint32_t next = CLV_REF_EMPTY;
+        bool left_next = true;
+        if (L != CLV_REF_EMPTY && Rr != CLV_REF_EMPTY) {
+          float ld, rd;
+          const bool lh = box_distance_pre(lb, R, ld), rh = box_distance_pre(rb, R, rd);
+          if (lh && rh) {
+            left_next = ld < rd;
+            next = left_next ? L : Rr;
+            const uint32_t far = left_next ? Rr : L;
+            float fN = 0.0f, fF = 0.0f;
+            if (CLV_REF_KIND(far) == CLV_REF_NODE) {
+              float fb[6];
+#pragma unroll
+              for (int k = 0; k < 6; ++k) fb[k] = left_next ? rb[k] : lb[k];
+              slab(fb, r.o, R.inv, fN, fF);
+            }
+            if (sp < CLV_STACK) {
+              stack[sp++] = make_float4(__uint_as_float(far), fmaxf(ld, rd), fN, fF);
+            } else if (err) {
+              atomicOr(err, CLV_ERR_STACK);
+            }
+          } else if (lh) {
+            next = L;
+          } else if (rh) {
+            next = Rr;
+            left_next = false;
+          }
+        } else if (L != CLV_REF_EMPTY) {
+          next = L;
+        } else if (Rr != CLV_REF_EMPTY) {
+          next = Rr;
+          left_next = false;
         }
-        StackEntry& e = stack[sp++];
-        e.ref = far;
-        e.hits = hits;
-        e.far_d = far_d;
-        if (CLV_REF_KIND(far) == CLV_REF_NODE) slab(fbox, r.o, inv, e.N, e.F);
-      } else if (lh) {
-        next = L;
-        nbox = lb;
-      } else if (rh) {
-        next = R;
-        nbox = rb;
-      }
-    } else if (L != CLV_REF_EMPTY) {
-      next = L;
-      nbox = lb;
-    } else if (R != CLV_REF_EMPTY) {
-      next = R;
-      nbox = rb;
-    }
-    // descend into `next` (or pop deferred far children)
-    while (true) {
-      if (next != CLV_REF_EMPTY) {
-        if (CLV_REF_KIND(next) == CLV_REF_NODE) {
-          if (cnt) cnt->nodes++;
-          float N, F;
-          if (nbox) slab(nbox, r.o, inv, N, F);
-          else { N = stack[sp].N; F = stack[sp].F; }
-          if (slab_pass(N, F, tmin, tmax)) break;  // continue at node `next`
-        } else if (leaf_test(S, next, r, tmin, tmax, rng, hit, cnt, err)) {
-          tmax = hit.t;
-          ++hits;
+        if (next != CLV_REF_EMPTY) {
+          if (CLV_REF_KIND(next) == CLV_REF_NODE) {
+            float nb[6];
+#pragma unroll
+            for (int k = 0; k < 6; ++k) nb[k] = left_next ? lb[k] : rb[k];
+            slab(nb, r.o, R.inv, N, F);
+          }
+          ref = next;
+          descend = true;
         }
       }
-      // pop
-      next = CLV_REF_EMPTY;
-      while (sp > 0) {
-        const StackEntry& e = stack[--sp];
-        if (hits > e.hits && hit.t < e.far_d) continue;  // near subtree hit closer than far box
-        next = e.ref;
-        nbox = nullptr;  // own-box slab of a popped node is stack[sp]
-        break;
+    } else {
+      if (leaf_test<COMPLEX>(S, ref, r, tmin, tmax, rng, hit, full, cnt, err)) {
+        tmax = hit.t;
+        found = true;
+        marked = sp;
       }
-      if (next == CLV_REF_EMPTY) return hit.ref != CLV_REF_EMPTY;
     }
-    cur = next;
+    if (descend) continue;
+    // pop the next deferred far child whose visit the reference would make
+    bool popped = false;
+    while (sp > 0) {
+      --sp;
+      const float4 e = stack[sp];
+      const bool near_hit = sp < marked;
+      if (marked > sp) marked = sp;
+      if (near_hit && hit.t < e.y) continue;  // near subtree's hit is closer than the far box
+      ref = __float_as_uint(e.x);
+      N = e.z;
+      F = e.w;
+      popped = true;
+      break;
+    }
+    if (!popped) break;
   }
+  return found;
 }
 
 // Full record of the closest hit (deterministic rebuild for primitives).
-__device__ __forceinline__ void hit_record(const ClvDeviceScene& S, const Ray& r, const Hit& h, Rec& rec) {
+__device__ __forceinline__ void hit_record(const ClvDeviceScene& S, const Ray& r, const Hit& h, const Rec& full,
+                                           Rec& rec) {
   const uint32_t kind = CLV_REF_KIND(h.ref), idx = CLV_REF_INDEX(h.ref);
   if (kind == CLV_REF_TRI || kind == CLV_REF_QUAD) {
     float f[16];
@@ -568,7 +628,7 @@ __device__ __forceinline__ void hit_record(const ClvDeviceScene& S, const Ray& r
     sphere_record(mk(s.x, s.y, s.z), s.w, r, h.t, rec);
     rec.mat = S.sphere_mat[idx];
   } else {
-    rec = h.full;
+    rec = full;
   }
 }
 __device__ __forceinline__ uint32_t hit_gid(const ClvDeviceScene& S, uint32_t ref) {

@@ -52,7 +52,9 @@ typedef struct clv_render_opts {
   uint32_t sampler;             /* 0 = random (default); 1 = blue noise: unsupported */
   uint64_t seed;                /* stream seed; identical seeds give identical images */
   uint32_t sample_offset;       /* index of the first sample (progressive rendering) */
-  uint32_t samples_per_thread;  /* 0 = automatic */
+  uint32_t samples_per_thread;  /* megakernel only: samples per thread, 0 = automatic */
+  uint32_t engine;              /* 0 = wavefront (default), 1 = single megakernel */
+  uint32_t path_slots;          /* wavefront paths in flight, 0 = automatic */
 } clv_render_opts;
 
 typedef struct clv_scene_info {
@@ -106,7 +108,9 @@ void clv_device_scene_free(clv_device_scene* dscene);
 int clv_render(clv_device_scene* dscene, const clv_render_opts* opts, float* xyz_out, clv_stats* stats);
 
 /* Device variant: ADDS the per-pixel sums of film deposits (f64, not divided
- * by spp) into film_dev (width*height*3 doubles, caller-zeroed), on `stream`. */
+ * by spp) into film_dev (width*height*3 doubles, caller-zeroed), on `stream`.
+ * The wavefront engine polls a live-path counter from the host, so the call
+ * returns once the film is complete. */
 int clv_render_device(clv_device_scene* dscene, const clv_render_opts* opts, double* film_dev, void* stream);
 
 /* Film resolve (clovers-cli/src/write.rs:39-44): mean = film / spp (f64) ->
@@ -141,6 +145,12 @@ int clv_device_status(clv_device_scene* dscene, uint32_t* flags_out);
 
 const char* clv_last_error(void);
 const char* clv_version(void);
+
+/* ---- diagnostics (no counterpart in the reference) ----------------------- */
+
+/* Checks the traversal's fast slab division (reciprocal + one FMA correction)
+ * against IEEE division on n random operand pairs; mismatches must be 0. */
+int clv_selftest_division(uint64_t n, uint64_t seed, uint64_t* mismatches);
 
 #ifdef __cplusplus
 }

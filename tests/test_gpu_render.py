@@ -27,20 +27,21 @@ def relmse(img, ref, eps=1e-2):
     return float(np.mean((img - ref) ** 2 / (ref ** 2 + eps)))
 
 
-def _render(path, w, h, spp, depth, seed, **kw):
+def _render(path, w, h, spp, depth, seed, engine="wavefront", **kw):
     d = cg.Scene.from_json(path, w, h).upload()
     opts = cg.RenderOptions(input=path, width=w, height=h, samples=spp, max_depth=depth, seed=seed, **kw)
     stats = {}
-    img = cg.draw(cg.GlobalOptions(quiet=True), opts, d, stats=stats)
+    img = cg.draw(cg.GlobalOptions(quiet=True), opts, d, stats=stats, engine=engine)
     assert stats["device_errors"] == 0
     return img.astype(np.float64), stats
 
 
+@pytest.mark.parametrize("engine", ["wavefront", "megakernel"])
 @pytest.mark.parametrize("scene_fixture,w,h,spp,depth", [("box_scene_path", 48, 48, 32, 16),
                                                          ("spheres_scene_path", 64, 36, 16, 50)])
-def test_same_seed_matches_oracle(request, scene_fixture, w, h, spp, depth):
+def test_same_seed_matches_oracle(request, scene_fixture, w, h, spp, depth, engine):
     path = request.getfixturevalue(scene_fixture)
-    img, stats = _render(path, w, h, spp, depth, seed=1234)
+    img, stats = _render(path, w, h, spp, depth, seed=1234, engine=engine)
     ref = oracle.Scene.from_json(path, w, h).render(w, h, spp, depth, seed=1234) / spp
     assert stats["samples"] == w * h * spp
     err = relmse(img, ref)
