@@ -1,0 +1,409 @@
+"""Benchmark of the clovers render hot path on GB300.
+
+Workload (one step): the enclosed-box scene (a 555-unit box in the layout of
+the reference's cornell.json: five diffuse walls, a 130x105 area light, two
+rotated boxes, a glass sphere) rendered at 512x512, 256 samples per pixel,
+max depth 16, by the wavefront path tracer: 67,108,864 samples per step.
+Metric: Msamples/s = width*height*spp / GPU seconds (whole job over all ranks).
+
+Also reported: the closest-hit ray-cast workload of the same configuration
+(2^24 seeded random rays against an SAH BVH over 2^20 random triangles),
+as traversal Grays/s with its HBM roofline.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+`--impl reference` times the reference's algorithm on the host cores instead:
+the reference (Rust) cannot be built here, so its CPU restatement (oracle/)
+runs the same workload, row-parallel over all host threads like the
+reference's rayon loop, on a bounded sample of samples per pixel.
+"""
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+W_IMG, H_IMG, SPP, DEPTH = 512, 512, 256, 16
+RAYS, TRIS = 1 << 24, 1 << 20
+SEED = 1
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """Per-launch DRAM bytes from the committed ncu summary (profiles/traffic.txt), if present."""
+    out = {}
+    path = os.path.join(ROOT, "profiles", "traffic.txt")
+    if os.path.exists(path):
+        for line in open(path):
+            line = line.strip()
+            if line and not line.startswith("#") and "=" in line:
+                k, v = line.split("=", 1)
+                try:
+                    out[k.strip()] = float(v)
+                except ValueError:
+                    pass
+    return out
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    FIELDS = ["clocks.sm", "clocks.max.sm", "clocks_event_reasons.active", "clocks_event_reasons.hw_slowdown",
+              "clocks_event_reasons.hw_thermal_slowdown", "clocks_event_reasons.sw_thermal_slowdown",
+              "clocks_event_reasons.sw_power_cap"]
+
+    def __init__(self, gpu_index):
+        self.gpu_index = gpu_index
+        self.proc = None
+        self.tmp = None
+
+    def __enter__(self):
+        try:
+            self.tmp = tempfile.NamedTemporaryFile("w+", delete=False, suffix=".csv")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu_index), "--query-gpu=" + ",".join(self.FIELDS),
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.tmp, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or self.tmp is None:
+            return None
+        try:
+            self.tmp.flush()
+            rows = [l.strip().split(", ") for l in open(self.tmp.name) if l.strip()]
+            os.unlink(self.tmp.name)
+        except Exception:
+            return None
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            if len(r) < 7:
+                continue
+            try:
+                sm.append(float(r[0]))
+                mx.append(float(r[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, r[3:7]):
+                if v.strip().lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        backend = "nccl" if args.impl != "reference" else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def all_max(world, value):
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def box_scene_file():
+    from clovers_gb300 import scenes
+    path = os.path.join(tempfile.gettempdir(), "clovers_bench_box_%d.json" % os.getpid())
+    scenes.write_scene(scenes.enclosed_box(), path)
+    return path
+
+
+def run_reference(args, world, rank):
+    """The reference algorithm (CPU restatement) on the host cores, same workload, bounded sample."""
+    if rank != 0:
+        return
+    import oracle
+    threads = os.cpu_count() or 1
+    path = box_scene_file()
+    sc = oracle.Scene.from_json(path, W_IMG, H_IMG)
+    spp_sample = args.cpu_spp
+    for i in range(args.warmup):
+        sc.render(W_IMG, H_IMG, 1, DEPTH, SEED, window=(0, 0, W_IMG, 16), threads=threads)
+    times = []
+    for k in range(args.steps):
+        t0 = time.perf_counter()
+        sc.render(W_IMG, H_IMG, spp_sample, DEPTH, SEED, sample_offset=k * spp_sample, threads=threads)
+        times.append(time.perf_counter() - t0)
+    samples = W_IMG * H_IMG * spp_sample
+    value = samples * len(times) / sum(times) / 1e6
+    sample = "512x512 image at %d spp per step (of the workload's 256 spp)" % spp_sample
+    line = {
+        "impl": "reference", "metric": "Msamples/s", "value": round(value, 4), "unit": "Msamples/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1e3 * sum(times) / len(times), 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded enclosed-box scene)",
+        "config": {"workload": "enclosed box 512x512, 256 spp, depth 16", "sample": sample, "parallelism": "host threads"},
+        "cpu_baseline": {"value": round(value, 4), "unit": "Msamples/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": round(value, 4), "unit": "Msamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference is Rust and cannot be built here (no rustc/cargo); its algorithm runs as the "
+                "C++ restatement in oracle/, row-parallel over all host threads",
+    }
+    print(json.dumps(line), flush=True)
+    os.unlink(path)
+
+
+def cpu_baseline_render(path, spp_sample):
+    import oracle
+    threads = os.cpu_count() or 1
+    sc = oracle.Scene.from_json(path, W_IMG, H_IMG)
+    sc.render(W_IMG, H_IMG, 1, DEPTH, SEED, window=(0, 0, W_IMG, 8), threads=threads)  # warm-up
+    t0 = time.perf_counter()
+    sc.render(W_IMG, H_IMG, spp_sample, DEPTH, SEED, threads=threads)
+    el = time.perf_counter() - t0
+    return {"value": round(W_IMG * H_IMG * spp_sample / el / 1e6, 4), "unit": "Msamples/s", "cores": threads,
+            "kind": "port", "sample": "512x512 at %d spp (%.2f s)" % (spp_sample, el)}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-spp", type=int, default=2, help="samples per pixel of the CPU baseline sample")
+    ap.add_argument("--no-traversal", action="store_true", help="skip the ray-cast section")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline legs")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    world, rank, local = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+        return
+
+    import torch
+    import clovers_gb300 as cg
+    from clovers_gb300 import _lib, scenes
+
+    torch.cuda.set_device(local)
+    L = _lib.lib()
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    hbm_peak, peak_kind = measured_peaks()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > 129 MB L2
+
+    # ---------------------------------------------------------------- render
+    path = box_scene_file()
+    host_scene = cg.Scene.from_json(path, W_IMG, H_IMG)
+    dscene = host_scene.upload()
+    npix = W_IMG * H_IMG
+    film = torch.zeros(npix * 3, dtype=torch.float64, device="cuda")
+
+    def opts_for(step):
+        o = cg.render_opts(cg.RenderOptions(width=W_IMG, height=H_IMG, samples=SPP, max_depth=DEPTH, seed=SEED))
+        o.sample_offset = (rank * 1000003 + step) * SPP  # weak scaling: every rank renders its own samples
+        return o
+
+    for w in range(args.warmup):
+        film.zero_()
+        _lib.check(L.clv_render_device(dscene.handle, ctypes.byref(opts_for(10**6 + w)), film.data_ptr(), sp))
+    torch.cuda.synchronize()
+    launches0 = L.clv_kernel_launches()
+    gpu_index = os.environ.get("CUDA_VISIBLE_DEVICES", str(local)).split(",")[local if world > 1 else 0]
+    step_ms = []
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(gpu_index) as clocks:
+        wall0 = time.perf_counter()
+        for k in range(args.steps):
+            film.zero_()
+            flush.zero_()  # L2 flush between timed steps
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            _lib.check(L.clv_render_device(dscene.handle, ctypes.byref(opts_for(k)), film.data_ptr(), sp))
+            e1.record(stream)
+            e1.synchronize()
+            step_ms.append(e0.elapsed_time(e1))
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - wall0
+    barrier(world)
+    launches = L.clv_kernel_launches() - launches0
+    ms_step = all_max(world, sum(step_ms) / len(step_ms))
+    samples_step = npix * SPP
+    value = world * samples_step / (ms_step / 1e3) / 1e6
+
+    # e2e: through the host-buffer C ABI (scene upload + render + image download), every step
+    xyz = np.empty((npix, 3), np.float32)
+    host_opts = opts_for(0)
+    e2e_times = []
+    st = _lib.StatsC()
+    h2d = 0
+    for k in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        d2 = host_scene.upload()
+        host_opts.sample_offset = (rank * 1000003 + 5000 + k) * SPP
+        _lib.check(L.clv_render(d2.handle, ctypes.byref(host_opts), xyz.ctypes.data, ctypes.byref(st)))
+        e2e_times.append(time.perf_counter() - t0)
+        d2.close()
+    info = host_scene.info()
+    # bytes the upload copies (nodes, records, materials, spectral tables, illuminants, CMF)
+    h2d = (info["nodes"] * 64 + info["triangles"] * 64 + info["quads"] * 64 + info["spheres"] * 16 +
+           info["compound"] * 64 + info["materials"] * 112 + 38 * 400 * 4 + 400 * 12)
+    e2e_s = all_max(world, sum(e2e_times) / len(e2e_times))
+    e2e_value = world * samples_step / e2e_s / 1e6
+
+    # profiling pass (untimed): per-kernel device time and traversal counts for the roofline
+    prof = _lib.RenderProfileC()
+    film.zero_()
+    _lib.check(L.clv_render_profile_run(dscene.handle, ctypes.byref(opts_for(777)), film.data_ptr(), sp,
+                                        ctypes.byref(prof)))
+    torch.cuda.synchronize()
+    segs = prof.path_segments
+    # algorithmic bytes per closest-hit query (one per bounce of a live path):
+    #   intersect: reads meta + origin + direction (48 B), writes the hit (16 B) and a queue entry (4 B),
+    #              and fetches one 64-B node per BVHNode::hit call and one 64-B record per primitive test;
+    #   shade (specular/diffuse/finish): reads the queue entry (4 B), path state + hit (88 B) and writes
+    #              the next state (64 B) per query; per sample 80 B read at the end, 24 B of film and
+    #              72 B for the regenerated path.
+    isect_bytes = segs * (48 + 16 + 4) + 64 * (prof.node_visits + prof.prim_tests)
+    shade_bytes = segs * (4 + 88 + 64) + prof.paths * (80 + 24 + 72)
+    kernels = {"wf_intersect": (prof.ms_intersect, isect_bytes, prof.intersect_launches),
+               "wf_shade": (prof.ms_shade, shade_bytes, prof.shade_launches)}
+    dom = max(kernels, key=lambda k: kernels[k][0])
+    d_ms, d_bytes, d_launches = kernels[dom]
+    achieved = d_bytes / (d_ms / 1e3) / 1e9
+    traffic = ncu_traffic()
+    roofline = {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",
+                "frac": round(achieved / hbm_peak, 4), "peak_kind": peak_kind,
+                "traffic": traffic.get(dom + ".bytes_per_launch"),
+                "algorithmic_bytes_per_launch": round(d_bytes / max(1, d_launches)),
+                "kernel_ms_per_step": {k: round(v[0], 3) for k, v in kernels.items()},
+                "path_segments": segs, "node_visits": prof.node_visits, "prim_tests": prof.prim_tests}
+
+    line = {
+        "metric": "Msamples/s", "value": round(value, 3), "unit": "Msamples/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded enclosed-box scene in the reference's scene format)",
+        "config": {"workload": "enclosed box 512x512, 256 spp, depth 16 (wavefront engine)",
+                   "samples_per_step": samples_step, "l2": "flushed between steps (256 MiB write)",
+                   "parallelism": "replicas" if world > 1 else "single GPU", "wall_s_timed_loop": round(wall, 3)},
+        "e2e": {"value": round(e2e_value, 3), "unit": "Msamples/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(npix * 3 * 4)},
+        "gpu_launches": int(launches),
+        "roofline": roofline,
+        "clocks": clocks.summary(),
+    }
+
+    # ------------------------------------------------------------- ray casts
+    if not args.no_traversal:
+        v, idx = scenes.triangle_soup(TRIS, seed=2)
+        mesh = cg.Scene.from_mesh(v, idx)
+        dm = mesh.upload()
+        rays_h = scenes.random_rays(RAYS, seed=3)
+        rays = torch.from_numpy(rays_h).cuda()
+        prim = torch.empty(RAYS, dtype=torch.int32, device="cuda")
+        tt = torch.empty(RAYS, dtype=torch.float32, device="cuda")
+        for _ in range(args.warmup):
+            _lib.check(L.clv_raycast_device(dm.handle, rays.data_ptr(), RAYS, prim.data_ptr(), tt.data_ptr(),
+                                            None, None, sp))
+        ms = []
+        torch.cuda.synchronize()
+        for _ in range(args.steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            _lib.check(L.clv_raycast_device(dm.handle, rays.data_ptr(), RAYS, prim.data_ptr(), tt.data_ptr(),
+                                            None, None, sp))
+            e1.record(stream)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        r_ms = all_max(world, sum(ms) / len(ms))
+        nodes = torch.empty(RAYS, dtype=torch.int32, device="cuda")
+        tests = torch.empty(RAYS, dtype=torch.int32, device="cuda")
+        _lib.check(L.clv_raycast_device(dm.handle, rays.data_ptr(), RAYS, prim.data_ptr(), tt.data_ptr(),
+                                        nodes.data_ptr(), tests.data_ptr(), sp))
+        torch.cuda.synchronize()
+        nv = int(nodes.sum(dtype=torch.int64).item())
+        pt = int(tests.sum(dtype=torch.int64).item())
+        rbytes = RAYS * (32 + 8) + 64 * (nv + pt)
+        r_ach = rbytes / (r_ms / 1e3) / 1e9
+        # e2e ray casts: host rays in, host ids/distances out
+        t0 = time.perf_counter()
+        cg.raycast(dm, rays_h)
+        r_e2e = time.perf_counter() - t0
+        trav = {"workload": "2^24 random rays vs 2^20 random triangles (SAH BVH, closest hit)",
+                "metric": "Grays/s", "value": round(RAYS / (r_ms / 1e3) / 1e9, 4), "ms_per_step": round(r_ms, 3),
+                "e2e": {"value": round(RAYS / r_e2e / 1e9, 4), "unit": "Grays/s", "h2d_bytes_per_step": RAYS * 32,
+                        "d2h_bytes_per_step": RAYS * 8},
+                "nodes_per_ray": round(nv / RAYS, 2), "prims_per_ray": round(pt / RAYS, 2),
+                "roofline": {"kernel": "raycast_kernel", "bound": "hbm", "achieved": round(r_ach, 1),
+                             "peak": hbm_peak, "unit": "GB/s", "frac": round(r_ach / hbm_peak, 4),
+                             "traffic": traffic.get("raycast_kernel.bytes_per_launch"),
+                             "algorithmic_bytes_per_launch": int(rbytes)}}
+        if rank == 0 and world == 1 and not args.no_cpu:
+            import oracle
+            om = oracle.Scene.from_mesh(v, idx)
+            n_cpu = 1 << 17
+            t0 = time.perf_counter()
+            om.raycast(rays_h[:n_cpu], threads=os.cpu_count() or 1)
+            el = time.perf_counter() - t0
+            trav["cpu_baseline"] = {"value": round(n_cpu / el / 1e9, 6), "unit": "Grays/s",
+                                    "cores": os.cpu_count() or 1, "kind": "port",
+                                    "sample": "first %d of the 2^24 rays (%.2f s)" % (n_cpu, el)}
+        line["traversal"] = trav
+
+    if rank == 0 and world == 1 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline_render(path, args.cpu_spp)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    os.unlink(path)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

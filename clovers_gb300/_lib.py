@@ -35,6 +35,12 @@ class StatsC(ctypes.Structure):
     _fields_ = [("gpu_ms", c_f64), ("samples", c_u64), ("device_errors", c_u32), ("kernel_launches", c_u32)]
 
 
+class RenderProfileC(ctypes.Structure):
+    _fields_ = [("ms_init", c_f64), ("ms_intersect", c_f64), ("ms_shade", c_f64), ("intersect_launches", c_u64),
+                ("shade_launches", c_u64), ("paths", c_u64), ("path_segments", c_u64), ("node_visits", c_u64),
+                ("prim_tests", c_u64), ("path_slots", c_u64)]
+
+
 # name -> (restype, argtypes); mirrors include/clovers_gpu.h
 SIGNATURES = {
     "clv_scene_load_json": (c_i32, [ctypes.c_char_p, c_u32, c_u32, c_i32, P(ctypes.c_void_p)]),
@@ -56,6 +62,9 @@ SIGNATURES = {
                                    ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "clv_device_status": (c_i32, [ctypes.c_void_p, P(c_u32)]),
     "clv_selftest_division": (c_i32, [c_u64, c_u64, P(c_u64)]),
+    "clv_kernel_launches": (c_u64, []),
+    "clv_render_profile_run": (c_i32, [ctypes.c_void_p, P(RenderOptsC), ctypes.c_void_p, ctypes.c_void_p,
+                                       P(RenderProfileC)]),
     "clv_last_error": (ctypes.c_char_p, []),
     "clv_version": (ctypes.c_char_p, []),
 }

@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -27,7 +28,7 @@ using namespace clvd;
 
 // ------------------------------------------------------------------ kernels --
 
-template <bool COMPLEX>
+template <int CPLX>
 __global__ void __launch_bounds__(128) raycast_kernel(ClvDeviceScene S, const float4* __restrict__ rays, uint64_t n,
                                                       uint32_t* __restrict__ prim, float* __restrict__ tout,
                                                       uint32_t* __restrict__ nodes, uint32_t* __restrict__ tests,
@@ -41,7 +42,7 @@ __global__ void __launch_bounds__(128) raycast_kernel(ClvDeviceScene S, const fl
     Counters c{0u, 0u};
     Rng rng;
     rng.init(0, (uint32_t)i, 0);
-    const bool any = closest_hit<COMPLEX>(S, r, a.w, b.w, &rng, h, nullptr, want ? &c : nullptr, err);
+    const bool any = closest_hit<CPLX>(S, r, a.w, b.w, &rng, h, nullptr, want ? &c : nullptr, err);
     __stcs(prim + i, any ? hit_gid(S, h.ref) : 0xFFFFFFFFu);
     __stcs(tout + i, any ? h.t : 0.0f);
     if (want) {
@@ -96,7 +97,7 @@ __device__ void trace_path(const ClvDeviceScene& S, Ray ray, uint32_t max_depth,
     if (depth > max_depth) break;
     Hit h;
     Rec full;
-    if (!closest_hit<true>(S, ray, CLV_EPS_ACNE, CLV_FLT_MAX, &rng, h, &full, nullptr, err)) {
+    if (!closest_hit<2>(S, ray, CLV_EPS_ACNE, CLV_FLT_MAX, &rng, h, &full, nullptr, err)) {
 #pragma unroll
       for (int i = 0; i < 4; ++i) L[i] += beta[i] * spd_get(S, S.background_spd, waves[i]);
       break;
@@ -259,7 +260,7 @@ __global__ void debug_kernel(ClvDeviceScene S, RenderParams P, double* __restric
   Hit h;
   Rec full;
   Counters c{0u, 0u};
-  const bool any = closest_hit<true>(S, r, CLV_EPS_ACNE, CLV_FLT_MAX, &rng, h, &full, &c, err);
+  const bool any = closest_hit<2>(S, r, CLV_EPS_ACNE, CLV_FLT_MAX, &rng, h, &full, &c, err);
   if (P.mode == CLV_MODE_NORMAL_MAP) {  // normals.rs:11-37
     if (any) {
       Rec rec;
@@ -343,6 +344,7 @@ __global__ void selftest_division_kernel(uint64_t n, uint64_t seed, unsigned lon
 namespace {
 
 thread_local std::string g_error;
+std::atomic<unsigned long long> g_launches{0};
 
 int fail(int code, const std::string& msg) {
   g_error = msg;
@@ -383,6 +385,28 @@ struct clv_scene {
   clv::HostScene host;
 };
 
+// Which traversal variant the scene needs: 0 primitives only, 1 wrapper
+// chains handled inline (chain_hit), 2 media or lists (interpreter).
+static uint32_t compound_level(const clv::HostScene& h) {
+  if (h.objs.empty()) return 0;
+  for (size_t i = 0; i < h.objs.size(); ++i) {
+    const ClvObj& o = h.objs[i];
+    if (o.kind == CLV_OBJ_MEDIUM || o.kind == CLV_OBJ_LIST) return 2;
+    if (o.kind == CLV_OBJ_TRANSLATE || o.kind == CLV_OBJ_ROTATEY) {
+      int depth = 0;
+      uint32_t r = CLV_MAKE_REF(CLV_REF_OBJ, i);
+      while (CLV_REF_KIND(r) == CLV_REF_OBJ) {
+        const ClvObj& w = h.objs[CLV_REF_INDEX(r)];
+        if (w.kind != CLV_OBJ_TRANSLATE && w.kind != CLV_OBJ_ROTATEY) break;
+        ++depth;
+        r = w.a;
+      }
+      if (depth > CLV_CHAIN) return 2;
+    }
+  }
+  return 1;
+}
+
 struct clv_device_scene {
   ClvDeviceScene view{};
   std::vector<void*> owned;
@@ -421,15 +445,15 @@ struct clv_device_scene {
     W.o_time = reinterpret_cast<float4*>(p); p += n * 16;
     W.d_lambda = reinterpret_cast<float4*>(p); p += n * 16;
     W.beta = reinterpret_cast<float4*>(p); p += n * 16;
-    W.L = reinterpret_cast<float4*>(p); p += n * 16;
     W.meta = reinterpret_cast<uint4*>(p); p += n * 16;
     W.hit = reinterpret_cast<float4*>(p); p += n * 16;
     W.full = reinterpret_cast<float4*>(p); p += n * 48;
-    W.key = reinterpret_cast<uint2*>(p);
+    W.key = reinterpret_cast<uint2*>(p); p += n * 8;
+    W.queue = reinterpret_cast<uint32_t*>(p);
     W.Q = q;
     return W;
   }
-  static constexpr size_t kWfSlotBytes = 16 * 6 + 48 + 8;
+  static constexpr size_t kWfSlotBytes = 16 * 5 + 48 + 8 + 12;
   void* ensure_scratch(size_t bytes) {
     if (bytes > scratch_bytes) {
       if (scratch) cudaFree(scratch);
@@ -487,6 +511,21 @@ extern "C" {
 
 const char* clv_last_error(void) { return g_error.c_str(); }
 const char* clv_version(void) { return "clovers_gb300 0.1 (sm_103a)"; }
+
+uint64_t clv_kernel_launches(void) { return g_launches.load(); }
+
+static int render_wavefront(clv_device_scene* d, const clv_render_opts* o, double* film, cudaStream_t st,
+                            clv_render_profile* prof);
+
+int clv_render_profile_run(clv_device_scene* d, const clv_render_opts* o, double* film_dev, void* stream,
+                           clv_render_profile* out) {
+  int rc = check_opts(d, o);
+  if (rc) return rc;
+  if (!film_dev || !out) return fail(CLV_E_INVALID, "null argument");
+  if (o->mode != CLV_MODE_PATH_TRACING || o->engine != 0)
+    return fail(CLV_E_INVALID, "profiling covers the wavefront path tracer only");
+  return render_wavefront(d, o, film_dev, (cudaStream_t)stream, out);
+}
 
 int clv_selftest_division(uint64_t n, uint64_t seed, uint64_t* mismatches) {
   if (!mismatches) return fail(CLV_E_INVALID, "null argument");
@@ -612,6 +651,7 @@ int clv_scene_upload(const clv_scene* s, clv_device_scene** out) {
     v.n_objs = (uint32_t)h.objs.size();
     v.n_materials = (uint32_t)h.materials.size();
     v.max_depth_tree = h.tree_depth;
+    v.compound_level = compound_level(h);
     v.mis_depth = h.mis_depth;
     v.camera = h.camera;
     ck(cudaMalloc(&d->err, sizeof(uint32_t)), "cudaMalloc");
@@ -645,12 +685,15 @@ int clv_raycast_device(const clv_device_scene* d, const float* rays_dev, uint64_
   if (n == 0) return CLV_OK;
   if ((reinterpret_cast<uintptr_t>(rays_dev) & 15u) != 0) return fail(CLV_E_INVALID, "rays must be 16-byte aligned");
   const int block = 128;
-  if (d->view.n_objs)
-    raycast_kernel<true><<<launch_grid(n, block), block, 0, (cudaStream_t)stream>>>(
-        d->view, reinterpret_cast<const float4*>(rays_dev), n, prim_dev, t_dev, nodes_dev, tests_dev, d->err);
-  else
-    raycast_kernel<false><<<launch_grid(n, block), block, 0, (cudaStream_t)stream>>>(
-        d->view, reinterpret_cast<const float4*>(rays_dev), n, prim_dev, t_dev, nodes_dev, tests_dev, d->err);
+  g_launches += 1;
+  const uint32_t grid = launch_grid(n, block);
+  const float4* r4 = reinterpret_cast<const float4*>(rays_dev);
+  cudaStream_t st = (cudaStream_t)stream;
+  switch (d->view.compound_level) {
+    case 0: raycast_kernel<0><<<grid, block, 0, st>>>(d->view, r4, n, prim_dev, t_dev, nodes_dev, tests_dev, d->err); break;
+    case 1: raycast_kernel<1><<<grid, block, 0, st>>>(d->view, r4, n, prim_dev, t_dev, nodes_dev, tests_dev, d->err); break;
+    default: raycast_kernel<2><<<grid, block, 0, st>>>(d->view, r4, n, prim_dev, t_dev, nodes_dev, tests_dev, d->err);
+  }
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail(CLV_E_CUDA, std::string("raycast launch: ") + cudaGetErrorString(e));
   return CLV_OK;
@@ -688,7 +731,18 @@ int clv_raycast(clv_device_scene* d, const float* rays, uint64_t n, uint32_t* pr
   }
 }
 
-static int render_wavefront(clv_device_scene* d, const clv_render_opts* o, double* film, cudaStream_t st) {
+// Wavefront render loop.  With `prof` set, each intersect and shade launch is
+// bracketed by events and the traversal work is counted (diagnostic runs).
+static int render_wavefront(clv_device_scene* d, const clv_render_opts* o, double* film, cudaStream_t st,
+                            clv_render_profile* prof) {
+  std::vector<cudaEvent_t> evs;
+  unsigned long long* dcnt = nullptr;
+  auto cleanup = [&]() {
+    for (cudaEvent_t e : evs) cudaEventDestroy(e);
+    evs.clear();
+    if (dcnt) cudaFree(dcnt);
+    dcnt = nullptr;
+  };
   try {
     WfParams P;
     P.width = o->width;
@@ -702,31 +756,84 @@ static int render_wavefront(clv_device_scene* d, const clv_render_opts* o, doubl
     q = std::min<uint64_t>(q, P.total);
     q = (q + 127) / 128 * 128;
     WfState W = d->wavefront_state((uint32_t)q);
-    WfCounters c0{std::min<uint64_t>(q, P.total), 0u, 0u};
+    WfCounters c0{std::min<uint64_t>(q, P.total), 0u, {0u, 0u, 0u}};
     ck(cudaMemcpyAsync(d->wf_counters, &c0, sizeof c0, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync");
     const int block = 128;
     const uint32_t grid = (uint32_t)((q + block - 1) / block);
+    const uint32_t level = d->view.compound_level;
+    const int batch = 8;  // bounces between polls of the live-path counter
+    WfCounters* C = d->wf_counters;
+    // shading kernels walk their queues with a grid-stride loop over a fixed grid
+    const uint32_t qgrid = std::min<uint32_t>(grid, (uint32_t)sm_count() * 16);
+    if (prof) {
+      std::memset(prof, 0, sizeof *prof);
+      ck(cudaMalloc(&dcnt, 3 * sizeof(unsigned long long)), "cudaMalloc");
+      ck(cudaMemsetAsync(dcnt, 0, 3 * sizeof(unsigned long long), st), "cudaMemsetAsync");
+      evs.resize(4 * batch + 2);
+      for (auto& e : evs) ck(cudaEventCreate(&e), "cudaEventCreate");
+      ck(cudaEventRecord(evs[4 * batch], st), "cudaEventRecord");
+    }
     wf_init<<<grid, block, 0, st>>>(d->view, P, W);
-    const bool complex = d->view.n_objs != 0;
-    // a path lives at most max_depth + 1 bounces; the live counter is polled every `batch` bounces
-    const int batch = 8;
+    g_launches += 1;
+    if (prof) {
+      ck(cudaEventRecord(evs[4 * batch + 1], st), "cudaEventRecord");
+      ck(cudaEventSynchronize(evs[4 * batch + 1]), "cudaEventSynchronize");
+      float ms = 0.0f;
+      cudaEventElapsedTime(&ms, evs[4 * batch], evs[4 * batch + 1]);
+      prof->ms_init = ms;
+    }
     for (uint64_t it = 0;; it += batch) {
       for (int k = 0; k < batch; ++k) {
-        cudaMemsetAsync(&d->wf_counters->live, 0, sizeof(unsigned int), st);
-        if (complex) wf_intersect<true><<<grid, block, 0, st>>>(d->view, W, d->err);
-        else wf_intersect<false><<<grid, block, 0, st>>>(d->view, W, d->err);
-        wf_shade<<<grid, block, 0, st>>>(d->view, P, W, d->wf_counters, film, d->err);
+        cudaMemsetAsync(&d->wf_counters->live, 0, 4 * sizeof(unsigned int), st);  // live + 3 queue lengths
+        if (prof) cudaEventRecord(evs[4 * k], st);
+        switch (level * 2 + (prof ? 1 : 0)) {
+          case 0: wf_intersect<0, false><<<grid, block, 0, st>>>(d->view, W, C, d->err, nullptr); break;
+          case 1: wf_intersect<0, true><<<grid, block, 0, st>>>(d->view, W, C, d->err, dcnt); break;
+          case 2: wf_intersect<1, false><<<grid, block, 0, st>>>(d->view, W, C, d->err, nullptr); break;
+          case 3: wf_intersect<1, true><<<grid, block, 0, st>>>(d->view, W, C, d->err, dcnt); break;
+          case 4: wf_intersect<2, false><<<grid, block, 0, st>>>(d->view, W, C, d->err, nullptr); break;
+          default: wf_intersect<2, true><<<grid, block, 0, st>>>(d->view, W, C, d->err, dcnt); break;
+        }
+        if (prof) cudaEventRecord(evs[4 * k + 1], st);
+        if (prof) cudaEventRecord(evs[4 * k + 2], st);
+        wf_shade_specular<<<qgrid, block, 0, st>>>(d->view, P, W, C, d->err);
+        wf_shade_diffuse<<<qgrid, block, 0, st>>>(d->view, P, W, C, d->err);
+        wf_finish<<<qgrid, block, 0, st>>>(d->view, P, W, C, film);
+        if (prof) cudaEventRecord(evs[4 * k + 3], st);
       }
+      g_launches += 4 * batch;
       ck(cudaGetLastError(), "wavefront launch");
       ck(cudaMemcpyAsync(d->wf_live_host, &d->wf_counters->live, sizeof(unsigned int), cudaMemcpyDeviceToHost, st),
          "cudaMemcpyAsync");
       ck(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+      if (prof) {
+        for (int k = 0; k < batch; ++k) {
+          float a = 0.0f, b = 0.0f;
+          cudaEventElapsedTime(&a, evs[4 * k], evs[4 * k + 1]);
+          cudaEventElapsedTime(&b, evs[4 * k + 2], evs[4 * k + 3]);
+          prof->ms_intersect += a;
+          prof->ms_shade += b;
+        }
+        prof->intersect_launches += batch;
+        prof->shade_launches += batch;
+      }
       if (*d->wf_live_host == 0) break;
       if (it > (uint64_t)4 * (P.total / q + 1) * (o->max_depth + 2) + 64)
         throw std::runtime_error("wavefront did not drain");  // unreachable unless a kernel misbehaves
     }
+    if (prof) {
+      unsigned long long h[3];
+      ck(cudaMemcpy(h, dcnt, sizeof h, cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
+      prof->path_segments = h[0];
+      prof->node_visits = h[1];
+      prof->prim_tests = h[2];
+      prof->paths = P.total;
+      prof->path_slots = q;
+    }
+    cleanup();
     return CLV_OK;
   } catch (std::exception& e) {
+    cleanup();
     return fail(CLV_E_CUDA, e.what());
   }
 }
@@ -736,8 +843,10 @@ int clv_render_device(clv_device_scene* d, const clv_render_opts* o, double* fil
   if (rc) return rc;
   if (!film_dev) return fail(CLV_E_INVALID, "null film");
   const int block = 128;
-  if (o->mode == CLV_MODE_PATH_TRACING && o->engine == 0) return render_wavefront(d, o, film_dev, (cudaStream_t)stream);
+  if (o->mode == CLV_MODE_PATH_TRACING && o->engine == 0)
+    return render_wavefront(d, o, film_dev, (cudaStream_t)stream, nullptr);
   const RenderParams P = make_params(o);
+  g_launches += 1;
   if (o->mode == CLV_MODE_PATH_TRACING) {
     render_kernel<<<launch_grid(P.npix * P.chunks, block), block, 0, (cudaStream_t)stream>>>(d->view, P, film_dev,
                                                                                              d->err);
@@ -761,6 +870,7 @@ int clv_resolve_device(const double* film_dev, uint32_t width, uint32_t height, 
   const uint64_t n = (uint64_t)width * height;
   if (n == 0) return CLV_OK;
   resolve_kernel<<<(uint32_t)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(R, film_dev, xyz_dev, rgb_dev);
+  g_launches += 1;
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail(CLV_E_CUDA, std::string("resolve launch: ") + cudaGetErrorString(e));
   return CLV_OK;

@@ -377,6 +377,144 @@ __device__ __noinline__ bool ObjEval<LEVEL>::hit(const ClvDeviceScene& S, uint32
   return false;
 }
 
+// Flat evaluator for the common compound shape: a chain of Translate /
+// RotateY wrappers (up to CLV_CHAIN levels) over a Boxy, quad, triangle,
+// sphere or moving sphere.  It walks down transforming the ray exactly as the
+// wrappers' hit() do (translate.rs:41-78, rotate.rs:82-159), tests the
+// terminal, then walks back up applying each wrapper's record transform and
+// set_face_normal with that level's ray direction (recomputed from the top,
+// which keeps the loop's state small).  Returns 0 miss, 1 hit, 2 not handled
+// here (media, lists, deeper chains).
+#define CLV_CHAIN 4
+__device__ __forceinline__ V chain_dir(const ClvDeviceScene& S, uint32_t ref, V d, int upto) {
+  // direction of the ray as seen below level `upto` (inclusive)
+  for (int j = 0; j <= upto; ++j) {
+    const ClvObj& o = S.objs[CLV_REF_INDEX(ref)];
+    if (o.kind == CLV_OBJ_ROTATEY) {
+      const float sn = o.p[0], cs = o.p[1];
+      V rd = d;
+      rd.x = cs * d.x - sn * d.z;
+      rd.z = sn * d.x + cs * d.z;
+      d = unit(rd);
+    }
+    ref = o.a;
+  }
+  return d;
+}
+__device__ __forceinline__ int chain_hit(const ClvDeviceScene& S, uint32_t top, const Ray& r0, float tmin, float tmax,
+                                         Rec& rec, Counters* cnt) {
+  int n = 0;
+  Ray r = r0;
+  uint32_t ref = top;
+  while (CLV_REF_KIND(ref) == CLV_REF_OBJ) {
+    const ClvObj& o = S.objs[CLV_REF_INDEX(ref)];
+    if (o.kind == CLV_OBJ_TRANSLATE) {
+      if (n == CLV_CHAIN) return 2;
+      r.o = sub(r.o, mk(o.p[0], o.p[1], o.p[2]));
+    } else if (o.kind == CLV_OBJ_ROTATEY) {
+      if (n == CLV_CHAIN) return 2;
+      const float sn = o.p[0], cs = o.p[1];
+      V ro = r.o, rd = r.d;
+      ro.x = cs * r.o.x - sn * r.o.z;
+      ro.z = sn * r.o.x + cs * r.o.z;
+      rd.x = cs * r.d.x - sn * r.d.z;
+      rd.z = sn * r.d.x + cs * r.d.z;
+      r.o = ro;
+      r.d = unit(rd);
+    } else if (o.kind == CLV_OBJ_BOXY || o.kind == CLV_OBJ_MOVING) {
+      break;
+    } else {
+      return 2;
+    }
+    ++n;
+    ref = o.a;
+  }
+  // terminal
+  const uint32_t kind = CLV_REF_KIND(ref), idx = CLV_REF_INDEX(ref);
+  bool any = false;
+  if (kind == CLV_REF_OBJ) {
+    const ClvObj& o = S.objs[idx];
+    if (o.kind == CLV_OBJ_BOXY) {  // closest of its 6 quads (boxy.rs:76-94)
+      float closest = tmax;
+      for (int k = 0; k < 6; ++k) {
+        if (cnt) cnt->prims++;
+        float f[16], t, a, b;
+        load_planar(S.quads, o.a + k, f);
+        if (planar_test(f, false, r, tmin, closest, t, a, b)) {
+          planar_record(f, r, t, a, b, rec);
+          rec.mat = S.quad_mat[o.a + k];
+          closest = t;
+          any = true;
+        }
+      }
+    } else {  // MovingSphere (moving_sphere.rs:104-160)
+      if (cnt) cnt->prims++;
+      const V c0 = mk(o.p[0], o.p[1], o.p[2]), c1 = mk(o.p[3], o.p[4], o.p[5]);
+      const V c = add(c0, scl((r.time - o.p[6]) / (o.p[7] - o.p[6]), sub(c1, c0)));
+      float t;
+      if (sphere_test(make_float4(c.x, c.y, c.z, o.p[8]), r, tmin, tmax, t)) {
+        sphere_record(c, o.p[8], r, t, rec);
+        rec.mat = o.b;
+        any = true;
+      }
+    }
+  } else if (kind == CLV_REF_TRI || kind == CLV_REF_QUAD) {
+    if (cnt) cnt->prims++;
+    float f[16], t, a, b;
+    load_planar(kind == CLV_REF_TRI ? S.tris : S.quads, idx, f);
+    if (planar_test(f, kind == CLV_REF_TRI, r, tmin, tmax, t, a, b)) {
+      planar_record(f, r, t, a, b, rec);
+      rec.mat = kind == CLV_REF_TRI ? S.tri_mat[idx] : S.quad_mat[idx];
+      any = true;
+    }
+  } else if (kind == CLV_REF_SPHERE) {
+    if (cnt) cnt->prims++;
+    const float4 sp = load_sphere(S, idx);
+    float t;
+    if (sphere_test(sp, r, tmin, tmax, t)) {
+      sphere_record(mk(sp.x, sp.y, sp.z), sp.w, r, t, rec);
+      rec.mat = S.sphere_mat[idx];
+      any = true;
+    }
+  } else {
+    return 2;
+  }
+  if (!any) return 0;
+  for (int l = n - 1; l >= 0; --l) {
+    uint32_t wr = top;
+    for (int j = 0; j < l; ++j) wr = S.objs[CLV_REF_INDEX(wr)].a;
+    const ClvObj& o = S.objs[CLV_REF_INDEX(wr)];
+    if (o.kind == CLV_OBJ_TRANSLATE) {
+      rec.p = add(rec.p, mk(o.p[0], o.p[1], o.p[2]));
+      const V d = l == 0 ? r0.d : chain_dir(S, top, r0.d, l - 1);
+      const V nn = rec.n;
+      rec.front = dot(d, nn) < 0.0f;
+      rec.n = rec.front ? nn : neg(nn);
+    } else {
+      const float sn = o.p[0], cs = o.p[1];
+      V p = rec.p, nn = rec.n;
+      p.x = cs * rec.p.x + sn * rec.p.z;
+      p.z = -sn * rec.p.x + cs * rec.p.z;
+      nn.x = cs * rec.n.x + sn * rec.n.z;
+      nn.z = -sn * rec.n.x + cs * rec.n.z;
+      rec.p = p;
+      const V un = unit(nn);
+      const V d = chain_dir(S, top, r0.d, l);
+      rec.front = dot(d, un) < 0.0f;
+      rec.n = rec.front ? un : neg(un);
+    }
+  }
+  return 1;
+}
+
+// A compound BVH leaf, out of line so the traversal loop stays small.
+__device__ __noinline__ bool compound_leaf(const ClvDeviceScene& S, uint32_t ref, const Ray& r, float tmin,
+                                           float tmax, Rng* rng, Rec& rec, Counters* cnt, uint32_t* err) {
+  const int c = chain_hit(S, ref, r, tmin, tmax, rec, cnt);
+  if (c != 2) return c == 1;
+  return ObjEval<0>::hit(S, ref, r, tmin, tmax, rng, rec, cnt, err);
+}
+
 // pdf_value of one MIS leaf object (HitableTrait::pdf_value of each type).
 __device__ __forceinline__ float planar_pdf(const ClvDeviceScene& S, bool tri, uint32_t idx, V origin, V dir) {
   float f[16], t, a, b;
@@ -469,8 +607,9 @@ __device__ __forceinline__ bool box_distance_pre(const float* b, const RayPre& R
   return tmax >= tmin && tmax > 0.0f;
 }
 
-// Tests one BVH leaf with the current tmax.
-template <bool COMPLEX>
+// Tests one BVH leaf with the current tmax.  CPLX: 0 primitives only,
+// 1 + wrapper chains (inline), 2 + media and lists (out-of-line interpreter).
+template <int CPLX>
 __device__ __forceinline__ bool leaf_test(const ClvDeviceScene& S, uint32_t ref, const Ray& r, float tmin,
                                           float tmax, Rng* rng, Hit& hit, Rec* full, Counters* cnt, uint32_t* err) {
   const uint32_t kind = CLV_REF_KIND(ref), idx = CLV_REF_INDEX(ref);
@@ -493,9 +632,19 @@ __device__ __forceinline__ bool leaf_test(const ClvDeviceScene& S, uint32_t ref,
     hit.ref = ref;
     return true;
   }
-  if (COMPLEX) {
+  if (CPLX == 1) {
     Rec rec;
-    if (!ObjEval<0>::hit(S, ref, r, tmin, tmax, rng, rec, cnt, err)) return false;
+    const int c = chain_hit(S, ref, r, tmin, tmax, rec, cnt);
+    if (c == 2 && err) atomicOr(err, CLV_ERR_NEST);  // host routes such scenes to CPLX 2
+    if (c != 1) return false;
+    hit.t = rec.t;
+    hit.ref = ref;
+    if (full) *full = rec;
+    return true;
+  }
+  if (CPLX == 2) {
+    Rec rec;
+    if (!compound_leaf(S, ref, r, tmin, tmax, rng, rec, cnt, err)) return false;
     hit.t = rec.t;
     hit.ref = ref;
     if (full) *full = rec;
@@ -513,7 +662,7 @@ __device__ __forceinline__ bool leaf_test(const ClvDeviceScene& S, uint32_t ref,
 // stack belongs to an ancestor whose near subtree is being traversed, so when
 // a hit is accepted all current entries are marked, which keeps the marked
 // entries a prefix [0, marked) of the stack.
-template <bool COMPLEX>
+template <int CPLX>
 __device__ bool closest_hit(const ClvDeviceScene& S, const Ray& r, float tmin, float tmax, Rng* rng, Hit& hit,
                             Rec* full, Counters* cnt, uint32_t* err) {
   hit.ref = CLV_REF_EMPTY;
@@ -588,7 +737,7 @@ __device__ bool closest_hit(const ClvDeviceScene& S, const Ray& r, float tmin, f
         }
       }
     } else {
-      if (leaf_test<COMPLEX>(S, ref, r, tmin, tmax, rng, hit, full, cnt, err)) {
+      if (leaf_test<CPLX>(S, ref, r, tmin, tmax, rng, hit, full, cnt, err)) {
         tmax = hit.t;
         found = true;
         marked = sp;

@@ -19,10 +19,11 @@
 namespace clvd {
 
 struct WfState {
+  uint32_t* queue;   // 3 * Q slot indices, one segment per class
   float4* o_time;    // origin.xyz, time
   float4* d_lambda;  // direction.xyz, wavelength (int bits)
-  float4* beta;      // throughput per wavelength
-  float4* L;         // accumulated spectral power per wavelength
+  float4* beta;      // throughput per wavelength (only lights and the background
+                     // emit, so a path's power is beta times its final emission)
   uint4* meta;       // pixel, depth, rng counter, flags (1 = live)
   uint2* key;        // rng key
   float4* hit;       // t, ref bits, a, b
@@ -30,10 +31,13 @@ struct WfState {
   uint32_t Q;
 };
 
+#define WF_Q_FINISH 0  // misses, emitters and paths ended in the shade kernels
+#define WF_Q_SPEC 1    // metal, dielectric, dispersive
+#define WF_Q_DIFF 2    // lambertian, isotropic
 struct WfCounters {
   unsigned long long next_work;  // next unassigned work item
-  unsigned int live;             // live paths after the last shade pass
-  unsigned int pad;
+  unsigned int live;             // live paths after the last shading pass
+  unsigned int queue[3];         // per-class queue lengths of this bounce
 };
 
 struct WfParams {
@@ -78,7 +82,6 @@ __device__ __forceinline__ void wf_start_path(const ClvDeviceScene& S, const WfP
   W.o_time[i] = make_float4(r.o.x, r.o.y, r.o.z, r.time);
   W.d_lambda[i] = make_float4(r.d.x, r.d.y, r.d.z, __int_as_float(r.lambda));
   W.beta[i] = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
-  W.L[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   W.meta[i] = make_uint4(pixel, 0u, rng.counter, 1u);
   W.key[i] = make_uint2((uint32_t)rng.key, (uint32_t)(rng.key >> 32));
 }
@@ -93,33 +96,85 @@ __global__ void wf_init(ClvDeviceScene S, WfParams P, WfState W) {
   }
 }
 
-template <bool COMPLEX>
-__global__ void __launch_bounds__(128) wf_intersect(ClvDeviceScene S, WfState W, uint32_t* err) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= W.Q) return;
-  const uint4 m = W.meta[i];
-  if (!(m.w & 1u)) return;
-  const float4 a = W.o_time[i], b = W.d_lambda[i];
-  const Ray r{mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, __float_as_int(b.w)};
-  Hit h;
-  if (COMPLEX) {
-    Rng rng;
-    const uint2 k = W.key[i];
-    rng.key = (uint64_t)k.x | ((uint64_t)k.y << 32);
-    rng.counter = m.z;
-    Rec full;
-    const bool any = closest_hit<true>(S, r, CLV_EPS_ACNE, CLV_FLT_MAX, &rng, h, &full, nullptr, err);
-    if (rng.counter != m.z) W.meta[i].z = rng.counter;  // media drew randomness
-    if (any && CLV_REF_KIND(h.ref) == CLV_REF_OBJ) {
-      W.full[3 * i] = make_float4(full.p.x, full.p.y, full.p.z, full.u);
-      W.full[3 * i + 1] = make_float4(full.n.x, full.n.y, full.n.z, full.v);
-      W.full[3 * i + 2] = make_float4(full.front ? 1.0f : 0.0f, __uint_as_float(full.mat), 0.0f, 0.0f);
-    }
-    W.hit[i] = make_float4(any ? h.t : 0.0f, __uint_as_float(any ? h.ref : CLV_REF_EMPTY), h.a, h.b);
-  } else {
-    const bool any = closest_hit<false>(S, r, CLV_EPS_ACNE, CLV_FLT_MAX, nullptr, h, nullptr, nullptr, err);
-    W.hit[i] = make_float4(any ? h.t : 0.0f, __uint_as_float(any ? h.ref : CLV_REF_EMPTY), h.a, h.b);
+// counters (optional): [0] live paths intersected, [1] BVHNode::hit calls, [2] primitive tests
+__device__ __forceinline__ void warp_add_counts(unsigned long long* cnt, uint32_t live, uint32_t nodes,
+                                                uint32_t prims) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    live += __shfl_down_sync(0xFFFFFFFFu, live, off);
+    nodes += __shfl_down_sync(0xFFFFFFFFu, nodes, off);
+    prims += __shfl_down_sync(0xFFFFFFFFu, prims, off);
   }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(cnt, (unsigned long long)live);
+    atomicAdd(cnt + 1, (unsigned long long)nodes);
+    atomicAdd(cnt + 2, (unsigned long long)prims);
+  }
+}
+
+// Appends slot i to queue `cls`: lanes with the same class are grouped with
+// __match_any_sync and each group reserves its slots with one atomic.
+__device__ __forceinline__ void wf_enqueue(const WfState& W, WfCounters* C, int cls, uint32_t i) {
+  const unsigned active = __activemask();
+  const unsigned peers = __match_any_sync(active, cls);
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(peers) - 1;
+  unsigned base = 0;
+  if (lane == leader) base = atomicAdd(&C->queue[cls], (unsigned)__popc(peers));
+  base = __shfl_sync(peers, base, leader);
+  W.queue[(size_t)cls * W.Q + base + __popc(peers & ((1u << lane) - 1u))] = i;
+}
+
+__device__ __forceinline__ int material_class(const ClvDeviceScene& S, uint32_t mat) {
+  const uint32_t k = S.materials[mat].kind;
+  if (k == CLV_MAT_LAMBERTIAN || k == CLV_MAT_ISOTROPIC) return WF_Q_DIFF;
+  if (k == CLV_MAT_DIFFUSELIGHT || k == CLV_MAT_CONELIGHT) return WF_Q_FINISH;
+  return WF_Q_SPEC;
+}
+
+template <int CPLX, bool COUNT>
+__global__ void __launch_bounds__(128) wf_intersect(ClvDeviceScene S, WfState W, WfCounters* C, uint32_t* err,
+                                                    unsigned long long* cnt) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  Counters c{0u, 0u};
+  uint32_t live = 0;
+  if (i < W.Q) {
+    const uint4 m = W.meta[i];
+    if (m.w & 1u) {
+      live = 1;
+      const float4 a = W.o_time[i], b = W.d_lambda[i];
+      const Ray r{mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, __float_as_int(b.w)};
+      Hit h;
+      Rec full;
+      Rng rng;
+      if (CPLX == 2) {  // media draw randomness inside the traversal
+        const uint2 k = W.key[i];
+        rng.key = (uint64_t)k.x | ((uint64_t)k.y << 32);
+        rng.counter = m.z;
+      }
+      const bool any = closest_hit<CPLX>(S, r, CLV_EPS_ACNE, CLV_FLT_MAX, CPLX == 2 ? &rng : nullptr, h,
+                                         CPLX ? &full : nullptr, COUNT ? &c : nullptr, err);
+      if (CPLX == 2 && rng.counter != m.z) W.meta[i].z = rng.counter;
+      int cls = WF_Q_FINISH;
+      if (any) {
+        const uint32_t kind = CLV_REF_KIND(h.ref), idx = CLV_REF_INDEX(h.ref);
+        uint32_t mat;
+        if (kind == CLV_REF_TRI) mat = S.tri_mat[idx];
+        else if (kind == CLV_REF_QUAD) mat = S.quad_mat[idx];
+        else if (kind == CLV_REF_SPHERE) mat = S.sphere_mat[idx];
+        else mat = full.mat;
+        cls = material_class(S, mat);
+        if (CPLX && kind == CLV_REF_OBJ) {
+          W.full[3 * i] = make_float4(full.p.x, full.p.y, full.p.z, full.u);
+          W.full[3 * i + 1] = make_float4(full.n.x, full.n.y, full.n.z, full.v);
+          W.full[3 * i + 2] = make_float4(full.front ? 1.0f : 0.0f, __uint_as_float(full.mat), 0.0f, 0.0f);
+        }
+      }
+      W.hit[i] = make_float4(any ? h.t : 0.0f, __uint_as_float(any ? h.ref : CLV_REF_EMPTY), h.a, h.b);
+      wf_enqueue(W, C, cls, i);
+    }
+  }
+  if (COUNT) warp_add_counts(cnt, live, c.nodes, c.prims);
 }
 
 __device__ __forceinline__ bool wf_is_normal_pos(float v) {
@@ -127,96 +182,183 @@ __device__ __forceinline__ bool wf_is_normal_pos(float v) {
   return v > 0.0f && a >= 1.17549435e-38f && a <= 3.40282347e+38f;
 }
 
-// One bounce of trace().  Returns false when the path ends (its L is final).
-__device__ __forceinline__ bool shade_bounce(const ClvDeviceScene& S, Ray& ray, float beta[4], float L[4],
-                                             const Hit& h, const Rec& full, Rng& rng, uint32_t* err) {
+struct WfPath {
+  Ray ray;
+  float beta[4];
+  uint4 meta;
+  Rng rng;
+};
+__device__ __forceinline__ void wf_load(const WfState& W, uint32_t i, WfPath& P) {
+  const float4 a = W.o_time[i], b = W.d_lambda[i];
+  P.ray = Ray{mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, __float_as_int(b.w)};
+  const float4 bv = W.beta[i];
+  P.beta[0] = bv.x; P.beta[1] = bv.y; P.beta[2] = bv.z; P.beta[3] = bv.w;
+  P.meta = W.meta[i];
+  const uint2 k = W.key[i];
+  P.rng.key = (uint64_t)k.x | ((uint64_t)k.y << 32);
+  P.rng.counter = P.meta.z;
+}
+__device__ __forceinline__ void wf_hit_record(const ClvDeviceScene& S, const WfState& W, uint32_t i, const Ray& ray,
+                                              Hit& h, Rec& rec) {
+  const float4 hv = W.hit[i];
+  h.t = hv.x;
+  h.ref = __float_as_uint(hv.y);
+  h.a = hv.z;
+  h.b = hv.w;
+  Rec full;
+  if (h.ref != CLV_REF_EMPTY && CLV_REF_KIND(h.ref) == CLV_REF_OBJ) {
+    const float4 f0 = W.full[3 * i], f1 = W.full[3 * i + 1], f2 = W.full[3 * i + 2];
+    full.t = h.t;
+    full.p = mk(f0.x, f0.y, f0.z);
+    full.u = f0.w;
+    full.n = mk(f1.x, f1.y, f1.z);
+    full.v = f1.w;
+    full.front = f2.x != 0.0f;
+    full.mat = __float_as_uint(f2.y);
+  }
+  if (h.ref != CLV_REF_EMPTY) hit_record(S, ray, h, full, rec);
+}
+// attenuation of trace.rs:61-70: hero only on wavelength-dependent materials
+__device__ __forceinline__ void wf_attenuation(const ClvDeviceScene& S, const ClvMaterial& m, const Ray& ray,
+                                               const Rec& rec, float atten[4]) {
   const int hero = ray.lambda;
-  int waves[4];
-  wf_rotate(hero, waves);
-  if (h.ref == CLV_REF_EMPTY) {  // background (trace.rs:42-48)
-#pragma unroll
-    for (int i = 0; i < 4; ++i) L[i] += beta[i] * spd_get(S, S.background_spd, waves[i]);
-    return false;
-  }
-  Rec rec;
-  hit_record(S, ray, h, full, rec);
-  const ClvMaterial& m = S.materials[rec.mat];
-  const uint32_t kind = m.kind;
-  if (kind == CLV_MAT_DIFFUSELIGHT || kind == CLV_MAT_CONELIGHT) {  // no scatter: emitted only
-#pragma unroll
-    for (int i = 0; i < 4; ++i) L[i] += beta[i] * mat_emit(S, m, ray, waves[i], rec);
-    return false;
-  }
-  // the other kinds emit 0 (MaterialTrait::emit default)
-  V nd;
-  bool specular = true;
-  float spdf = 0.0f, mis = 1.0f;
-  if (kind == CLV_MAT_METAL) {  // metal.rs:27-51
-    const V refl = reflect(ray.d, rec.n);
-    nd = unit(add(refl, scl(m.fuzz, random_unit_vector(rng))));
-  } else if (kind == CLV_MAT_DIELECTRIC || kind == CLV_MAT_DISPERSIVE) {  // dielectric.rs, dispersive.rs
-    const float ri = kind == CLV_MAT_DIELECTRIC ? m.refractive_index : dispersive_index(m, ray.lambda);
-    const float ratio = rec.front ? 1.0f / ri : ri;
-    const float ct = fminf(-dot(ray.d, rec.n), 1.0f);
-    const float st = sqrtf(1.0f - ct * ct);
-    if (ratio * st > 1.0f) {
-      nd = reflect(ray.d, rec.n);
-    } else {
-      const float rp = schlick(ct, ratio);
-      nd = rng.f32() < rp ? reflect(ray.d, rec.n) : refract(ray.d, rec.n, ratio);
-    }
-  } else {  // Lambertian (CosinePDF) / Isotropic (SpherePDF) mixed 50/50 with the light tree (pdf.rs:122-140)
-    specular = false;
-    const bool lamb = kind == CLV_MAT_LAMBERTIAN;
-    V gen;
-    if (rng.boolean()) {
-      gen = mis_random(S, rec.p, rng);
-    } else if (lamb) {  // ONB::build_from_w(normal).local(random_cosine_direction)
-      const V w = rec.n;
-      const V a = fabsf(w.x) > 0.9f ? unit(mk(0.0f, 1.0f, 0.0f)) : unit(mk(1.0f, 0.0f, 0.0f));
-      const V vv = unit(cross(w, a));
-      const V uu = unit(cross(w, vv));
-      const V c = random_cosine_direction(rng);
-      gen = unit(add(add(scl(c.x, uu), scl(c.y, vv)), scl(c.z, w)));
-    } else {
-      gen = random_unit_vector(rng);
-    }
-    nd = unit(gen);
-    const float light_v = mis_pdf(S, rec.p, nd, hero, ray.time, err);
-    float bsdf_v;
-    if (lamb) {
-      const float cosine = dot(unit(nd), rec.n);
-      bsdf_v = cosine <= 0.0f ? 0.0f : cosine / CLV_PI;
-    } else {
-      bsdf_v = 1.0f / (4.0f * CLV_PI);
-    }
-    mis = 0.5f * light_v + 0.5f * bsdf_v;
-    if (lamb) {  // Lambertian::scattering_pdf: None below the surface -> emitted (0) only
-      const float c = dot(rec.n, unit(nd));
-      if (c < 0.0f) return false;
-      spdf = c / CLV_PI;
-    } else {
-      spdf = 1.0f / (4.0f * CLV_PI);
-    }
-  }
-  float atten[4];  // hero only on wavelength-dependent materials (trace.rs:61-70)
   if (m.wavelength_dependent) {
     atten[0] = mat_color(S, m, ray, hero, rec);
     atten[1] = atten[2] = atten[3] = 0.0f;
   } else {
+    int waves[4];
+    wf_rotate(hero, waves);
 #pragma unroll
-    for (int i = 0; i < 4; ++i) atten[i] = mat_color(S, m, ray, waves[i], rec);
+    for (int j = 0; j < 4; ++j) atten[j] = mat_color(S, m, ray, waves[j], rec);
   }
-  if (specular) {
-#pragma unroll
-    for (int i = 0; i < 4; ++i) beta[i] = beta[i] * atten[i];
-  } else {
-#pragma unroll
-    for (int i = 0; i < 4; ++i) beta[i] = beta[i] * (atten[i] * spdf / mis);
+}
+// continue the path with `nd` (depth + 1) or end it at the depth limit
+__device__ __forceinline__ bool wf_advance(const WfParams& P, const WfState& W, WfCounters* C, uint32_t i, WfPath& p,
+                                           V origin, V nd) {
+  const uint32_t depth = p.meta.y + 1;
+  if (depth > P.max_depth) {  // trace at depth > max_depth returns 0
+    W.meta[i].z = p.rng.counter;
+    wf_enqueue(W, C, WF_Q_FINISH, i);
+    return false;
   }
-  ray.o = rec.p;
-  ray.d = nd;
+  W.o_time[i] = make_float4(origin.x, origin.y, origin.z, p.ray.time);
+  W.d_lambda[i] = make_float4(nd.x, nd.y, nd.z, __int_as_float(p.ray.lambda));
+  W.beta[i] = make_float4(p.beta[0], p.beta[1], p.beta[2], p.beta[3]);
+  W.meta[i] = make_uint4(p.meta.x, depth, p.rng.counter, 1u);
   return true;
+}
+__device__ __forceinline__ void wf_count_live(WfCounters* C, bool live) {
+  const unsigned lm = __ballot_sync(0xFFFFFFFFu, live);
+  if ((threadIdx.x & 31) == 0 && lm) atomicAdd(&C->live, (unsigned)__popc(lm));
+}
+
+// Specular bounce: Metal (metal.rs:27-51), Dielectric / Dispersive (dielectric.rs:37-81, dispersive.rs:58-123)
+__global__ void __launch_bounds__(128) wf_shade_specular(ClvDeviceScene S, WfParams P, WfState W, WfCounters* C,
+                                                         uint32_t* err) {
+  const uint32_t n = C->queue[WF_Q_SPEC];
+  const uint32_t stride = gridDim.x * blockDim.x;
+  const uint32_t first = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t rounds = (n + stride - 1) / stride;
+  for (uint32_t r = 0; r < rounds; ++r) {
+    const uint32_t q = first + r * stride;
+    bool live = false;
+    if (q < n) {
+      const uint32_t i = W.queue[(size_t)WF_Q_SPEC * W.Q + q];
+      WfPath p;
+      wf_load(W, i, p);
+      Hit h;
+      Rec rec;
+      wf_hit_record(S, W, i, p.ray, h, rec);
+      const ClvMaterial& m = S.materials[rec.mat];
+      V nd;
+      if (m.kind == CLV_MAT_METAL) {
+        nd = unit(add(reflect(p.ray.d, rec.n), scl(m.fuzz, random_unit_vector(p.rng))));
+      } else {
+        const float ri = m.kind == CLV_MAT_DIELECTRIC ? m.refractive_index : dispersive_index(m, p.ray.lambda);
+        const float ratio = rec.front ? 1.0f / ri : ri;
+        const float ct = fminf(-dot(p.ray.d, rec.n), 1.0f);
+        const float st = sqrtf(1.0f - ct * ct);
+        if (ratio * st > 1.0f) {
+          nd = reflect(p.ray.d, rec.n);
+        } else {
+          const float rp = schlick(ct, ratio);
+          nd = p.rng.f32() < rp ? reflect(p.ray.d, rec.n) : refract(p.ray.d, rec.n, ratio);
+        }
+      }
+      float atten[4];
+      wf_attenuation(S, m, p.ray, rec, atten);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) p.beta[j] = p.beta[j] * atten[j];
+      live = wf_advance(P, W, C, i, p, rec.p, nd);
+    }
+    wf_count_live(C, live);
+  }
+}
+
+// Diffuse bounce: MixturePDF(HitablePDF(priority tree), Cosine/SpherePDF), pdf.rs:122-140, trace.rs:80-119
+__global__ void __launch_bounds__(128) wf_shade_diffuse(ClvDeviceScene S, WfParams P, WfState W, WfCounters* C,
+                                                        uint32_t* err) {
+  const uint32_t n = C->queue[WF_Q_DIFF];
+  const uint32_t stride = gridDim.x * blockDim.x;
+  const uint32_t first = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t rounds = (n + stride - 1) / stride;
+  for (uint32_t r = 0; r < rounds; ++r) {
+    const uint32_t q = first + r * stride;
+    bool live = false;
+    if (q < n) {
+      const uint32_t i = W.queue[(size_t)WF_Q_DIFF * W.Q + q];
+      WfPath p;
+      wf_load(W, i, p);
+      Hit h;
+      Rec rec;
+      wf_hit_record(S, W, i, p.ray, h, rec);
+      const ClvMaterial& m = S.materials[rec.mat];
+      const bool lamb = m.kind == CLV_MAT_LAMBERTIAN;
+      V gen;
+      if (p.rng.boolean()) {
+        gen = mis_random(S, rec.p, p.rng);
+      } else if (lamb) {  // ONB::build_from_w(normal).local(random_cosine_direction)
+        const V w = rec.n;
+        const V a = fabsf(w.x) > 0.9f ? unit(mk(0.0f, 1.0f, 0.0f)) : unit(mk(1.0f, 0.0f, 0.0f));
+        const V vv = unit(cross(w, a));
+        const V uu = unit(cross(w, vv));
+        const V c = random_cosine_direction(p.rng);
+        gen = unit(add(add(scl(c.x, uu), scl(c.y, vv)), scl(c.z, w)));
+      } else {
+        gen = random_unit_vector(p.rng);
+      }
+      const V nd = unit(gen);
+      const float light_v = mis_pdf(S, rec.p, nd, p.ray.lambda, p.ray.time, err);
+      float bsdf_v;
+      if (lamb) {
+        const float cosine = dot(unit(nd), rec.n);
+        bsdf_v = cosine <= 0.0f ? 0.0f : cosine / CLV_PI;
+      } else {
+        bsdf_v = 1.0f / (4.0f * CLV_PI);
+      }
+      const float mis = 0.5f * light_v + 0.5f * bsdf_v;
+      float spdf;
+      bool scatter = true;
+      if (lamb) {  // Lambertian::scattering_pdf: None below the surface -> emitted (0) only
+        const float cs = dot(rec.n, unit(nd));
+        scatter = !(cs < 0.0f);
+        spdf = cs / CLV_PI;
+      } else {
+        spdf = 1.0f / (4.0f * CLV_PI);
+      }
+      if (!scatter) {
+        W.meta[i].z = p.rng.counter;
+        wf_enqueue(W, C, WF_Q_FINISH, i);
+      } else {
+        float atten[4];
+        wf_attenuation(S, m, p.ray, rec, atten);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) p.beta[j] = p.beta[j] * (atten[j] * spdf / mis);
+        live = wf_advance(P, W, C, i, p, rec.p, nd);
+      }
+    }
+    wf_count_live(C, live);
+  }
 }
 
 // film rule of draw_cpu.rs:131-142, deposited as f64 sums
@@ -247,75 +389,65 @@ __device__ __forceinline__ void film_deposit(const ClvDeviceScene& S, double* fi
   if (a2 != 0.0) atomicAdd(f + 2, a2);
 }
 
-__global__ void __launch_bounds__(128) wf_shade(ClvDeviceScene S, WfParams P, WfState W, WfCounters* C,
-                                                double* __restrict__ film, uint32_t* err) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  bool live = false, need = false;
-  if (i < W.Q) {
-    uint4 m = W.meta[i];
-    if (m.w & 1u) {
+// Ends paths: background on a miss (trace.rs:42-48) or emission of a light
+// (trace.rs:51-58), film deposit, then the slot takes the next work item.
+__global__ void __launch_bounds__(128) wf_finish(ClvDeviceScene S, WfParams P, WfState W, WfCounters* C,
+                                                 double* __restrict__ film) {
+  const uint32_t n = C->queue[WF_Q_FINISH];
+  const uint32_t stride = gridDim.x * blockDim.x;
+  const uint32_t first = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t rounds = (n + stride - 1) / stride;
+  for (uint32_t r = 0; r < rounds; ++r) {
+    const uint32_t q = first + r * stride;
+    bool need = false;
+    uint32_t i = 0;
+    if (q < n) {
+      i = W.queue[(size_t)WF_Q_FINISH * W.Q + q];
       const float4 a = W.o_time[i], b = W.d_lambda[i];
-      Ray ray{mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, __float_as_int(b.w)};
-      const float4 hv = W.hit[i];
+      const Ray ray{mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, __float_as_int(b.w)};
+      const float4 bv = W.beta[i];
+      const float beta[4] = {bv.x, bv.y, bv.z, bv.w};
+      float L[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+      int waves[4];
+      wf_rotate(ray.lambda, waves);
       Hit h;
-      h.t = hv.x;
-      h.ref = __float_as_uint(hv.y);
-      h.a = hv.z;
-      h.b = hv.w;
-      Rec full;
-      if (h.ref != CLV_REF_EMPTY && CLV_REF_KIND(h.ref) == CLV_REF_OBJ) {
-        const float4 f0 = W.full[3 * i], f1 = W.full[3 * i + 1], f2 = W.full[3 * i + 2];
-        full.t = h.t;
-        full.p = mk(f0.x, f0.y, f0.z);
-        full.u = f0.w;
-        full.n = mk(f1.x, f1.y, f1.z);
-        full.v = f1.w;
-        full.front = f2.x != 0.0f;
-        full.mat = __float_as_uint(f2.y);
-      }
-      Rng rng;
-      const uint2 k = W.key[i];
-      rng.key = (uint64_t)k.x | ((uint64_t)k.y << 32);
-      rng.counter = m.z;
-      const float4 bv = W.beta[i], lv = W.L[i];
-      float beta[4] = {bv.x, bv.y, bv.z, bv.w}, L[4] = {lv.x, lv.y, lv.z, lv.w};
-      const int hero = ray.lambda;
-      bool cont = shade_bounce(S, ray, beta, L, h, full, rng, err);
-      const uint32_t depth = m.y + 1;
-      if (cont && depth > P.max_depth) cont = false;  // trace at depth > max_depth returns 0
-      if (cont) {
-        W.o_time[i] = make_float4(ray.o.x, ray.o.y, ray.o.z, ray.time);
-        W.d_lambda[i] = make_float4(ray.d.x, ray.d.y, ray.d.z, __int_as_float(ray.lambda));
-        W.beta[i] = make_float4(beta[0], beta[1], beta[2], beta[3]);
-        W.L[i] = make_float4(L[0], L[1], L[2], L[3]);
-        W.meta[i] = make_uint4(m.x, depth, rng.counter, 1u);
-        live = true;
+      Rec rec;
+      wf_hit_record(S, W, i, ray, h, rec);
+      if (h.ref == CLV_REF_EMPTY) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) L[j] += beta[j] * spd_get(S, S.background_spd, waves[j]);
       } else {
-        film_deposit(S, film, m.x, hero, L);
-        need = true;
+        const ClvMaterial& m = S.materials[rec.mat];
+        if (m.kind == CLV_MAT_DIFFUSELIGHT || m.kind == CLV_MAT_CONELIGHT) {
+#pragma unroll
+          for (int j = 0; j < 4; ++j) L[j] += beta[j] * mat_emit(S, m, ray, waves[j], rec);
+        }
+        // paths that ended in the shade kernels (depth limit, no scatter) add nothing here
+      }
+      film_deposit(S, film, W.meta[i].x, ray.lambda, L);
+      need = true;
+    }
+    // finished paths take new work items, one atomic per warp
+    const unsigned mask = __ballot_sync(0xFFFFFFFFu, need);
+    bool live = false;
+    if (mask) {
+      const int lane = threadIdx.x & 31;
+      const int leader = __ffs(mask) - 1;
+      unsigned long long base = 0;
+      if (lane == leader) base = atomicAdd(&C->next_work, (unsigned long long)__popc(mask));
+      base = __shfl_sync(0xFFFFFFFFu, base, leader);
+      if (need) {
+        const uint64_t w = base + __popc(mask & ((1u << lane) - 1u));
+        if (w < P.total) {
+          wf_start_path(S, P, W, i, w);
+          live = true;
+        } else {
+          W.meta[i].w = 0u;
+        }
       }
     }
+    wf_count_live(C, live);
   }
-  // finished paths take new work items, one atomic per warp
-  const unsigned mask = __ballot_sync(0xFFFFFFFFu, need);
-  if (mask) {
-    const int lane = threadIdx.x & 31;
-    const int leader = __ffs(mask) - 1;
-    unsigned long long base = 0;
-    if (lane == leader) base = atomicAdd(&C->next_work, (unsigned long long)__popc(mask));
-    base = __shfl_sync(0xFFFFFFFFu, base, leader);
-    if (need) {
-      const uint64_t w = base + __popc(mask & ((1u << lane) - 1u));
-      if (w < P.total) {
-        wf_start_path(S, P, W, i, w);
-        live = true;
-      } else {
-        W.meta[i].w = 0u;
-      }
-    }
-  }
-  const unsigned lm = __ballot_sync(0xFFFFFFFFu, live);
-  if ((threadIdx.x & 31) == 0 && lm) atomicAdd(&C->live, (unsigned)__popc(lm));
 }
 
 }  // namespace clvd

@@ -146,7 +146,23 @@ int clv_device_status(clv_device_scene* dscene, uint32_t* flags_out);
 const char* clv_last_error(void);
 const char* clv_version(void);
 
+/* Number of kernels this library has launched since it was loaded. */
+uint64_t clv_kernel_launches(void);
+
 /* ---- diagnostics (no counterpart in the reference) ----------------------- */
+
+/* One wavefront render with per-kernel device times and traversal counts. */
+typedef struct clv_render_profile {
+  double ms_init, ms_intersect, ms_shade;  /* summed device time per kernel type */
+  uint64_t intersect_launches, shade_launches;
+  uint64_t paths;          /* samples traced */
+  uint64_t path_segments;  /* closest-hit queries (one per bounce of a live path) */
+  uint64_t node_visits;    /* BVHNode::hit calls over all queries */
+  uint64_t prim_tests;     /* primitive tests over all queries */
+  uint64_t path_slots;     /* paths in flight */
+} clv_render_profile;
+int clv_render_profile_run(clv_device_scene* dscene, const clv_render_opts* opts, double* film_dev, void* stream,
+                           clv_render_profile* out);
 
 /* Checks the traversal's fast slab division (reciprocal + one FMA correction)
  * against IEEE division on n random operand pairs; mismatches must be 0. */
