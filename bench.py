@@ -212,7 +212,8 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cpu-spp", type=int, default=2, help="samples per pixel of the CPU baseline sample")
+    ap.add_argument("--cpu-spp", type=int, default=16, help="samples per pixel of each reference-arm step")
+    ap.add_argument("--cpu-baseline-spp", type=int, default=64, help="samples per pixel of the CPU baseline leg")
     ap.add_argument("--no-traversal", action="store_true", help="skip the ray-cast section")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline legs")
     args = ap.parse_args()
@@ -396,7 +397,7 @@ def main():
         line["traversal"] = trav
 
     if rank == 0 and world == 1 and not args.no_cpu:
-        line["cpu_baseline"] = cpu_baseline_render(path, args.cpu_spp)
+        line["cpu_baseline"] = cpu_baseline_render(path, args.cpu_baseline_spp)
     if rank == 0:
         print(json.dumps(line), flush=True)
     os.unlink(path)

@@ -29,7 +29,7 @@ using namespace clvd;
 // ------------------------------------------------------------------ kernels --
 
 template <int CPLX>
-__global__ void __launch_bounds__(128) raycast_kernel(ClvDeviceScene S, const float4* __restrict__ rays, uint64_t n,
+__global__ void __launch_bounds__(128, CLV_MINB) raycast_kernel(ClvDeviceScene S, const float4* __restrict__ rays, uint64_t n,
                                                       uint32_t* __restrict__ prim, float* __restrict__ tout,
                                                       uint32_t* __restrict__ nodes, uint32_t* __restrict__ tests,
                                                       uint32_t* err) {
@@ -316,25 +316,50 @@ __global__ void resolve_kernel(ResolveParams R, const double* __restrict__ film,
 // Self-test of div_rn against IEEE division on random operands: a spans
 // magnitudes 2^-40..2^40 with random signs, d spans 2^-70..2^70 including
 // values outside div_rn's fast range, zeros and infinities.
-__global__ void selftest_division_kernel(uint64_t n, uint64_t seed, unsigned long long* bad) {
+__device__ __forceinline__ float selftest_coord(uint64_t h) {
+  // 0, or a random float of magnitude 2^-70 .. 2^59
+  if ((h & 63) == 0) return 0.0f;
+  const uint32_t e = 127 - 70 + (uint32_t)((h >> 8) % 130);
+  return __uint_as_float((uint32_t)(h >> 32) & 0x807FFFFFu | (e << 23));
+}
+// Self-test of the traversal's divisions against IEEE division.
+// mode 0: div_rn on arbitrary operands (zeros, infinities, subnormals);
+// mode 1: div_fast on the operands the traversal admits: a = b - o with b, o
+//         0 or of magnitude 2^-70..2^59, |d| in 2^-60..2.
+__global__ void selftest_division_kernel(uint64_t n, uint64_t seed, int mode, unsigned long long* bad) {
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   unsigned long long local = 0;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
     const uint64_t h1 = mix64(seed ^ (i * 0x9E3779B97F4A7C15ull)), h2 = mix64(h1 + 0x632BE59BD9B4E019ull);
-    float a = __uint_as_float((uint32_t)(h1 & 0x807FFFFFu) | ((uint32_t)(87 + (h1 >> 32) % 81) << 23));
-    float d = __uint_as_float((uint32_t)(h2 & 0x807FFFFFu) | ((uint32_t)(57 + (h2 >> 32) % 141) << 23));
-    const uint32_t sel = (uint32_t)(h2 >> 56);
-    if (sel == 0) d = 0.0f;
-    if (sel == 1) d = -0.0f;
-    if (sel == 2) a = 0.0f;
-    if (sel == 3) d = __uint_as_float(0x7F800000u);
-    if (sel == 4) d = __uint_as_float((uint32_t)(h2 & 0x807FFFFFu));  // subnormal
+    const uint64_t h3 = mix64(h2 + 0x1234567ull);
+    float a, d;
+    if (mode == 0) {
+      a = __uint_as_float((uint32_t)(h1 & 0x807FFFFFu) | ((uint32_t)(87 + (h1 >> 32) % 81) << 23));
+      d = __uint_as_float((uint32_t)(h2 & 0x807FFFFFu) | ((uint32_t)(57 + (h2 >> 32) % 141) << 23));
+      const uint32_t sel = (uint32_t)(h2 >> 56);
+      if (sel == 0) d = 0.0f;
+      if (sel == 1) d = -0.0f;
+      if (sel == 2) a = 0.0f;
+      if (sel == 3) d = __uint_as_float(0x7F800000u);
+      if (sel == 4) d = __uint_as_float((uint32_t)(h2 & 0x807FFFFFu));  // subnormal
+    } else {
+      const float b = selftest_coord(h1), o = ((h3 >> 60) == 0) ? b : selftest_coord(h3);
+      a = b - o;
+      const uint32_t e = 127 - 60 + (uint32_t)((h2 >> 8) % 62);  // 2^-60 .. 2^1
+      d = __uint_as_float(((uint32_t)(h2 >> 32) & 0x807FFFFFu) | (e << 23));
+    }
     const float inv = 1.0f / d;
-    const float ad = fabsf(d);
-    const bool fast = ad >= 8.67361738e-19f && ad <= 1.15292150e18f;
-    const float q = fast ? div_rn(a, d, inv) : a / d;
+    float q;
+    if (mode == 0) {
+      const float ad = fabsf(d);
+      const bool fast = ad >= 8.67361738e-19f && ad <= 1.15292150e18f;
+      q = fast ? div_rn(a, d, inv) : a / d;
+    } else {
+      q = div_fast(a, d, inv);
+    }
     const float e = a / d;
-    if (__float_as_uint(q) != __float_as_uint(e) && !(q != q && e != e)) ++local;
+    // zero signs are irrelevant to the traversal (values only meet comparisons)
+    if (__float_as_uint(q) != __float_as_uint(e) && !(q != q && e != e) && !(q == 0.0f && e == 0.0f)) ++local;
   }
   if (local) atomicAdd(bad, local);
 }
@@ -384,6 +409,21 @@ int sm_count() {
 struct clv_scene {
   clv::HostScene host;
 };
+
+// Whether every coordinate of every BVH box is 0 or of magnitude in
+// [2^-70, 2^59] (the precondition of the traversal's unguarded division).
+static bool boxes_div_safe(const clv::HostScene& h) {
+  auto ok = [](float x) {
+    const float a = std::fabs(x);
+    return x == 0.0f || (a >= 8.47032947e-22f && a <= 5.76460752e17f);
+  };
+  for (int k = 0; k < 6; ++k)
+    if (!ok(h.root_box[k])) return false;
+  for (const ClvNode& n : h.nodes)
+    for (int k = 0; k < 6; ++k)
+      if (!ok(n.lbox[k]) || !ok(n.rbox[k])) return false;
+  return true;
+}
 
 // Which traversal variant the scene needs: 0 primitives only, 1 wrapper
 // chains handled inline (chain_hit), 2 media or lists (interpreter).
@@ -533,7 +573,8 @@ int clv_selftest_division(uint64_t n, uint64_t seed, uint64_t* mismatches) {
     unsigned long long* bad = nullptr;
     ck(cudaMalloc(&bad, sizeof(unsigned long long)), "cudaMalloc");
     ck(cudaMemset(bad, 0, sizeof(unsigned long long)), "cudaMemset");
-    selftest_division_kernel<<<launch_grid(n, 256), 256>>>(n, seed, bad);
+    selftest_division_kernel<<<launch_grid(n, 256), 256>>>(n, seed, 0, bad);
+    selftest_division_kernel<<<launch_grid(n, 256), 256>>>(n, seed + 1, 1, bad);
     unsigned long long h = 0;
     const cudaError_t e = cudaMemcpy(&h, bad, sizeof h, cudaMemcpyDeviceToHost);
     cudaFree(bad);
@@ -652,6 +693,7 @@ int clv_scene_upload(const clv_scene* s, clv_device_scene** out) {
     v.n_materials = (uint32_t)h.materials.size();
     v.max_depth_tree = h.tree_depth;
     v.compound_level = compound_level(h);
+    v.boxes_div_safe = boxes_div_safe(h) ? 1u : 0u;
     v.mis_depth = h.mis_depth;
     v.camera = h.camera;
     ck(cudaMalloc(&d->err, sizeof(uint32_t)), "cudaMalloc");

@@ -34,6 +34,9 @@ namespace clvd {
 #define CLV_STACK 64       // traversal stack entries (host rejects deeper trees)
 #define CLV_MIS_STACK 32   // MIS tree evaluation stack
 #define CLV_NEST 6         // wrapper nesting depth handled by the object interpreter
+#ifndef CLV_MINB
+#define CLV_MINB 8         // resident blocks per SM asked of the traversal kernels (64 registers)
+#endif
 
 // Device error flags (bitwise OR into a status word the host reads).
 #define CLV_ERR_STACK 1u
@@ -572,8 +575,15 @@ struct Hit {
 // q0 = RN(a*inv); the residual a - q0*d is exact with an FMA and one
 // correction step q0 + residual*inv rounds to the correctly rounded quotient
 // (Markstein's theorem; Muller et al., Handbook of Floating-Point Arithmetic,
-// ch. 8) while no intermediate overflows or underflows.  Outside the guarded
-// range the IEEE division is used, so every result equals a / d exactly.
+// ch. 8) provided nothing overflows or underflows.  The traversal uses the
+// unguarded form only when that is guaranteed for every box of the scene and
+// the ray (see RayPre::fast); otherwise it divides.
+__device__ __forceinline__ float div_fast(float a, float d, float inv) {
+  const float q0 = a * inv;
+  const float r = __fmaf_rn(-q0, d, a);
+  return __fmaf_rn(r, inv, q0);
+}
+// the guarded form, valid for any operands (used by the self-test)
 __device__ __forceinline__ float div_rn(float a, float d, float inv) {
   const float q0 = a * inv;
   const float aq = fabsf(q0);
@@ -584,14 +594,26 @@ __device__ __forceinline__ float div_rn(float a, float d, float inv) {
   return a / d;
 }
 
-// Per-ray constants of the traversal.
+// Per-ray constants of the traversal.  `fast` holds when the scene's box
+// coordinates and the ray origin are each 0 or of magnitude in [2^-70, 2^59]
+// and the direction components have magnitude in [2^-60, 2]: then every
+// a = box - origin is 0 or of magnitude in [2^-93, 2^60], every quotient a/d
+// is 0 or normal and finite, and div_fast equals a / d exactly.
 struct RayPre {
   V o, d, inv;
-  bool fast;  // all |d| in [2^-60, 2^60]: div_rn's guard suffices
+  bool fast;
 };
+__device__ __forceinline__ bool coord_ok(float x) {
+  const float a = fabsf(x);
+  return x == 0.0f || (a >= 8.47032947e-22f && a <= 5.76460752e17f);  // 2^-70 .. 2^59
+}
+__device__ __forceinline__ bool dir_ok(float x) {
+  const float a = fabsf(x);
+  return a >= 8.67361738e-19f && a <= 2.0f;  // 2^-60 .. 2
+}
 __device__ __forceinline__ float divc(const RayPre& R, float a, int axis) {
   const float d = comp(R.d, axis), inv = comp(R.inv, axis);
-  return R.fast ? div_rn(a, d, inv) : a / d;
+  return R.fast ? div_fast(a, d, inv) : a / d;
 }
 // AABB::distance with div_rn
 __device__ __forceinline__ bool box_distance_pre(const float* b, const RayPre& R, float& out) {
@@ -671,11 +693,8 @@ __device__ bool closest_hit(const ClvDeviceScene& S, const Ray& r, float tmin, f
   R.o = r.o;
   R.d = r.d;
   R.inv = mk(1.0f / r.d.x, 1.0f / r.d.y, 1.0f / r.d.z);
-  {
-    const float ax = fabsf(r.d.x), ay = fabsf(r.d.y), az = fabsf(r.d.z);
-    const float lo = 8.67361738e-19f, hi = 1.15292150e18f;
-    R.fast = ax >= lo && ax <= hi && ay >= lo && ay <= hi && az >= lo && az <= hi;
-  }
+  R.fast = S.boxes_div_safe && dir_ok(r.d.x) && dir_ok(r.d.y) && dir_ok(r.d.z) && coord_ok(r.o.x) &&
+           coord_ok(r.o.y) && coord_ok(r.o.z);
   float4 stack[CLV_STACK];
   int sp = 0, marked = 0;
   uint32_t ref = S.root;

@@ -126,6 +126,7 @@ struct ClvDeviceScene {
   uint32_t n_nodes, n_tris, n_quads, n_spheres, n_objs, n_materials;
   uint32_t max_depth_tree;  // depth of the main BVH (stack bound)
   uint32_t compound_level;  // 0 primitives only, 1 wrapper chains, 2 media / lists present
+  uint32_t boxes_div_safe;  // every BVH box coordinate is 0 or of magnitude in [2^-70, 2^59]
   uint32_t mis_depth;
   ClvCamera camera;
 };

@@ -133,7 +133,7 @@ __device__ __forceinline__ int material_class(const ClvDeviceScene& S, uint32_t 
 }
 
 template <int CPLX, bool COUNT>
-__global__ void __launch_bounds__(128) wf_intersect(ClvDeviceScene S, WfState W, WfCounters* C, uint32_t* err,
+__global__ void __launch_bounds__(128, CLV_MINB) wf_intersect(ClvDeviceScene S, WfState W, WfCounters* C, uint32_t* err,
                                                     unsigned long long* cnt) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   Counters c{0u, 0u};

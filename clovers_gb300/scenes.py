@@ -141,3 +141,86 @@ def camera_rays(width, height, camera_fn):
             out[k, 7] = 3.4028234663852886e38
             k += 1
     return out
+
+
+def write_binary_stl(path, triangles):
+    """Binary STL of triangles (n, 3, 3) float32 (normals written as zero)."""
+    import struct
+    tris = np.asarray(triangles, np.float32).reshape(-1, 3, 3)
+    with open(path, "wb") as f:
+        f.write(b"\0" * 80 + struct.pack("<I", tris.shape[0]))
+        rec = np.zeros((tris.shape[0], 50), np.uint8)
+        body = np.concatenate([np.zeros((tris.shape[0], 3), np.float32), tris.reshape(-1, 9)], axis=1)
+        rec[:, :48] = body.view(np.uint8).reshape(-1, 48)
+        f.write(rec.tobytes())
+    return path
+
+
+def prism_triangles():
+    """A triangular prism as 8 triangles (2 end caps, 3 rectangular sides split in two)."""
+    a = np.array([[0, 0, 0], [1, 0, 0], [0.5, 0.866, 0]], np.float32)
+    b = a + np.array([0, 0, 1], np.float32)
+    tris = [a, b[::-1]]
+    for i in range(3):
+        j = (i + 1) % 3
+        tris += [np.stack([a[i], a[j], b[j]]), np.stack([a[i], b[j], b[i]])]
+    return np.stack(tris)
+
+
+def kitchen_sink(stl_path):
+    """Every object, material and texture kind on the render path in one small scene."""
+    objects = [
+        {"kind": "Quad", "q": [-10, 0, -10], "u": [20, 0, 0], "v": [0, 0, 20], "material": "surface checker floor"},
+        {"kind": "Quad", "q": [-10, 0, -6], "u": [20, 0, 0], "v": [0, 10, 0], "material": "spatial checker wall"},
+        {"kind": "Quad", "priority": True, "q": [-2, 7.99, -2], "u": [4, 0, 0], "v": [0, 0, 4], "material": "lamp d65"},
+        {"kind": "Sphere", "priority": True, "center": [4, 6, -1], "radius": 0.5, "material": "cone lamp"},
+        {"kind": "Triangle", "priority": True, "q": [-6, 5, 3], "u": [1.5, 0, 0], "v": [0, 1.5, 0],
+         "material": {"kind": "DiffuseLight", "emit": {"kind": "IlluminantLedB3", "intensity": 3.0}}},
+        {"kind": "Sphere", "center": [-3, 1, 0], "radius": 1, "material": "thin film"},
+        {"kind": "Sphere", "center": [0, 1, -2], "radius": 1, "material": "cauchy glass"},
+        {"kind": "Sphere", "center": [3, 1, 1], "radius": 1, "material": "sellmeier glass"},
+        {"kind": "Sphere", "center": [0, 0.6, 2.5], "radius": 0.6, "material": "fuzzy metal"},
+        {"kind": "MovingSphere", "center_0": [-1.5, 0.4, 3], "center_1": [-1.5, 0.9, 3], "radius": 0.4,
+         "material": "tinted glass"},
+        {"kind": "Translate", "offset": [1.5, 0, -4],
+         "object": {"kind": "RotateY", "angle": 30,
+                    "object": {"kind": "Boxy", "corner_0": [0, 0, 0], "corner_1": [1, 2, 1], "material": "lambert"}}},
+        {"kind": "ConstantMedium", "density": 0.6,
+         "boundary": {"kind": "Boxy", "corner_0": [-5, 0, -4], "corner_1": [-3.5, 1.5, -2.5]},
+         "texture": {"kind": "SolidColor", "color": [0.9, 0.9, 0.7]}},
+        {"kind": "ConstantMedium", "density": 0.3,
+         "boundary": {"kind": "Sphere", "center": [5, 1, -3], "radius": 0.9},
+         "texture": {"kind": "IlluminantD50", "intensity": 0.8}},
+        {"kind": "Translate", "offset": [0, 3, 4],
+         "object": {"kind": "ObjectList", "objects": [
+             {"kind": "Quad", "q": [-1, 0, 0], "u": [1, 0, 0], "v": [0, 1, 0], "material": "lambert"},
+             {"kind": "Quad", "q": [0, 0, 0], "u": [1, 0, 0], "v": [0, 1, 0], "material": "lambert"}]}},
+        {"kind": "ObjectList", "objects": [
+            {"kind": "Sphere", "center": [-4, 3, -4], "radius": 0.3, "material": "lambert"},
+            {"kind": "Triangle", "q": [2, 3, -5], "u": [1, 0, 0], "v": [0, 1, 0], "material": "lambert"}]},
+        {"kind": "STL", "path": stl_path, "center": [-1, 2.5, -4], "scale": 1.2, "rotation": [0, 20, -30],
+         "material": "sellmeier glass"},
+    ]
+    materials = [
+        {"name": "surface checker floor", "kind": "Lambertian",
+         "albedo": {"kind": "SurfaceChecker", "even": [0.8, 0.8, 0.8], "odd": {"hex": "#335577"}, "density": 8}},
+        {"name": "spatial checker wall", "kind": "Lambertian",
+         "albedo": {"kind": "SpatialChecker", "even": {"srgb": [0.9, 0.4, 0.2]}, "odd": {"lin_srgb": [0.1, 0.2, 0.6]},
+                    "density": 2}},
+        {"name": "lamp d65", "kind": "DiffuseLight", "emit": {"kind": "IlluminantD65", "intensity": 4.0}},
+        {"name": "cone lamp", "kind": "ConeLight", "spread": 40.0,
+         "emit": {"kind": "SolidColor", "color": {"xyz_e": [30, 25, 20]}}},
+        {"name": "thin film", "kind": "Lambertian", "albedo": {"kind": "SolidColor", "color": [0.7, 0.7, 0.7]},
+         "thin_film": {"refractive_index": 1.33, "thickness": 420.0}},
+        {"name": "cauchy glass", "kind": "Dispersive", "cauchy_a": 1.728, "cauchy_b": 0.01342},
+        {"name": "sellmeier glass", "kind": "Dispersive", "sellmeier_b": [1.0396, 0.2318, 1.0105],
+         "sellmeier_c": [0.0060, 0.0200, 103.56]},
+        {"name": "fuzzy metal", "kind": "Metal", "albedo": {"kind": "SolidColor", "color": {"xyz_d65": [0.6, 0.6, 0.5]}},
+         "fuzz": 0.3},
+        {"name": "tinted glass", "kind": "Dielectric", "refractive_index": 1.45, "color": [0.9, 1.0, 0.8]},
+        {"name": "lambert", "kind": "Lambertian", "albedo": {"kind": "SolidColor", "color": [0.5, 0.6, 0.4]}},
+    ]
+    camera = {"look_from": [0.0, 4.0, 14.0], "look_at": [0.0, 1.5, 0.0], "up": [0.0, 1.0, 0.0],
+              "vertical_fov": 40.0, "aperture": 0.1, "focus_distance": 13.0}
+    return {"time_0": 0, "time_1": 1, "camera": camera, "background_color": [0.05, 0.06, 0.1],
+            "objects": objects, "materials": materials}

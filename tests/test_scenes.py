@@ -1,0 +1,113 @@
+"""Scene coverage: every object, material and texture kind of the render path.
+
+CPU: the product's and the oracle's loaders agree on every scene file the
+reference ships (object counts and BVH / MIS-tree shapes), and on the
+kitchen-sink scene.  GPU: same-seed renders of the kitchen-sink scene match
+the oracle, and ray casts through its compound objects (wrapper chains,
+media drawing randomness inside the traversal, nested lists) are bit-exact.
+"""
+
+import glob
+import json
+import os
+
+import numpy as np
+import pytest
+
+import clovers_gb300 as cg
+import oracle
+from clovers_gb300 import scenes
+
+REFERENCE = "/root/reference"
+
+
+@pytest.fixture(scope="module")
+def sink_path(tmp_path_factory):
+    d = tmp_path_factory.mktemp("sink")
+    stl = scenes.write_binary_stl(str(d / "prism.stl"), scenes.prism_triangles())
+    return scenes.write_scene(scenes.kitchen_sink(stl), str(d / "sink.json"))
+
+
+def test_kitchen_sink_loads_identically(sink_path):
+    info = cg.Scene.from_json(sink_path, 64, 48).info()
+    o = oracle.Scene.from_json(sink_path, 64, 48)
+    st = o.tree_stats()
+    assert info["objects"] == o.object_count()
+    assert (info["nodes"], info["tree_depth"], info["mis_nodes"]) == (st["nodes"], st["tree_depth"], st["mis_nodes"])
+    assert info["compound"] > 5 and info["triangles"] >= 8
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REFERENCE, "scenes")), reason="reference checkout not present")
+def test_reference_scene_files_load_like_the_oracle(monkeypatch):
+    monkeypatch.chdir(REFERENCE)  # the reference's scenes name mesh paths relative to its root
+    checked = 0
+    for path in sorted(glob.glob(os.path.join(REFERENCE, "scenes", "*.json"))):
+        try:
+            ours = cg.Scene.from_json(path, 320, 240).info()
+        except cg.ClvError as e:
+            ours = e
+        try:
+            ref = oracle.Scene.from_json(path, 320, 240)
+        except ValueError as e:
+            ref = e
+        if isinstance(ours, Exception) or isinstance(ref, Exception):
+            # both refuse the same files: GLTF / PLY meshes (not part of this build) or missing blobs
+            assert isinstance(ours, Exception) and isinstance(ref, Exception), (path, ours, ref)
+            continue
+        st = ref.tree_stats()
+        assert ours["objects"] == ref.object_count(), path
+        assert (ours["nodes"], ours["tree_depth"], ours["mis_nodes"]) == (st["nodes"], st["tree_depth"],
+                                                                          st["mis_nodes"]), path
+        checked += 1
+    assert checked >= 6
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("engine", ["wavefront", "megakernel"])
+def test_kitchen_sink_same_seed(sink_path, engine):
+    w, h, spp, depth = 80, 60, 16, 12
+    d = cg.Scene.from_json(sink_path, w, h).upload()
+    assert d.info["compound"] > 0
+    stats = {}
+    img = cg.draw(cg.GlobalOptions(quiet=True), cg.RenderOptions(width=w, height=h, samples=spp, max_depth=depth,
+                                                                 seed=77), d, stats=stats, engine=engine)
+    assert stats["device_errors"] == 0
+    ref = oracle.Scene.from_json(sink_path, w, h).render(w, h, spp, depth, seed=77) / spp
+    err = float(np.mean((img - ref) ** 2 / (ref ** 2 + 1e-2)))
+    close = np.all(np.abs(img - ref) <= 1e-4 * (np.abs(ref) + 1e-3), axis=1).mean()
+    print("kitchen sink %s: relMSE %.3g, pixels within tolerance %.4f" % (engine, err, close))
+    assert err <= 1e-3
+    assert close >= 0.95
+
+
+@pytest.mark.gpu
+def test_kitchen_sink_raycast_parity(sink_path):
+    w, h = 160, 120
+    d = cg.Scene.from_json(sink_path, w, h).upload()
+    o = oracle.Scene.from_json(sink_path, w, h)
+    cam = scenes.camera_rays(w, h, lambda pu, pv: o.camera_ray(pu, pv))
+    rng = np.random.default_rng(4)
+    extra = scenes.random_rays(30000, seed=5)
+    extra[:, 0:3] = rng.uniform(-6, 6, (30000, 3)).astype(np.float32)
+    rays = np.concatenate([cam, extra])
+    prim, t, nodes, tests = cg.raycast(d, rays, with_counts=True)
+    oprim, ot, onodes, otests = o.raycast(rays, with_counts=True)
+    # media sample their free-flight distance with log(), whose last bit differs between CUDA and the
+    # host libm: for hits on a medium (top-level objects 11 and 12) distances agree within 4 ulp and the
+    # traversal counts may differ; everything else is bit-exact.
+    media = np.isin(oprim, [11, 12])
+    assert np.array_equal(prim[~media], oprim[~media])
+    hit = (oprim != 0xFFFFFFFF) & ~media
+    assert np.array_equal(t[hit].view(np.uint32), ot[hit].view(np.uint32))
+    mh = media & (prim == oprim)
+    ulps = np.abs(t[mh].view(np.int32).astype(np.int64) - ot[mh].view(np.int32).astype(np.int64))
+    assert ulps.size == 0 or ulps.max() <= 4
+    assert (prim[media] == oprim[media]).mean() > 0.99
+    bad = np.nonzero(((nodes != onodes) | (tests != otests)) & ~media)[0]
+    if bad.size:
+        for k in bad[:8]:
+            print("ray %d %s prim %d/%d nodes %d/%d tests %d/%d" % (k, rays[k].tolist(), prim[k], oprim[k], nodes[k],
+                                                                   onodes[k], tests[k], otests[k]))
+    assert bad.size == 0, "%d rays with different traversal counts" % bad.size
+    hit = oprim != 0xFFFFFFFF
+    assert hit.mean() > 0.5
