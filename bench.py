@@ -177,13 +177,14 @@ def run_reference(args, world, rank):
         times.append(time.perf_counter() - t0)
     samples = W_IMG * H_IMG * spp_sample
     value = samples * len(times) / sum(times) / 1e6
-    sample = "512x512 image at %d spp per step (of the workload's 256 spp)" % spp_sample
+    sample = "%dx%d image at %d spp per step (of the workload's %d spp)" % (W_IMG, H_IMG, spp_sample, SPP)
     line = {
         "impl": "reference", "metric": "Msamples/s", "value": round(value, 4), "unit": "Msamples/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(1e3 * sum(times) / len(times), 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded enclosed-box scene)",
-        "config": {"workload": "enclosed box 512x512, 256 spp, depth 16", "sample": sample, "parallelism": "host threads"},
+        "config": {"workload": "enclosed box %dx%d, %d spp, depth %d" % (W_IMG, H_IMG, SPP, DEPTH), "sample": sample,
+                   "parallelism": "host threads"},
         "cpu_baseline": {"value": round(value, 4), "unit": "Msamples/s", "cores": threads, "kind": "port",
                          "sample": sample},
         "e2e": {"value": round(value, 4), "unit": "Msamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -207,6 +208,7 @@ def cpu_baseline_render(path, spp_sample):
 
 
 def main():
+    global W_IMG, H_IMG, SPP, RAYS, TRIS
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
@@ -215,9 +217,16 @@ def main():
     ap.add_argument("--cpu-spp", type=int, default=16, help="samples per pixel of each reference-arm step")
     ap.add_argument("--cpu-baseline-spp", type=int, default=64, help="samples per pixel of the CPU baseline leg")
     ap.add_argument("--no-traversal", action="store_true", help="skip the ray-cast section")
+    ap.add_argument("--no-render", action="store_true", help="skip the render section (ray casts only)")
+    ap.add_argument("--size", type=int, default=W_IMG, help="image width = height (reduced cases for profiling)")
+    ap.add_argument("--spp", type=int, default=SPP, help="samples per pixel (reduced cases for profiling)")
+    ap.add_argument("--rays", type=int, default=RAYS, help="ray count of the ray-cast section")
+    ap.add_argument("--tris", type=int, default=TRIS, help="triangle count of the ray-cast section")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline legs")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    W_IMG = H_IMG = args.size
+    SPP, RAYS, TRIS = args.spp, args.rays, args.tris
     world, rank, local = dist_setup(args)
     if args.impl == "reference":
         run_reference(args, world, rank)
@@ -234,109 +243,113 @@ def main():
     hbm_peak, peak_kind = measured_peaks()
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > 129 MB L2
 
-    # ---------------------------------------------------------------- render
     path = box_scene_file()
-    host_scene = cg.Scene.from_json(path, W_IMG, H_IMG)
-    dscene = host_scene.upload()
-    npix = W_IMG * H_IMG
-    film = torch.zeros(npix * 3, dtype=torch.float64, device="cuda")
-
-    def opts_for(step):
-        o = cg.render_opts(cg.RenderOptions(width=W_IMG, height=H_IMG, samples=SPP, max_depth=DEPTH, seed=SEED))
-        o.sample_offset = (rank * 1000003 + step) * SPP  # weak scaling: every rank renders its own samples
-        return o
-
-    for w in range(args.warmup):
-        film.zero_()
-        _lib.check(L.clv_render_device(dscene.handle, ctypes.byref(opts_for(10**6 + w)), film.data_ptr(), sp))
-    torch.cuda.synchronize()
-    launches0 = L.clv_kernel_launches()
     gpu_index = os.environ.get("CUDA_VISIBLE_DEVICES", str(local)).split(",")[local if world > 1 else 0]
-    step_ms = []
-    barrier(world)
-    torch.cuda.synchronize()
-    with ClockSampler(gpu_index) as clocks:
-        wall0 = time.perf_counter()
-        for k in range(args.steps):
-            film.zero_()
-            flush.zero_()  # L2 flush between timed steps
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            _lib.check(L.clv_render_device(dscene.handle, ctypes.byref(opts_for(k)), film.data_ptr(), sp))
-            e1.record(stream)
-            e1.synchronize()
-            step_ms.append(e0.elapsed_time(e1))
-        torch.cuda.synchronize()
-        wall = time.perf_counter() - wall0
-    barrier(world)
-    launches = L.clv_kernel_launches() - launches0
-    ms_step = all_max(world, sum(step_ms) / len(step_ms))
-    samples_step = npix * SPP
-    value = world * samples_step / (ms_step / 1e3) / 1e6
-
-    # e2e: through the host-buffer C ABI (scene upload + render + image download), every step
-    xyz = np.empty((npix, 3), np.float32)
-    host_opts = opts_for(0)
-    e2e_times = []
-    st = _lib.StatsC()
-    h2d = 0
-    for k in range(args.steps):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        d2 = host_scene.upload()
-        host_opts.sample_offset = (rank * 1000003 + 5000 + k) * SPP
-        _lib.check(L.clv_render(d2.handle, ctypes.byref(host_opts), xyz.ctypes.data, ctypes.byref(st)))
-        e2e_times.append(time.perf_counter() - t0)
-        d2.close()
-    info = host_scene.info()
-    # bytes the upload copies (nodes, records, materials, spectral tables, illuminants, CMF)
-    h2d = (info["nodes"] * 64 + info["triangles"] * 64 + info["quads"] * 64 + info["spheres"] * 16 +
-           info["compound"] * 64 + info["materials"] * 112 + 38 * 400 * 4 + 400 * 12)
-    e2e_s = all_max(world, sum(e2e_times) / len(e2e_times))
-    e2e_value = world * samples_step / e2e_s / 1e6
-
-    # profiling pass (untimed): per-kernel device time and traversal counts for the roofline
-    prof = _lib.RenderProfileC()
-    film.zero_()
-    _lib.check(L.clv_render_profile_run(dscene.handle, ctypes.byref(opts_for(777)), film.data_ptr(), sp,
-                                        ctypes.byref(prof)))
-    torch.cuda.synchronize()
-    segs = prof.path_segments
-    # algorithmic bytes per closest-hit query (one per bounce of a live path):
-    #   intersect: reads meta + origin + direction (48 B), writes the hit (16 B) and a queue entry (4 B),
-    #              and fetches one 64-B node per BVHNode::hit call and one 64-B record per primitive test;
-    #   shade (specular/diffuse/finish): reads the queue entry (4 B), path state + hit (88 B) and writes
-    #              the next state (64 B) per query; per sample 80 B read at the end, 24 B of film and
-    #              72 B for the regenerated path.
-    isect_bytes = segs * (48 + 16 + 4) + 64 * (prof.node_visits + prof.prim_tests)
-    shade_bytes = segs * (4 + 88 + 64) + prof.paths * (80 + 24 + 72)
-    kernels = {"wf_intersect": (prof.ms_intersect, isect_bytes, prof.intersect_launches),
-               "wf_shade": (prof.ms_shade, shade_bytes, prof.shade_launches)}
-    dom = max(kernels, key=lambda k: kernels[k][0])
-    d_ms, d_bytes, d_launches = kernels[dom]
-    achieved = d_bytes / (d_ms / 1e3) / 1e9
     traffic = ncu_traffic()
-    roofline = {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",
-                "frac": round(achieved / hbm_peak, 4), "peak_kind": peak_kind,
-                "traffic": traffic.get(dom + ".bytes_per_launch"),
-                "algorithmic_bytes_per_launch": round(d_bytes / max(1, d_launches)),
-                "kernel_ms_per_step": {k: round(v[0], 3) for k, v in kernels.items()},
-                "path_segments": segs, "node_visits": prof.node_visits, "prim_tests": prof.prim_tests}
+    if args.no_render:
+        line = {"metric": "Grays/s", "unit": "Grays/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "higher_is_better": True, "config": {"workload": "ray casts only"}}
+    else:
+        # ---------------------------------------------------------------- render
+        host_scene = cg.Scene.from_json(path, W_IMG, H_IMG)
+        dscene = host_scene.upload()
+        npix = W_IMG * H_IMG
+        film = torch.zeros(npix * 3, dtype=torch.float64, device="cuda")
 
-    line = {
-        "metric": "Msamples/s", "value": round(value, 3), "unit": "Msamples/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded enclosed-box scene in the reference's scene format)",
-        "config": {"workload": "enclosed box 512x512, 256 spp, depth 16 (wavefront engine)",
-                   "samples_per_step": samples_step, "l2": "flushed between steps (256 MiB write)",
-                   "parallelism": "replicas" if world > 1 else "single GPU", "wall_s_timed_loop": round(wall, 3)},
-        "e2e": {"value": round(e2e_value, 3), "unit": "Msamples/s", "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(npix * 3 * 4)},
-        "gpu_launches": int(launches),
-        "roofline": roofline,
-        "clocks": clocks.summary(),
-    }
+        def opts_for(step):
+            o = cg.render_opts(cg.RenderOptions(width=W_IMG, height=H_IMG, samples=SPP, max_depth=DEPTH, seed=SEED))
+            o.sample_offset = (rank * 1000003 + step) * SPP  # weak scaling: every rank renders its own samples
+            return o
+
+        for w in range(args.warmup):
+            film.zero_()
+            _lib.check(L.clv_render_device(dscene.handle, ctypes.byref(opts_for(10**6 + w)), film.data_ptr(), sp))
+        torch.cuda.synchronize()
+        launches0 = L.clv_kernel_launches()
+        step_ms = []
+        barrier(world)
+        torch.cuda.synchronize()
+        with ClockSampler(gpu_index) as clocks:
+            wall0 = time.perf_counter()
+            for k in range(args.steps):
+                film.zero_()
+                flush.zero_()  # L2 flush between timed steps
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                _lib.check(L.clv_render_device(dscene.handle, ctypes.byref(opts_for(k)), film.data_ptr(), sp))
+                e1.record(stream)
+                e1.synchronize()
+                step_ms.append(e0.elapsed_time(e1))
+            torch.cuda.synchronize()
+            wall = time.perf_counter() - wall0
+        barrier(world)
+        launches = L.clv_kernel_launches() - launches0
+        ms_step = all_max(world, sum(step_ms) / len(step_ms))
+        samples_step = npix * SPP
+        value = world * samples_step / (ms_step / 1e3) / 1e6
+
+        # e2e: through the host-buffer C ABI (scene upload + render + image download), every step
+        xyz = np.empty((npix, 3), np.float32)
+        host_opts = opts_for(0)
+        e2e_times = []
+        st = _lib.StatsC()
+        h2d = 0
+        for k in range(args.steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            d2 = host_scene.upload()
+            host_opts.sample_offset = (rank * 1000003 + 5000 + k) * SPP
+            _lib.check(L.clv_render(d2.handle, ctypes.byref(host_opts), xyz.ctypes.data, ctypes.byref(st)))
+            e2e_times.append(time.perf_counter() - t0)
+            d2.close()
+        info = host_scene.info()
+        # bytes the upload copies (nodes, records, materials, spectral tables, illuminants, CMF)
+        h2d = (info["nodes"] * 64 + info["triangles"] * 64 + info["quads"] * 64 + info["spheres"] * 16 +
+               info["compound"] * 64 + info["materials"] * 112 + 38 * 400 * 4 + 400 * 12)
+        e2e_s = all_max(world, sum(e2e_times) / len(e2e_times))
+        e2e_value = world * samples_step / e2e_s / 1e6
+
+        # profiling pass (untimed): per-kernel device time and traversal counts for the roofline
+        prof = _lib.RenderProfileC()
+        film.zero_()
+        _lib.check(L.clv_render_profile_run(dscene.handle, ctypes.byref(opts_for(777)), film.data_ptr(), sp,
+                                            ctypes.byref(prof)))
+        torch.cuda.synchronize()
+        segs = prof.path_segments
+        # algorithmic bytes per closest-hit query (one per bounce of a live path):
+        #   intersect: reads meta + origin + direction (48 B), writes the hit (16 B) and a queue entry (4 B),
+        #              and fetches one 64-B node per BVHNode::hit call and one 64-B record per primitive test;
+        #   shade (specular/diffuse/finish): reads the queue entry (4 B), path state + hit (88 B) and writes
+        #              the next state (64 B) per query; per sample 80 B read at the end, 24 B of film and
+        #              72 B for the regenerated path.
+        isect_bytes = segs * (48 + 16 + 4) + 64 * (prof.node_visits + prof.prim_tests)
+        shade_bytes = segs * (4 + 88 + 64) + prof.paths * (80 + 24 + 72)
+        kernels = {"wf_intersect": (prof.ms_intersect, isect_bytes, prof.intersect_launches),
+                   "wf_shade": (prof.ms_shade, shade_bytes, prof.shade_launches)}
+        dom = max(kernels, key=lambda k: kernels[k][0])
+        d_ms, d_bytes, d_launches = kernels[dom]
+        achieved = d_bytes / (d_ms / 1e3) / 1e9
+        roofline = {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",
+                    "frac": round(achieved / hbm_peak, 4), "peak_kind": peak_kind,
+                    "traffic": traffic.get(dom + ".bytes_per_launch"),
+                    "algorithmic_bytes_per_launch": round(d_bytes / max(1, d_launches)),
+                    "kernel_ms_per_step": {k: round(v[0], 3) for k, v in kernels.items()},
+                    "path_segments": segs, "node_visits": prof.node_visits, "prim_tests": prof.prim_tests}
+
+        line = {
+            "metric": "Msamples/s", "value": round(value, 3), "unit": "Msamples/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded enclosed-box scene in the reference's scene format)",
+            "config": {"workload": "enclosed box %dx%d, %d spp, depth %d (wavefront engine)" % (W_IMG, H_IMG, SPP, DEPTH),
+                       "samples_per_step": samples_step, "l2": "flushed between steps (256 MiB write)",
+                       "parallelism": "replicas" if world > 1 else "single GPU", "wall_s_timed_loop": round(wall, 3)},
+            "e2e": {"value": round(e2e_value, 3), "unit": "Msamples/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(npix * 3 * 4)},
+            "gpu_launches": int(launches),
+            "roofline": roofline,
+            "clocks": clocks.summary(),
+        }
 
     # ------------------------------------------------------------- ray casts
     if not args.no_traversal:
@@ -375,7 +388,7 @@ def main():
         t0 = time.perf_counter()
         cg.raycast(dm, rays_h)
         r_e2e = time.perf_counter() - t0
-        trav = {"workload": "2^24 random rays vs 2^20 random triangles (SAH BVH, closest hit)",
+        trav = {"workload": "%d random rays vs %d random triangles (SAH BVH, closest hit)" % (RAYS, TRIS),
                 "metric": "Grays/s", "value": round(RAYS / (r_ms / 1e3) / 1e9, 4), "ms_per_step": round(r_ms, 3),
                 "e2e": {"value": round(RAYS / r_e2e / 1e9, 4), "unit": "Grays/s", "h2d_bytes_per_step": RAYS * 32,
                         "d2h_bytes_per_step": RAYS * 8},
@@ -395,8 +408,10 @@ def main():
                                     "cores": os.cpu_count() or 1, "kind": "port",
                                     "sample": "first %d of the 2^24 rays (%.2f s)" % (n_cpu, el)}
         line["traversal"] = trav
+        if args.no_render:
+            line.update(value=trav["value"], ms_per_step=trav["ms_per_step"])
 
-    if rank == 0 and world == 1 and not args.no_cpu:
+    if rank == 0 and world == 1 and not args.no_cpu and not args.no_render:
         line["cpu_baseline"] = cpu_baseline_render(path, args.cpu_baseline_spp)
     if rank == 0:
         print(json.dumps(line), flush=True)
