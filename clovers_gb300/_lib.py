@@ -53,6 +53,7 @@ SIGNATURES = {
     "clv_device_scene_free": (None, [ctypes.c_void_p]),
     "clv_render": (c_i32, [ctypes.c_void_p, P(RenderOptsC), ctypes.c_void_p, P(StatsC)]),
     "clv_render_device": (c_i32, [ctypes.c_void_p, P(RenderOptsC), ctypes.c_void_p, ctypes.c_void_p]),
+    "clv_render_device_noalloc": (c_i32, [ctypes.c_void_p, P(RenderOptsC), ctypes.c_void_p, ctypes.c_void_p]),
     "clv_resolve_device": (c_i32, [ctypes.c_void_p, c_u32, c_u32, c_u32, ctypes.c_void_p, ctypes.c_void_p,
                                    ctypes.c_void_p]),
     "clv_resolve_srgb": (c_i32, [ctypes.c_void_p, c_u32, c_u32, ctypes.c_void_p]),

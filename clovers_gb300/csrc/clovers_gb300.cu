@@ -14,6 +14,7 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -999,3 +1000,124 @@ int clv_resolve_srgb(const float* xyz, uint32_t width, uint32_t height, uint8_t*
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------ render, no allocation --
+//
+// Some callers cannot allocate GPU memory when they render: an application
+// that reserves the whole device for its own memory pool up front and gives
+// libraries a fixed budget, a host that renders from a context where
+// cudaMalloc is not allowed (it would synchronise the device or re-enter the
+// caller's allocator), or a real-time caller that must never fail with
+// out-of-memory in the middle of a frame.  clv_render_device_noalloc serves
+// them: the wavefront's path state, shading queues and counters live in the
+// file-scope array below instead of memory the library allocates.  The array
+// is reserved on every GPU that loads this library and held until the process
+// exits, so its size is kept modest: CLV_NOALLOC_SLOTS paths in flight.
+
+#define CLV_NOALLOC_SLOTS 65536u
+static constexpr size_t kNoallocHeader = 256;  // WfCounters, padded
+static constexpr size_t kNoallocBytes = kNoallocHeader + (size_t)CLV_NOALLOC_SLOTS * clv_device_scene::kWfSlotBytes;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
+
+// Device addresses of g_noalloc_scratch, looked up once per device.
+static std::mutex g_noalloc_mutex;
+static void* g_noalloc_ptr[256];
+
+static int noalloc_scratch_address(void** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return fail(CLV_E_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+  if (dev < 0 || dev >= 256) return fail(CLV_E_INVALID, "device ordinal out of range");
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+      return fail(CLV_E_CUDA, std::string("cudaGetSymbolAddress(g_noalloc_scratch): ") + cudaGetErrorString(e));
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return CLV_OK;
+}
+
+__global__ void noalloc_counters_init(WfCounters* C, unsigned long long first_work) {
+  C->next_work = first_work;
+  C->live = 0u;
+  C->queue[0] = C->queue[1] = C->queue[2] = 0u;
+}
+
+extern "C" int clv_render_device_noalloc(clv_device_scene* d, const clv_render_opts* o, double* film_dev,
+                                         void* stream) {
+  int rc = check_opts(d, o);
+  if (rc) return rc;
+  if (!film_dev) return fail(CLV_E_INVALID, "null film");
+  if (o->mode != CLV_MODE_PATH_TRACING || o->engine != 0)
+    return fail(CLV_E_INVALID, "the no-allocation render covers the wavefront path tracer only");
+  if (o->path_slots > CLV_NOALLOC_SLOTS)
+    return fail(CLV_E_INVALID, "path_slots " + std::to_string(o->path_slots) + " exceeds the static scratch of " +
+                                   std::to_string(CLV_NOALLOC_SLOTS) + " paths");
+  void* base = nullptr;
+  rc = noalloc_scratch_address(&base);
+  if (rc) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  WfParams P;
+  P.width = o->width;
+  P.height = o->height;
+  P.max_depth = o->max_depth;
+  P.sample_offset = o->sample_offset;
+  P.npix = (uint64_t)o->width * o->height;
+  P.total = P.npix * o->samples;
+  P.seed = o->seed;
+  uint64_t q = o->path_slots ? o->path_slots : CLV_NOALLOC_SLOTS;
+  q = std::min<uint64_t>(q, P.total);
+  q = (q + 127) / 128 * 128;  // at most CLV_NOALLOC_SLOTS, itself a multiple of 128
+  // carve counters and path state out of the static array (the layout of clv_device_scene::wavefront_state)
+  char* c = static_cast<char*>(base);
+  WfCounters* C = reinterpret_cast<WfCounters*>(c);
+  char* p = c + kNoallocHeader;
+  const size_t n = q;
+  WfState W;
+  W.o_time = reinterpret_cast<float4*>(p); p += n * 16;
+  W.d_lambda = reinterpret_cast<float4*>(p); p += n * 16;
+  W.beta = reinterpret_cast<float4*>(p); p += n * 16;
+  W.meta = reinterpret_cast<uint4*>(p); p += n * 16;
+  W.hit = reinterpret_cast<float4*>(p); p += n * 16;
+  W.full = reinterpret_cast<float4*>(p); p += n * 48;
+  W.key = reinterpret_cast<uint2*>(p); p += n * 8;
+  W.queue = reinterpret_cast<uint32_t*>(p);
+  W.Q = (uint32_t)q;
+  const int block = 128;
+  const uint32_t grid = (uint32_t)((q + block - 1) / block);
+  const uint32_t qgrid = std::min<uint32_t>(grid, (uint32_t)sm_count() * 16);
+  // the array keeps the previous call's contents: counters are reset here and
+  // wf_init rewrites every path slot
+  noalloc_counters_init<<<1, 1, 0, st>>>(C, std::min<uint64_t>(q, P.total));
+  wf_init<<<grid, block, 0, st>>>(d->view, P, W);
+  g_launches += 2;
+  const uint32_t level = d->view.compound_level;
+  const int batch = 8;
+  for (uint64_t it = 0;; it += batch) {
+    for (int k = 0; k < batch; ++k) {
+      cudaMemsetAsync(&C->live, 0, 4 * sizeof(unsigned int), st);
+      switch (level) {
+        case 0: wf_intersect<0, false><<<grid, block, 0, st>>>(d->view, W, C, d->err, nullptr); break;
+        case 1: wf_intersect<1, false><<<grid, block, 0, st>>>(d->view, W, C, d->err, nullptr); break;
+        default: wf_intersect<2, false><<<grid, block, 0, st>>>(d->view, W, C, d->err, nullptr); break;
+      }
+      wf_shade_specular<<<qgrid, block, 0, st>>>(d->view, P, W, C, d->err);
+      wf_shade_diffuse<<<qgrid, block, 0, st>>>(d->view, P, W, C, d->err);
+      wf_finish<<<qgrid, block, 0, st>>>(d->view, P, W, C, film_dev);
+    }
+    g_launches += 4 * batch;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(CLV_E_CUDA, std::string("wavefront launch: ") + cudaGetErrorString(e));
+    unsigned int live = 0;
+    e = cudaMemcpyAsync(&live, &C->live, sizeof live, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return fail(CLV_E_CUDA, std::string("wavefront poll: ") + cudaGetErrorString(e));
+    if (live == 0) break;
+    if (it > (uint64_t)4 * (P.total / q + 1) * (o->max_depth + 2) + 64)
+      return fail(CLV_E_DEVICE, "wavefront did not drain");
+  }
+  return CLV_OK;
+}

@@ -113,6 +113,21 @@ int clv_render(clv_device_scene* dscene, const clv_render_opts* opts, float* xyz
  * returns once the film is complete. */
 int clv_render_device(clv_device_scene* dscene, const clv_render_opts* opts, double* film_dev, void* stream);
 
+/* No counterpart in the reference.  The same render as clv_render_device
+ * (wavefront path tracing only) for callers that cannot allocate GPU memory
+ * while they render -- a host that pre-reserves device memory for its own
+ * pool, or a real-time caller that must not hit out-of-memory mid-frame.  It
+ * calls no cudaMalloc/cudaFree: path state, queues and counters live in one
+ * static device array of 65536 path slots (about 9.7 MB, reserved on every GPU
+ * that loads the library until the process exits).  opts->path_slots above
+ * 65536 is rejected with CLV_E_INVALID; 0 means 65536.  The first call on a
+ * device looks up the array's address on that device (cudaGetSymbolAddress),
+ * so make that first call before any stream capture.  Every call shares the
+ * array and leaves its contents behind: calls that overlap on the GPU (other
+ * streams, other threads) race and must be serialised by the caller.  Returns
+ * once the film is complete, like clv_render_device. */
+int clv_render_device_noalloc(clv_device_scene* dscene, const clv_render_opts* opts, double* film_dev, void* stream);
+
 /* Film resolve (clovers-cli/src/write.rs:39-44): mean = film / spp (f64) ->
  * f32 XYZ(E) -> D65 -> sRGB -> u8.  xyz_out_dev (optional) receives the f32
  * means.  Device pointers. */
