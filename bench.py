@@ -207,6 +207,151 @@ def cpu_baseline_render(path, spp_sample):
             "kind": "port", "sample": "512x512 at %d spp (%.2f s)" % (spp_sample, el)}
 
 
+CONFIGS = {
+    # name: (scene builder, width, height, spp, depth, description)
+    "c1": ("random_spheres", 400, 225, 64, 50, "random spheres 400x225, 64 spp, depth 50"),
+    "c3": ("dense_mesh_scene", 1920, 1080, 1024, 12,
+           "displaced geodesic sphere (873,620 triangles), thin film, 1920x1080, 1024 spp, depth 12"),
+    "c4": ("dispersive_prism", 1024, 1024, 256, 16, "dispersive prism + sphere, 1024x1024, depth 16 (plain)"),
+    "box": ("enclosed_box", 512, 512, 256, 16, "enclosed box 512x512, 256 spp, depth 16"),
+}
+GOLDEN = {"c4": "prism", "box": "box", "c1": "spheres"}
+
+
+def config_scene_file(builder, tmp):
+    from clovers_gb300 import scenes
+    if builder == "dispersive_prism":
+        stl = scenes.write_binary_stl(os.path.join(tmp, "prism.stl"), scenes.prism_triangles())
+        sc = scenes.dispersive_prism(stl)
+    elif builder == "dense_mesh_scene":
+        stl = scenes.write_binary_stl(os.path.join(tmp, "ico.stl"), scenes.displaced_icosphere(209))
+        sc = scenes.dense_mesh_scene(stl)
+    elif builder == "random_spheres":
+        sc = scenes.random_spheres(1)
+    else:
+        sc = getattr(scenes, builder)()
+    return scenes.write_scene(sc, os.path.join(tmp, builder + ".json"))
+
+
+def run_batch(args):
+    """64 scenes of uneven size in one wavefront (clv_render_batch) vs the same renders one by one."""
+    import torch
+    import clovers_gb300 as cg
+    from clovers_gb300 import _lib, scenes
+    L = _lib.lib()
+    sp = torch.cuda.current_stream().cuda_stream
+    tmp = tempfile.mkdtemp()
+    dev, opts, films, samples, tris = [], [], [], 0, 0
+    t0 = time.perf_counter()
+    for k in range(args.batch_scenes):
+        sc, w, h, spp = scenes.batch_scene(k, tmp)
+        path = scenes.write_scene(sc, os.path.join(tmp, "batch_%02d.json" % k))
+        hs = cg.Scene.from_json(path, w, h)
+        tris += hs.info()["triangles"]
+        dev.append(hs.upload())
+        opts.append(cg.render_opts(cg.RenderOptions(width=w, height=h, samples=spp, max_depth=DEPTH, seed=100 + k)))
+        films.append(torch.zeros(w * h * 3, dtype=torch.float64, device="cuda"))
+        samples += w * h * spp
+    load_s = time.perf_counter() - t0
+    n = len(dev)
+    handles = (ctypes.c_void_p * n)(*[d.handle.value for d in dev])
+    optarr = (_lib.RenderOptsC * n)(*opts)
+    ptrs = (ctypes.c_void_p * n)(*[f.data_ptr() for f in films])
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fn()
+        e1.record()
+        e1.synchronize()
+        return e0.elapsed_time(e1)
+
+    def batched():
+        _lib.check(L.clv_render_batch(handles, optarr, ptrs, n, sp))
+
+    def one_by_one():
+        for k in range(n):
+            _lib.check(L.clv_render_device(dev[k].handle, ctypes.byref(optarr[k]), films[k].data_ptr(), sp))
+
+    for _ in range(args.warmup):
+        batched()
+    t_batch = min(timed(batched) for _ in range(args.steps))
+    t_seq = min(timed(one_by_one) for _ in range(args.steps))
+    line = {"metric": "Msamples/s", "value": round(samples / (t_batch / 1e3) / 1e6, 3), "unit": "Msamples/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t_batch, 3),
+            "higher_is_better": True, "dtype": "f32", "data": "synthetic (seeds 100..%d)" % (99 + n),
+            "config": {"workload": "%d scenes in one wavefront: displaced geodesic spheres 1k-200k triangles, "
+                                   "0-3 smoke boxes, 128^2-1024^2, 16-512 spp, depth %d" % (n, DEPTH),
+                       "samples_per_step": samples, "triangles": tris, "scene_load_s": round(load_s, 2)},
+            "one_by_one": {"ms": round(t_seq, 3), "value": round(samples / (t_seq / 1e3) / 1e6, 3)}}
+    print(json.dumps(line), flush=True)
+
+
+def run_config(args):
+    """One workload of the configuration list: Msamples/s, and for workloads with a golden
+    oracle crop (tests/golden), the GPU time until the crop's relMSE reaches 1e-3."""
+    import torch
+    import clovers_gb300 as cg
+    from clovers_gb300 import _lib
+    builder, w, h, spp, depth, desc = CONFIGS[args.config]
+    L = _lib.lib()
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    tmp = tempfile.mkdtemp()
+    path = config_scene_file(builder, tmp)
+    t0 = time.perf_counter()
+    host = cg.Scene.from_json(path, w, h)
+    build_s = time.perf_counter() - t0
+    d = host.upload()
+    film = torch.zeros(w * h * 3, dtype=torch.float64, device="cuda")
+
+    def render(n_spp, offset, seed=SEED):
+        o = cg.render_opts(cg.RenderOptions(width=w, height=h, samples=n_spp, max_depth=depth, seed=seed))
+        o.sample_offset = offset
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        _lib.check(L.clv_render_device(d.handle, ctypes.byref(o), film.data_ptr(), sp))
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1)
+
+    for k in range(args.warmup):
+        film.zero_()
+        render(max(1, spp // 16), 10**7 + k * spp)
+    ms = []
+    for k in range(args.steps):
+        film.zero_()
+        ms.append(render(spp, k * spp))
+    ms_step = sum(ms) / len(ms)
+    line = {"metric": "Msamples/s", "value": round(w * h * spp / (ms_step / 1e3) / 1e6, 3), "unit": "Msamples/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3),
+            "higher_is_better": True, "dtype": "f32", "data": "synthetic (seeded generator, reference scene format)",
+            "config": {"workload": desc, "scene_load_and_bvh_s": round(build_s, 3), "objects": host.info()["objects"]}}
+    gold = GOLDEN.get(args.config)
+    gpath = os.path.join(ROOT, "tests", "golden", "%s_ref.npz" % gold) if gold else None
+    if gpath and os.path.exists(gpath):
+        g = np.load(gpath)
+        x0, r0, x1, r1 = [int(v) for v in g["window"]]
+        ref = g["mean"]
+        film.zero_()
+        total_ms, total_spp, chunk = 0.0, 0, args.chunk_spp
+        relmse = None
+        while total_spp < args.max_spp:
+            total_ms += render(chunk, total_spp, seed=SEED + 1000)
+            total_spp += chunk
+            img = (film.view(h, w, 3)[r0:r1, x0:x1].reshape(-1, 3) / total_spp).cpu().numpy()
+            relmse = float(np.mean((img - ref) ** 2 / (ref ** 2 + 1e-2)))
+            if relmse <= 1e-3:
+                break
+        line["time_to_relmse"] = {"target": 1e-3, "reached": bool(relmse is not None and relmse <= 1e-3),
+                                  "gpu_ms": round(total_ms, 2), "spp": total_spp, "relmse": relmse,
+                                  "reference": "oracle, 65536 spp, crop %s of %dx%d (tests/golden/%s_ref.npz)" % (
+                                      [x0, r0, x1, r1], w, h, gold),
+                                  "epsilon": 1e-2, "estimator": "plain (BSDF + light mixture MIS)"}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     global W_IMG, H_IMG, SPP, RAYS, TRIS
     ap = argparse.ArgumentParser()
@@ -222,11 +367,22 @@ def main():
     ap.add_argument("--spp", type=int, default=SPP, help="samples per pixel (reduced cases for profiling)")
     ap.add_argument("--rays", type=int, default=RAYS, help="ray count of the ray-cast section")
     ap.add_argument("--tris", type=int, default=TRIS, help="triangle count of the ray-cast section")
+    ap.add_argument("--config", choices=sorted(CONFIGS), help="measure another workload of the configuration list")
+    ap.add_argument("--chunk-spp", type=int, default=32, help="samples per pixel per progressive pass (relMSE)")
+    ap.add_argument("--max-spp", type=int, default=8192, help="cap of the progressive relMSE measurement")
+    ap.add_argument("--batch", action="store_true", help="measure the batched multi-scene workload")
+    ap.add_argument("--batch-scenes", type=int, default=64)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline legs")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     W_IMG = H_IMG = args.size
     SPP, RAYS, TRIS = args.spp, args.rays, args.tris
+    if args.config:
+        run_config(args)
+        return
+    if args.batch:
+        run_batch(args)
+        return
     world, rank, local = dist_setup(args)
     if args.impl == "reference":
         run_reference(args, world, rank)

@@ -26,8 +26,8 @@ import numpy as np
 from . import _lib
 from ._lib import ClvError, check, lib
 
-__all__ = ["GlobalOptions", "RenderOptions", "Scene", "DeviceScene", "initialize", "draw", "render",
-           "raycast", "resolve_srgb", "ClvError"]
+__all__ = ["GlobalOptions", "RenderOptions", "Scene", "DeviceScene", "initialize", "draw", "draw_batch", "render",
+           "raycast", "resolve_srgb", "ClvError", "DeviceBuffer"]
 
 
 @dataclasses.dataclass
@@ -163,6 +163,47 @@ def draw(global_options: GlobalOptions, render_options: RenderOptions, scene: De
     if stats is not None:
         stats.update(gpu_ms=st.gpu_ms, samples=st.samples, device_errors=st.device_errors,
                      kernel_launches=st.kernel_launches)
+    return out
+
+
+class DeviceBuffer:
+    """Device memory owned by the library's allocator (films, ray buffers)."""
+
+    def __init__(self, nbytes):
+        p = ctypes.c_void_p()
+        check(lib().clv_device_alloc(nbytes, ctypes.byref(p)))
+        self.ptr, self.nbytes = p, nbytes
+
+    def zero(self):
+        check(lib().clv_memset(self.ptr, 0, self.nbytes))
+        return self
+
+    def to_numpy(self, dtype, shape):
+        out = np.empty(shape, dtype)
+        check(lib().clv_memcpy(out.ctypes.data, self.ptr, out.nbytes))
+        return out
+
+    def __del__(self):
+        try:
+            if self.ptr:
+                lib().clv_device_free(self.ptr)
+        except Exception:
+            pass
+
+
+def draw_batch(scenes, options, stats=None):
+    """Renders several scenes in one wavefront (clv_render_batch): a list of (h*w, 3) XYZ(E) means."""
+    n = len(scenes)
+    if n == 0 or n != len(options):
+        raise ValueError("one RenderOptions per scene")
+    opts = (_lib.RenderOptsC * n)(*[render_opts(o) for o in options])
+    films = [DeviceBuffer(o.width * o.height * 3 * 8).zero() for o in options]
+    handles = (ctypes.c_void_p * n)(*[s.handle.value for s in scenes])
+    ptrs = (ctypes.c_void_p * n)(*[f.ptr.value for f in films])
+    check(lib().clv_render_batch(handles, opts, ptrs, n, None))
+    out = []
+    for f, o in zip(films, options):
+        out.append((f.to_numpy(np.float64, (o.width * o.height, 3)) / o.samples).astype(np.float32))
     return out
 
 

@@ -53,6 +53,7 @@ SIGNATURES = {
     "clv_device_scene_free": (None, [ctypes.c_void_p]),
     "clv_render": (c_i32, [ctypes.c_void_p, P(RenderOptsC), ctypes.c_void_p, P(StatsC)]),
     "clv_render_device": (c_i32, [ctypes.c_void_p, P(RenderOptsC), ctypes.c_void_p, ctypes.c_void_p]),
+    "clv_render_batch": (c_i32, [ctypes.c_void_p, P(RenderOptsC), ctypes.c_void_p, c_u32, ctypes.c_void_p]),
     "clv_render_device_noalloc": (c_i32, [ctypes.c_void_p, P(RenderOptsC), ctypes.c_void_p, ctypes.c_void_p]),
     "clv_resolve_device": (c_i32, [ctypes.c_void_p, c_u32, c_u32, c_u32, ctypes.c_void_p, ctypes.c_void_p,
                                    ctypes.c_void_p]),
@@ -64,6 +65,10 @@ SIGNATURES = {
     "clv_device_status": (c_i32, [ctypes.c_void_p, P(c_u32)]),
     "clv_selftest_division": (c_i32, [c_u64, c_u64, P(c_u64)]),
     "clv_kernel_launches": (c_u64, []),
+    "clv_device_alloc": (c_i32, [c_u64, P(ctypes.c_void_p)]),
+    "clv_device_free": (None, [ctypes.c_void_p]),
+    "clv_memcpy": (c_i32, [ctypes.c_void_p, ctypes.c_void_p, c_u64]),
+    "clv_memset": (c_i32, [ctypes.c_void_p, ctypes.c_int, c_u64]),
     "clv_render_profile_run": (c_i32, [ctypes.c_void_p, P(RenderOptsC), ctypes.c_void_p, ctypes.c_void_p,
                                        P(RenderProfileC)]),
     "clv_last_error": (ctypes.c_char_p, []),

@@ -555,6 +555,26 @@ const char* clv_version(void) { return "clovers_gb300 0.1 (sm_103a)"; }
 
 uint64_t clv_kernel_launches(void) { return g_launches.load(); }
 
+int clv_device_alloc(uint64_t bytes, void** out) {
+  if (!out) return fail(CLV_E_INVALID, "null argument");
+  const cudaError_t e = cudaMalloc(out, bytes ? bytes : 1);
+  if (e != cudaSuccess) return fail(CLV_E_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  return CLV_OK;
+}
+void clv_device_free(void* p) {
+  if (p) cudaFree(p);
+}
+int clv_memcpy(void* dst, const void* src, uint64_t bytes) {
+  const cudaError_t e = cudaMemcpy(dst, src, bytes, cudaMemcpyDefault);
+  if (e != cudaSuccess) return fail(CLV_E_CUDA, std::string("cudaMemcpy: ") + cudaGetErrorString(e));
+  return CLV_OK;
+}
+int clv_memset(void* dst, int value, uint64_t bytes) {
+  const cudaError_t e = cudaMemset(dst, value, bytes);
+  if (e != cudaSuccess) return fail(CLV_E_CUDA, std::string("cudaMemset: ") + cudaGetErrorString(e));
+  return CLV_OK;
+}
+
 static int render_wavefront(clv_device_scene* d, const clv_render_opts* o, double* film, cudaStream_t st,
                             clv_render_profile* prof);
 
@@ -816,7 +836,7 @@ static int render_wavefront(clv_device_scene* d, const clv_render_opts* o, doubl
       for (auto& e : evs) ck(cudaEventCreate(&e), "cudaEventCreate");
       ck(cudaEventRecord(evs[4 * batch], st), "cudaEventRecord");
     }
-    wf_init<<<grid, block, 0, st>>>(d->view, P, W);
+    wf_init<false><<<grid, block, 0, st>>>(d->view, P, W, WfBatch{});
     g_launches += 1;
     if (prof) {
       ck(cudaEventRecord(evs[4 * batch + 1], st), "cudaEventRecord");
@@ -830,18 +850,18 @@ static int render_wavefront(clv_device_scene* d, const clv_render_opts* o, doubl
         cudaMemsetAsync(&d->wf_counters->live, 0, 4 * sizeof(unsigned int), st);  // live + 3 queue lengths
         if (prof) cudaEventRecord(evs[4 * k], st);
         switch (level * 2 + (prof ? 1 : 0)) {
-          case 0: wf_intersect<0, false><<<grid, block, 0, st>>>(d->view, W, C, d->err, nullptr); break;
-          case 1: wf_intersect<0, true><<<grid, block, 0, st>>>(d->view, W, C, d->err, dcnt); break;
-          case 2: wf_intersect<1, false><<<grid, block, 0, st>>>(d->view, W, C, d->err, nullptr); break;
-          case 3: wf_intersect<1, true><<<grid, block, 0, st>>>(d->view, W, C, d->err, dcnt); break;
-          case 4: wf_intersect<2, false><<<grid, block, 0, st>>>(d->view, W, C, d->err, nullptr); break;
-          default: wf_intersect<2, true><<<grid, block, 0, st>>>(d->view, W, C, d->err, dcnt); break;
+          case 0: wf_intersect<0, false, false><<<grid, block, 0, st>>>(d->view, W, C, d->err, nullptr, WfBatch{}); break;
+          case 1: wf_intersect<0, true, false><<<grid, block, 0, st>>>(d->view, W, C, d->err, dcnt, WfBatch{}); break;
+          case 2: wf_intersect<1, false, false><<<grid, block, 0, st>>>(d->view, W, C, d->err, nullptr, WfBatch{}); break;
+          case 3: wf_intersect<1, true, false><<<grid, block, 0, st>>>(d->view, W, C, d->err, dcnt, WfBatch{}); break;
+          case 4: wf_intersect<2, false, false><<<grid, block, 0, st>>>(d->view, W, C, d->err, nullptr, WfBatch{}); break;
+          default: wf_intersect<2, true, false><<<grid, block, 0, st>>>(d->view, W, C, d->err, dcnt, WfBatch{}); break;
         }
         if (prof) cudaEventRecord(evs[4 * k + 1], st);
         if (prof) cudaEventRecord(evs[4 * k + 2], st);
-        wf_shade_specular<<<qgrid, block, 0, st>>>(d->view, P, W, C, d->err);
-        wf_shade_diffuse<<<qgrid, block, 0, st>>>(d->view, P, W, C, d->err);
-        wf_finish<<<qgrid, block, 0, st>>>(d->view, P, W, C, film);
+        wf_shade_specular<false><<<qgrid, block, 0, st>>>(d->view, P, W, C, d->err, WfBatch{});
+        wf_shade_diffuse<false><<<qgrid, block, 0, st>>>(d->view, P, W, C, d->err, WfBatch{});
+        wf_finish<false><<<qgrid, block, 0, st>>>(d->view, P, W, C, film, WfBatch{});
         if (prof) cudaEventRecord(evs[4 * k + 3], st);
       }
       g_launches += 4 * batch;
@@ -877,6 +897,109 @@ static int render_wavefront(clv_device_scene* d, const clv_render_opts* o, doubl
     return CLV_OK;
   } catch (std::exception& e) {
     cleanup();
+    return fail(CLV_E_CUDA, e.what());
+  }
+}
+
+int clv_render_batch(clv_device_scene* const* ds, const clv_render_opts* opts, double* const* films, uint32_t n,
+                     void* stream) {
+  if (!ds || !opts || !films || n == 0) return fail(CLV_E_INVALID, "null argument or empty batch");
+  if (n > (1u << 24)) return fail(CLV_E_INVALID, "too many scenes in one batch");
+  for (uint32_t k = 0; k < n; ++k) {
+    const int rc = check_opts(ds[k], &opts[k]);
+    if (rc) return rc;
+    if (!films[k]) return fail(CLV_E_INVALID, "null film");
+    if (opts[k].mode != CLV_MODE_PATH_TRACING) return fail(CLV_E_INVALID, "batches render path tracing only");
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  void* dmem = nullptr;
+  try {
+    std::vector<ClvDeviceScene> views(n);
+    std::vector<WfParams> params(n);
+    std::vector<unsigned long long> prefix(n + 1, 0ull);
+    std::vector<double*> fl(films, films + n);
+    uint32_t level = 0;
+    for (uint32_t k = 0; k < n; ++k) {
+      views[k] = ds[k]->view;
+      const clv_render_opts& o = opts[k];
+      WfParams& P = params[k];
+      P.width = o.width;
+      P.height = o.height;
+      P.max_depth = o.max_depth;
+      P.sample_offset = o.sample_offset;
+      P.npix = (uint64_t)o.width * o.height;
+      P.total = P.npix * o.samples;
+      P.seed = o.seed;
+      prefix[k + 1] = prefix[k] + P.total;
+      level = std::max(level, ds[k]->view.compound_level);
+    }
+    const unsigned long long total = prefix[n];
+    // one staging allocation for the batch tables
+    const size_t b_views = n * sizeof(ClvDeviceScene), b_params = n * sizeof(WfParams);
+    const size_t b_prefix = (n + 1) * sizeof(unsigned long long), b_films = n * sizeof(double*);
+    auto up = [](size_t x) { return (x + 255) / 256 * 256; };
+    const size_t bytes = up(b_views) + up(b_params) + up(b_prefix) + up(b_films);
+    ck(cudaMalloc(&dmem, bytes), "cudaMalloc batch tables");
+    char* c = static_cast<char*>(dmem);
+    WfBatch B;
+    B.scenes = reinterpret_cast<const ClvDeviceScene*>(c);
+    ck(cudaMemcpyAsync(c, views.data(), b_views, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync");
+    c += up(b_views);
+    B.params = reinterpret_cast<const WfParams*>(c);
+    ck(cudaMemcpyAsync(c, params.data(), b_params, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync");
+    c += up(b_params);
+    B.prefix = reinterpret_cast<const unsigned long long*>(c);
+    ck(cudaMemcpyAsync(c, prefix.data(), b_prefix, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync");
+    c += up(b_prefix);
+    B.films = reinterpret_cast<double* const*>(c);
+    ck(cudaMemcpyAsync(c, fl.data(), b_films, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync");
+    B.n = n;
+    B.total = total;
+    clv_device_scene* d0 = ds[0];  // path state, counters and the error word come from the first scene
+    uint64_t q = opts[0].path_slots ? opts[0].path_slots : (uint64_t)sm_count() * 2048 * 4;
+    q = std::min<uint64_t>(q, total);
+    q = (q + 127) / 128 * 128;
+    WfState W = d0->wavefront_state((uint32_t)q);
+    WfCounters c0{std::min<unsigned long long>(q, total), 0u, {0u, 0u, 0u}};
+    ck(cudaMemcpyAsync(d0->wf_counters, &c0, sizeof c0, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync");
+    WfCounters* C = d0->wf_counters;
+    const int block = 128;
+    const uint32_t grid = (uint32_t)((q + block - 1) / block);
+    const uint32_t qgrid = std::min<uint32_t>(grid, (uint32_t)sm_count() * 16);
+    const ClvDeviceScene& S0 = d0->view;
+    const WfParams P0 = params[0];
+    wf_init<true><<<grid, block, 0, st>>>(S0, P0, W, B);
+    g_launches += 1;
+    uint32_t max_depth = 0;
+    for (uint32_t k = 0; k < n; ++k) max_depth = std::max(max_depth, opts[k].max_depth);
+    const int batch = 8;
+    for (uint64_t it = 0;; it += batch) {
+      for (int k = 0; k < batch; ++k) {
+        cudaMemsetAsync(&C->live, 0, 4 * sizeof(unsigned int), st);
+        switch (level) {
+          case 0: wf_intersect<0, false, true><<<grid, block, 0, st>>>(S0, W, C, d0->err, nullptr, B); break;
+          case 1: wf_intersect<1, false, true><<<grid, block, 0, st>>>(S0, W, C, d0->err, nullptr, B); break;
+          default: wf_intersect<2, false, true><<<grid, block, 0, st>>>(S0, W, C, d0->err, nullptr, B); break;
+        }
+        wf_shade_specular<true><<<qgrid, block, 0, st>>>(S0, P0, W, C, d0->err, B);
+        wf_shade_diffuse<true><<<qgrid, block, 0, st>>>(S0, P0, W, C, d0->err, B);
+        wf_finish<true><<<qgrid, block, 0, st>>>(S0, P0, W, C, nullptr, B);
+      }
+      g_launches += 4 * batch;
+      ck(cudaGetLastError(), "wavefront launch");
+      ck(cudaMemcpyAsync(d0->wf_live_host, &C->live, sizeof(unsigned int), cudaMemcpyDeviceToHost, st),
+         "cudaMemcpyAsync");
+      ck(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+      if (*d0->wf_live_host == 0) break;
+      if (it > (uint64_t)4 * (total / q + 1) * (max_depth + 2) + 64) throw std::runtime_error("wavefront did not drain");
+    }
+    cudaFree(dmem);
+    return CLV_OK;
+  } catch (std::exception& e) {
+    if (dmem) {
+      cudaStreamSynchronize(st);
+      cudaFree(dmem);
+    }
     return fail(CLV_E_CUDA, e.what());
   }
 }
@@ -1092,7 +1215,7 @@ extern "C" int clv_render_device_noalloc(clv_device_scene* d, const clv_render_o
   // the array keeps the previous call's contents: counters are reset here and
   // wf_init rewrites every path slot
   noalloc_counters_init<<<1, 1, 0, st>>>(C, std::min<uint64_t>(q, P.total));
-  wf_init<<<grid, block, 0, st>>>(d->view, P, W);
+  wf_init<false><<<grid, block, 0, st>>>(d->view, P, W, WfBatch{});
   g_launches += 2;
   const uint32_t level = d->view.compound_level;
   const int batch = 8;
@@ -1100,13 +1223,13 @@ extern "C" int clv_render_device_noalloc(clv_device_scene* d, const clv_render_o
     for (int k = 0; k < batch; ++k) {
       cudaMemsetAsync(&C->live, 0, 4 * sizeof(unsigned int), st);
       switch (level) {
-        case 0: wf_intersect<0, false><<<grid, block, 0, st>>>(d->view, W, C, d->err, nullptr); break;
-        case 1: wf_intersect<1, false><<<grid, block, 0, st>>>(d->view, W, C, d->err, nullptr); break;
-        default: wf_intersect<2, false><<<grid, block, 0, st>>>(d->view, W, C, d->err, nullptr); break;
+        case 0: wf_intersect<0, false, false><<<grid, block, 0, st>>>(d->view, W, C, d->err, nullptr, WfBatch{}); break;
+        case 1: wf_intersect<1, false, false><<<grid, block, 0, st>>>(d->view, W, C, d->err, nullptr, WfBatch{}); break;
+        default: wf_intersect<2, false, false><<<grid, block, 0, st>>>(d->view, W, C, d->err, nullptr, WfBatch{}); break;
       }
-      wf_shade_specular<<<qgrid, block, 0, st>>>(d->view, P, W, C, d->err);
-      wf_shade_diffuse<<<qgrid, block, 0, st>>>(d->view, P, W, C, d->err);
-      wf_finish<<<qgrid, block, 0, st>>>(d->view, P, W, C, film_dev);
+      wf_shade_specular<false><<<qgrid, block, 0, st>>>(d->view, P, W, C, d->err, WfBatch{});
+      wf_shade_diffuse<false><<<qgrid, block, 0, st>>>(d->view, P, W, C, d->err, WfBatch{});
+      wf_finish<false><<<qgrid, block, 0, st>>>(d->view, P, W, C, film_dev, WfBatch{});
     }
     g_launches += 4 * batch;
     cudaError_t e = cudaGetLastError();

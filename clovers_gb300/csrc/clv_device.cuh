@@ -836,7 +836,14 @@ __device__ float mis_pdf(const ClvDeviceScene& S, V origin, V dir, int lambda, f
       st[sp++] = Frame{CLV_REF_INDEX(ref), 0u, 0.0f};
       ref = n.left;
     }
-    val = ref == CLV_REF_EMPTY ? 0.0f : ObjEval<0>::pdf(S, ref, origin, dir, lambda, time);
+    if (ref == CLV_REF_EMPTY) {
+      val = 0.0f;
+    } else {
+      const uint32_t k = CLV_REF_KIND(ref);
+      if (k == CLV_REF_TRI || k == CLV_REF_QUAD) val = planar_pdf(S, k == CLV_REF_TRI, CLV_REF_INDEX(ref), origin, dir);
+      else if (k == CLV_REF_SPHERE) val = sphere_pdf(load_sphere(S, CLV_REF_INDEX(ref)), origin, dir);
+      else val = ObjEval<0>::pdf(S, ref, origin, dir, lambda, time);
+    }
     // ascend: combine finished values
     while (true) {
       if (sp == 0) return val;

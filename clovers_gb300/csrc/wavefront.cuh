@@ -46,6 +46,26 @@ struct WfParams {
   uint64_t seed;
 };
 
+// Several scenes rendered by one wavefront: the work items of scene s are
+// [prefix[s], prefix[s+1]); a path slot records its scene in meta.w >> 8.
+struct WfBatch {
+  const ClvDeviceScene* scenes;
+  const WfParams* params;
+  const unsigned long long* prefix;  // n + 1 entries
+  double* const* films;
+  uint32_t n;
+  unsigned long long total;
+};
+__device__ __forceinline__ uint32_t wf_scene_of(const WfBatch& B, unsigned long long w) {
+  uint32_t lo = 0, hi = B.n;  // largest s with prefix[s] <= w
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (__ldg(B.prefix + mid) <= w) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
 __device__ __forceinline__ void wf_rotate(int hero, int w[4]) {
 #pragma unroll
   for (int j = 0; j < 4; ++j) w[j] = 380 + (hero - 380 + j * 100) % 400;
@@ -75,25 +95,34 @@ __device__ __forceinline__ Ray wf_camera_ray(const ClvDeviceScene& S, const WfPa
 }
 
 __device__ __forceinline__ void wf_start_path(const ClvDeviceScene& S, const WfParams& P, const WfState& W, uint32_t i,
-                                              uint64_t w) {
+                                              uint64_t w, uint32_t sid) {
   Rng rng;
   uint32_t pixel;
   const Ray r = wf_camera_ray(S, P, w, rng, pixel);
   W.o_time[i] = make_float4(r.o.x, r.o.y, r.o.z, r.time);
   W.d_lambda[i] = make_float4(r.d.x, r.d.y, r.d.z, __int_as_float(r.lambda));
   W.beta[i] = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
-  W.meta[i] = make_uint4(pixel, 0u, rng.counter, 1u);
+  W.meta[i] = make_uint4(pixel, 0u, rng.counter, 1u | (sid << 8));
   W.key[i] = make_uint2((uint32_t)rng.key, (uint32_t)(rng.key >> 32));
 }
 
-__global__ void wf_init(ClvDeviceScene S, WfParams P, WfState W) {
+template <bool BATCH>
+__global__ void wf_init(ClvDeviceScene S, WfParams P, WfState W, WfBatch B) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= W.Q) return;
-  if ((uint64_t)i < P.total) {
-    wf_start_path(S, P, W, i, i);
+  if constexpr (BATCH) {
+    if ((unsigned long long)i < B.total) {
+      const uint32_t sid = wf_scene_of(B, i);
+      wf_start_path(B.scenes[sid], B.params[sid], W, i, i - B.prefix[sid], sid);
+      return;
+    }
   } else {
-    W.meta[i] = make_uint4(0u, 0u, 0u, 0u);
+    if ((uint64_t)i < P.total) {
+      wf_start_path(S, P, W, i, i, 0u);
+      return;
+    }
   }
+  W.meta[i] = make_uint4(0u, 0u, 0u, 0u);
 }
 
 // counters (optional): [0] live paths intersected, [1] BVHNode::hit calls, [2] primitive tests
@@ -133,8 +162,43 @@ __device__ __forceinline__ int material_class(const ClvDeviceScene& S, uint32_t 
 }
 
 template <int CPLX, bool COUNT>
+__device__ __forceinline__ void intersect_slot(const ClvDeviceScene& S, const WfState& W, WfCounters* C, uint32_t* err,
+                                               uint32_t i, const uint4& m, Counters& c) {
+  const float4 a = W.o_time[i], b = W.d_lambda[i];
+  const Ray r{mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, __float_as_int(b.w)};
+  Hit h;
+  Rec full;
+  Rng rng;
+  if (CPLX == 2) {  // media draw randomness inside the traversal
+    const uint2 k = W.key[i];
+    rng.key = (uint64_t)k.x | ((uint64_t)k.y << 32);
+    rng.counter = m.z;
+  }
+  const bool any = closest_hit<CPLX>(S, r, CLV_EPS_ACNE, CLV_FLT_MAX, CPLX == 2 ? &rng : nullptr, h,
+                                     CPLX ? &full : nullptr, COUNT ? &c : nullptr, err);
+  if (CPLX == 2 && rng.counter != m.z) W.meta[i].z = rng.counter;
+  int cls = WF_Q_FINISH;
+  if (any) {
+    const uint32_t kind = CLV_REF_KIND(h.ref), idx = CLV_REF_INDEX(h.ref);
+    uint32_t mat;
+    if (kind == CLV_REF_TRI) mat = S.tri_mat[idx];
+    else if (kind == CLV_REF_QUAD) mat = S.quad_mat[idx];
+    else if (kind == CLV_REF_SPHERE) mat = S.sphere_mat[idx];
+    else mat = full.mat;
+    cls = material_class(S, mat);
+    if (CPLX && kind == CLV_REF_OBJ) {
+      W.full[3 * i] = make_float4(full.p.x, full.p.y, full.p.z, full.u);
+      W.full[3 * i + 1] = make_float4(full.n.x, full.n.y, full.n.z, full.v);
+      W.full[3 * i + 2] = make_float4(full.front ? 1.0f : 0.0f, __uint_as_float(full.mat), 0.0f, 0.0f);
+    }
+  }
+  W.hit[i] = make_float4(any ? h.t : 0.0f, __uint_as_float(any ? h.ref : CLV_REF_EMPTY), h.a, h.b);
+  wf_enqueue(W, C, cls, i);
+}
+
+template <int CPLX, bool COUNT, bool BATCH>
 __global__ void __launch_bounds__(128, CLV_MINB) wf_intersect(ClvDeviceScene S, WfState W, WfCounters* C, uint32_t* err,
-                                                    unsigned long long* cnt) {
+                                                              unsigned long long* cnt, WfBatch B) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   Counters c{0u, 0u};
   uint32_t live = 0;
@@ -142,36 +206,8 @@ __global__ void __launch_bounds__(128, CLV_MINB) wf_intersect(ClvDeviceScene S, 
     const uint4 m = W.meta[i];
     if (m.w & 1u) {
       live = 1;
-      const float4 a = W.o_time[i], b = W.d_lambda[i];
-      const Ray r{mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, __float_as_int(b.w)};
-      Hit h;
-      Rec full;
-      Rng rng;
-      if (CPLX == 2) {  // media draw randomness inside the traversal
-        const uint2 k = W.key[i];
-        rng.key = (uint64_t)k.x | ((uint64_t)k.y << 32);
-        rng.counter = m.z;
-      }
-      const bool any = closest_hit<CPLX>(S, r, CLV_EPS_ACNE, CLV_FLT_MAX, CPLX == 2 ? &rng : nullptr, h,
-                                         CPLX ? &full : nullptr, COUNT ? &c : nullptr, err);
-      if (CPLX == 2 && rng.counter != m.z) W.meta[i].z = rng.counter;
-      int cls = WF_Q_FINISH;
-      if (any) {
-        const uint32_t kind = CLV_REF_KIND(h.ref), idx = CLV_REF_INDEX(h.ref);
-        uint32_t mat;
-        if (kind == CLV_REF_TRI) mat = S.tri_mat[idx];
-        else if (kind == CLV_REF_QUAD) mat = S.quad_mat[idx];
-        else if (kind == CLV_REF_SPHERE) mat = S.sphere_mat[idx];
-        else mat = full.mat;
-        cls = material_class(S, mat);
-        if (CPLX && kind == CLV_REF_OBJ) {
-          W.full[3 * i] = make_float4(full.p.x, full.p.y, full.p.z, full.u);
-          W.full[3 * i + 1] = make_float4(full.n.x, full.n.y, full.n.z, full.v);
-          W.full[3 * i + 2] = make_float4(full.front ? 1.0f : 0.0f, __uint_as_float(full.mat), 0.0f, 0.0f);
-        }
-      }
-      W.hit[i] = make_float4(any ? h.t : 0.0f, __uint_as_float(any ? h.ref : CLV_REF_EMPTY), h.a, h.b);
-      wf_enqueue(W, C, cls, i);
+      if constexpr (BATCH) intersect_slot<CPLX, COUNT>(B.scenes[m.w >> 8], W, C, err, i, m, c);
+      else intersect_slot<CPLX, COUNT>(S, W, C, err, i, m, c);
     }
   }
   if (COUNT) warp_add_counts(cnt, live, c.nodes, c.prims);
@@ -244,7 +280,7 @@ __device__ __forceinline__ bool wf_advance(const WfParams& P, const WfState& W, 
   W.o_time[i] = make_float4(origin.x, origin.y, origin.z, p.ray.time);
   W.d_lambda[i] = make_float4(nd.x, nd.y, nd.z, __int_as_float(p.ray.lambda));
   W.beta[i] = make_float4(p.beta[0], p.beta[1], p.beta[2], p.beta[3]);
-  W.meta[i] = make_uint4(p.meta.x, depth, p.rng.counter, 1u);
+  W.meta[i] = make_uint4(p.meta.x, depth, p.rng.counter, (p.meta.w & ~0xFFu) | 1u);
   return true;
 }
 __device__ __forceinline__ void wf_count_live(WfCounters* C, bool live) {
@@ -253,8 +289,39 @@ __device__ __forceinline__ void wf_count_live(WfCounters* C, bool live) {
 }
 
 // Specular bounce: Metal (metal.rs:27-51), Dielectric / Dispersive (dielectric.rs:37-81, dispersive.rs:58-123)
+__device__ __forceinline__ bool specular_slot(const ClvDeviceScene& S, const WfParams& P, const WfState& W,
+                                              WfCounters* C, uint32_t i) {
+  WfPath p;
+  wf_load(W, i, p);
+  Hit h;
+  Rec rec;
+  wf_hit_record(S, W, i, p.ray, h, rec);
+  const ClvMaterial& m = S.materials[rec.mat];
+  V nd;
+  if (m.kind == CLV_MAT_METAL) {
+    nd = unit(add(reflect(p.ray.d, rec.n), scl(m.fuzz, random_unit_vector(p.rng))));
+  } else {
+    const float ri = m.kind == CLV_MAT_DIELECTRIC ? m.refractive_index : dispersive_index(m, p.ray.lambda);
+    const float ratio = rec.front ? 1.0f / ri : ri;
+    const float ct = fminf(-dot(p.ray.d, rec.n), 1.0f);
+    const float st = sqrtf(1.0f - ct * ct);
+    if (ratio * st > 1.0f) {
+      nd = reflect(p.ray.d, rec.n);
+    } else {
+      const float rp = schlick(ct, ratio);
+      nd = p.rng.f32() < rp ? reflect(p.ray.d, rec.n) : refract(p.ray.d, rec.n, ratio);
+    }
+  }
+  float atten[4];
+  wf_attenuation(S, m, p.ray, rec, atten);
+#pragma unroll
+  for (int j = 0; j < 4; ++j) p.beta[j] = p.beta[j] * atten[j];
+  return wf_advance(P, W, C, i, p, rec.p, nd);
+}
+
+template <bool BATCH>
 __global__ void __launch_bounds__(128) wf_shade_specular(ClvDeviceScene S, WfParams P, WfState W, WfCounters* C,
-                                                         uint32_t* err) {
+                                                         uint32_t* err, WfBatch B) {
   const uint32_t n = C->queue[WF_Q_SPEC];
   const uint32_t stride = gridDim.x * blockDim.x;
   const uint32_t first = blockIdx.x * blockDim.x + threadIdx.x;
@@ -264,40 +331,74 @@ __global__ void __launch_bounds__(128) wf_shade_specular(ClvDeviceScene S, WfPar
     bool live = false;
     if (q < n) {
       const uint32_t i = W.queue[(size_t)WF_Q_SPEC * W.Q + q];
-      WfPath p;
-      wf_load(W, i, p);
-      Hit h;
-      Rec rec;
-      wf_hit_record(S, W, i, p.ray, h, rec);
-      const ClvMaterial& m = S.materials[rec.mat];
-      V nd;
-      if (m.kind == CLV_MAT_METAL) {
-        nd = unit(add(reflect(p.ray.d, rec.n), scl(m.fuzz, random_unit_vector(p.rng))));
+      if constexpr (BATCH) {
+        const uint32_t sid = W.meta[i].w >> 8;
+        live = specular_slot(B.scenes[sid], B.params[sid], W, C, i);
       } else {
-        const float ri = m.kind == CLV_MAT_DIELECTRIC ? m.refractive_index : dispersive_index(m, p.ray.lambda);
-        const float ratio = rec.front ? 1.0f / ri : ri;
-        const float ct = fminf(-dot(p.ray.d, rec.n), 1.0f);
-        const float st = sqrtf(1.0f - ct * ct);
-        if (ratio * st > 1.0f) {
-          nd = reflect(p.ray.d, rec.n);
-        } else {
-          const float rp = schlick(ct, ratio);
-          nd = p.rng.f32() < rp ? reflect(p.ray.d, rec.n) : refract(p.ray.d, rec.n, ratio);
-        }
+        live = specular_slot(S, P, W, C, i);
       }
-      float atten[4];
-      wf_attenuation(S, m, p.ray, rec, atten);
-#pragma unroll
-      for (int j = 0; j < 4; ++j) p.beta[j] = p.beta[j] * atten[j];
-      live = wf_advance(P, W, C, i, p, rec.p, nd);
     }
     wf_count_live(C, live);
   }
 }
 
 // Diffuse bounce: MixturePDF(HitablePDF(priority tree), Cosine/SpherePDF), pdf.rs:122-140, trace.rs:80-119
+__device__ __forceinline__ bool diffuse_slot(const ClvDeviceScene& S, const WfParams& P, const WfState& W,
+                                             WfCounters* C, uint32_t* err, uint32_t i) {
+  WfPath p;
+  wf_load(W, i, p);
+  Hit h;
+  Rec rec;
+  wf_hit_record(S, W, i, p.ray, h, rec);
+  const ClvMaterial& m = S.materials[rec.mat];
+  const bool lamb = m.kind == CLV_MAT_LAMBERTIAN;
+  V gen;
+  if (p.rng.boolean()) {
+    gen = mis_random(S, rec.p, p.rng);
+  } else if (lamb) {  // ONB::build_from_w(normal).local(random_cosine_direction)
+    const V w = rec.n;
+    const V a = fabsf(w.x) > 0.9f ? unit(mk(0.0f, 1.0f, 0.0f)) : unit(mk(1.0f, 0.0f, 0.0f));
+    const V vv = unit(cross(w, a));
+    const V uu = unit(cross(w, vv));
+    const V c = random_cosine_direction(p.rng);
+    gen = unit(add(add(scl(c.x, uu), scl(c.y, vv)), scl(c.z, w)));
+  } else {
+    gen = random_unit_vector(p.rng);
+  }
+  const V nd = unit(gen);
+  const float light_v = mis_pdf(S, rec.p, nd, p.ray.lambda, p.ray.time, err);
+  float bsdf_v;
+  if (lamb) {
+    const float cosine = dot(unit(nd), rec.n);
+    bsdf_v = cosine <= 0.0f ? 0.0f : cosine / CLV_PI;
+  } else {
+    bsdf_v = 1.0f / (4.0f * CLV_PI);
+  }
+  const float mis = 0.5f * light_v + 0.5f * bsdf_v;
+  float spdf;
+  bool scatter = true;
+  if (lamb) {  // Lambertian::scattering_pdf: None below the surface -> emitted (0) only
+    const float cs = dot(rec.n, unit(nd));
+    scatter = !(cs < 0.0f);
+    spdf = cs / CLV_PI;
+  } else {
+    spdf = 1.0f / (4.0f * CLV_PI);
+  }
+  if (!scatter) {
+    W.meta[i].z = p.rng.counter;
+    wf_enqueue(W, C, WF_Q_FINISH, i);
+    return false;
+  }
+  float atten[4];
+  wf_attenuation(S, m, p.ray, rec, atten);
+#pragma unroll
+  for (int j = 0; j < 4; ++j) p.beta[j] = p.beta[j] * (atten[j] * spdf / mis);
+  return wf_advance(P, W, C, i, p, rec.p, nd);
+}
+
+template <bool BATCH>
 __global__ void __launch_bounds__(128) wf_shade_diffuse(ClvDeviceScene S, WfParams P, WfState W, WfCounters* C,
-                                                        uint32_t* err) {
+                                                        uint32_t* err, WfBatch B) {
   const uint32_t n = C->queue[WF_Q_DIFF];
   const uint32_t stride = gridDim.x * blockDim.x;
   const uint32_t first = blockIdx.x * blockDim.x + threadIdx.x;
@@ -307,54 +408,11 @@ __global__ void __launch_bounds__(128) wf_shade_diffuse(ClvDeviceScene S, WfPara
     bool live = false;
     if (q < n) {
       const uint32_t i = W.queue[(size_t)WF_Q_DIFF * W.Q + q];
-      WfPath p;
-      wf_load(W, i, p);
-      Hit h;
-      Rec rec;
-      wf_hit_record(S, W, i, p.ray, h, rec);
-      const ClvMaterial& m = S.materials[rec.mat];
-      const bool lamb = m.kind == CLV_MAT_LAMBERTIAN;
-      V gen;
-      if (p.rng.boolean()) {
-        gen = mis_random(S, rec.p, p.rng);
-      } else if (lamb) {  // ONB::build_from_w(normal).local(random_cosine_direction)
-        const V w = rec.n;
-        const V a = fabsf(w.x) > 0.9f ? unit(mk(0.0f, 1.0f, 0.0f)) : unit(mk(1.0f, 0.0f, 0.0f));
-        const V vv = unit(cross(w, a));
-        const V uu = unit(cross(w, vv));
-        const V c = random_cosine_direction(p.rng);
-        gen = unit(add(add(scl(c.x, uu), scl(c.y, vv)), scl(c.z, w)));
+      if constexpr (BATCH) {
+        const uint32_t sid = W.meta[i].w >> 8;
+        live = diffuse_slot(B.scenes[sid], B.params[sid], W, C, err, i);
       } else {
-        gen = random_unit_vector(p.rng);
-      }
-      const V nd = unit(gen);
-      const float light_v = mis_pdf(S, rec.p, nd, p.ray.lambda, p.ray.time, err);
-      float bsdf_v;
-      if (lamb) {
-        const float cosine = dot(unit(nd), rec.n);
-        bsdf_v = cosine <= 0.0f ? 0.0f : cosine / CLV_PI;
-      } else {
-        bsdf_v = 1.0f / (4.0f * CLV_PI);
-      }
-      const float mis = 0.5f * light_v + 0.5f * bsdf_v;
-      float spdf;
-      bool scatter = true;
-      if (lamb) {  // Lambertian::scattering_pdf: None below the surface -> emitted (0) only
-        const float cs = dot(rec.n, unit(nd));
-        scatter = !(cs < 0.0f);
-        spdf = cs / CLV_PI;
-      } else {
-        spdf = 1.0f / (4.0f * CLV_PI);
-      }
-      if (!scatter) {
-        W.meta[i].z = p.rng.counter;
-        wf_enqueue(W, C, WF_Q_FINISH, i);
-      } else {
-        float atten[4];
-        wf_attenuation(S, m, p.ray, rec, atten);
-#pragma unroll
-        for (int j = 0; j < 4; ++j) p.beta[j] = p.beta[j] * (atten[j] * spdf / mis);
-        live = wf_advance(P, W, C, i, p, rec.p, nd);
+        live = diffuse_slot(S, P, W, C, err, i);
       }
     }
     wf_count_live(C, live);
@@ -389,10 +447,36 @@ __device__ __forceinline__ void film_deposit(const ClvDeviceScene& S, double* fi
   if (a2 != 0.0) atomicAdd(f + 2, a2);
 }
 
-// Ends paths: background on a miss (trace.rs:42-48) or emission of a light
-// (trace.rs:51-58), film deposit, then the slot takes the next work item.
+// Background on a miss (trace.rs:42-48) or emission of a light (trace.rs:51-58), then the film deposit.
+__device__ __forceinline__ void finish_slot(const ClvDeviceScene& S, const WfState& W, double* film, uint32_t i) {
+  const float4 a = W.o_time[i], b = W.d_lambda[i];
+  const Ray ray{mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, __float_as_int(b.w)};
+  const float4 bv = W.beta[i];
+  const float beta[4] = {bv.x, bv.y, bv.z, bv.w};
+  float L[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+  int waves[4];
+  wf_rotate(ray.lambda, waves);
+  Hit h;
+  Rec rec;
+  wf_hit_record(S, W, i, ray, h, rec);
+  if (h.ref == CLV_REF_EMPTY) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) L[j] += beta[j] * spd_get(S, S.background_spd, waves[j]);
+  } else {
+    const ClvMaterial& m = S.materials[rec.mat];
+    if (m.kind == CLV_MAT_DIFFUSELIGHT || m.kind == CLV_MAT_CONELIGHT) {
+#pragma unroll
+      for (int j = 0; j < 4; ++j) L[j] += beta[j] * mat_emit(S, m, ray, waves[j], rec);
+    }
+    // paths that ended in the shade kernels (depth limit, no scatter) add nothing here
+  }
+  film_deposit(S, film, W.meta[i].x, ray.lambda, L);
+}
+
+// Ends paths, then each slot takes the next work item (one atomic per warp).
+template <bool BATCH>
 __global__ void __launch_bounds__(128) wf_finish(ClvDeviceScene S, WfParams P, WfState W, WfCounters* C,
-                                                 double* __restrict__ film) {
+                                                 double* __restrict__ film, WfBatch B) {
   const uint32_t n = C->queue[WF_Q_FINISH];
   const uint32_t stride = gridDim.x * blockDim.x;
   const uint32_t first = blockIdx.x * blockDim.x + threadIdx.x;
@@ -403,31 +487,14 @@ __global__ void __launch_bounds__(128) wf_finish(ClvDeviceScene S, WfParams P, W
     uint32_t i = 0;
     if (q < n) {
       i = W.queue[(size_t)WF_Q_FINISH * W.Q + q];
-      const float4 a = W.o_time[i], b = W.d_lambda[i];
-      const Ray ray{mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, __float_as_int(b.w)};
-      const float4 bv = W.beta[i];
-      const float beta[4] = {bv.x, bv.y, bv.z, bv.w};
-      float L[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-      int waves[4];
-      wf_rotate(ray.lambda, waves);
-      Hit h;
-      Rec rec;
-      wf_hit_record(S, W, i, ray, h, rec);
-      if (h.ref == CLV_REF_EMPTY) {
-#pragma unroll
-        for (int j = 0; j < 4; ++j) L[j] += beta[j] * spd_get(S, S.background_spd, waves[j]);
+      if constexpr (BATCH) {
+        const uint32_t sid = W.meta[i].w >> 8;
+        finish_slot(B.scenes[sid], W, B.films[sid], i);
       } else {
-        const ClvMaterial& m = S.materials[rec.mat];
-        if (m.kind == CLV_MAT_DIFFUSELIGHT || m.kind == CLV_MAT_CONELIGHT) {
-#pragma unroll
-          for (int j = 0; j < 4; ++j) L[j] += beta[j] * mat_emit(S, m, ray, waves[j], rec);
-        }
-        // paths that ended in the shade kernels (depth limit, no scatter) add nothing here
+        finish_slot(S, W, film, i);
       }
-      film_deposit(S, film, W.meta[i].x, ray.lambda, L);
       need = true;
     }
-    // finished paths take new work items, one atomic per warp
     const unsigned mask = __ballot_sync(0xFFFFFFFFu, need);
     bool live = false;
     if (mask) {
@@ -438,11 +505,21 @@ __global__ void __launch_bounds__(128) wf_finish(ClvDeviceScene S, WfParams P, W
       base = __shfl_sync(0xFFFFFFFFu, base, leader);
       if (need) {
         const uint64_t w = base + __popc(mask & ((1u << lane) - 1u));
-        if (w < P.total) {
-          wf_start_path(S, P, W, i, w);
-          live = true;
+        if constexpr (BATCH) {
+          if (w < B.total) {
+            const uint32_t sid = wf_scene_of(B, w);
+            wf_start_path(B.scenes[sid], B.params[sid], W, i, w - B.prefix[sid], sid);
+            live = true;
+          } else {
+            W.meta[i].w = 0u;
+          }
         } else {
-          W.meta[i].w = 0u;
+          if (w < P.total) {
+            wf_start_path(S, P, W, i, w, 0u);
+            live = true;
+          } else {
+            W.meta[i].w = 0u;
+          }
         }
       }
     }

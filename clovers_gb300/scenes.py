@@ -224,3 +224,162 @@ def kitchen_sink(stl_path):
               "vertical_fov": 40.0, "aperture": 0.1, "focus_distance": 13.0}
     return {"time_0": 0, "time_1": 1, "camera": camera, "background_color": [0.05, 0.06, 0.1],
             "objects": objects, "materials": materials}
+
+
+def dispersive_prism(stl_path):
+    """Dispersive-caustics workload: a Sellmeier-glass triangular prism (8 triangles), an r=0.3 glass
+    sphere, two 0.2x0.2 lights of radiance XYZ(E) 50 and a grey 0.5 floor (1024x1024, up to 4096 spp)."""
+    glass = {"name": "sellmeier glass", "kind": "Dispersive", "sellmeier_b": [1.0396, 0.2318, 1.0105],
+             "sellmeier_c": [0.0060, 0.0200, 103.56]}
+    lamp = {"name": "lamp", "kind": "DiffuseLight", "emit": {"kind": "SolidColor", "color": {"xyz_e": [50, 50, 50]}}}
+    floor = {"name": "floor", "kind": "Lambertian", "albedo": {"kind": "SolidColor", "color": [0.5, 0.5, 0.5]}}
+    objects = [
+        {"kind": "Quad", "q": [-5, 0, -5], "u": [10, 0, 0], "v": [0, 0, 10], "material": "floor"},
+        {"kind": "STL", "path": stl_path, "center": [-0.35, 0.35, -0.25], "scale": 0.7, "rotation": [90, 0, 15],
+         "material": "sellmeier glass", "priority": True},
+        {"kind": "Sphere", "priority": True, "center": [0.75, 0.3, 0.1], "radius": 0.3, "material": "sellmeier glass"},
+        {"kind": "Quad", "priority": True, "q": [-0.6, 2.0, -0.1], "u": [0.2, 0, 0], "v": [0, 0, 0.2],
+         "material": "lamp"},
+        {"kind": "Quad", "priority": True, "q": [0.9, 1.6, 0.5], "u": [0.2, 0, 0], "v": [0, 0, 0.2], "material": "lamp"},
+    ]
+    camera = {"look_from": [0.0, 2.2, 3.2], "look_at": [0.1, 0.2, 0.0], "up": [0.0, 1.0, 0.0],
+              "vertical_fov": 40.0, "aperture": 0.0, "focus_distance": 3.5}
+    return {"time_0": 0, "time_1": 1, "camera": camera, "background_color": [0, 0, 0],
+            "objects": objects, "materials": [glass, lamp, floor]}
+
+
+def _hash_noise(p, seed):
+    """Value noise in [-1, 1] on the integer lattice, trilinearly interpolated with smoothstep weights."""
+    i = np.floor(p).astype(np.int64)
+    f = p - i
+    w = f * f * (3.0 - 2.0 * f)
+
+    def h(ix, iy, iz):
+        x = (ix * 73856093) ^ (iy * 19349663) ^ (iz * 83492791) ^ (seed * 2654435761)
+        x = (x ^ (x >> 13)) * 1274126177
+        x = x ^ (x >> 16)
+        return (x & 0xFFFF).astype(np.float64) / 32767.5 - 1.0
+
+    out = 0.0
+    for dx in (0, 1):
+        for dy in (0, 1):
+            for dz in (0, 1):
+                wx = w[:, 0] if dx else 1 - w[:, 0]
+                wy = w[:, 1] if dy else 1 - w[:, 1]
+                wz = w[:, 2] if dz else 1 - w[:, 2]
+                out = out + wx * wy * wz * h(i[:, 0] + dx, i[:, 1] + dy, i[:, 2] + dz)
+    return out
+
+
+def fbm(p, seed, octaves=5):
+    total, amp, freq = 0.0, 0.5, 2.0
+    for _ in range(octaves):
+        total = total + amp * _hash_noise(p * freq, seed)
+        amp *= 0.5
+        freq *= 2.0
+    return total
+
+
+def displaced_icosphere(frequency, seed=3, amplitude=0.15):
+    """Geodesic sphere: each icosahedron face split into frequency^2 triangles (20 f^2 in total),
+    vertices pushed radially by amplitude * fbm(p).  Returns triangles (n, 3, 3) float32."""
+    t = (1.0 + 5 ** 0.5) / 2.0
+    V = np.array([[-1, t, 0], [1, t, 0], [-1, -t, 0], [1, -t, 0], [0, -1, t], [0, 1, t], [0, -1, -t], [0, 1, -t],
+                  [t, 0, -1], [t, 0, 1], [-t, 0, -1], [-t, 0, 1]], np.float64)
+    V /= np.linalg.norm(V, axis=1, keepdims=True)
+    F = [[0, 11, 5], [0, 5, 1], [0, 1, 7], [0, 7, 10], [0, 10, 11], [1, 5, 9], [5, 11, 4], [11, 10, 2], [10, 7, 6],
+         [7, 1, 8], [3, 9, 4], [3, 4, 2], [3, 2, 6], [3, 6, 8], [3, 8, 9], [4, 9, 5], [2, 4, 11], [6, 2, 10],
+         [8, 6, 7], [9, 8, 1]]
+    n = frequency
+    ii, jj = np.meshgrid(np.arange(n + 1), np.arange(n + 1), indexing="ij")
+    mask = ii + jj <= n
+    bi, bj = ii[mask], jj[mask]
+    index = -np.ones((n + 1, n + 1), np.int64)
+    index[bi, bj] = np.arange(bi.size)
+    up = []
+    for i in range(n):
+        for j in range(n - i):
+            up.append((index[i, j], index[i + 1, j], index[i, j + 1]))
+            if i + j + 1 < n:
+                up.append((index[i + 1, j], index[i + 1, j + 1], index[i, j + 1]))
+    up = np.array(up, np.int64)
+    tris = []
+    for a, b, c in F:
+        pa, pb, pc = V[a], V[b], V[c]
+        pts = (pa[None, :] * ((n - bi - bj) / n)[:, None] + pb[None, :] * (bi / n)[:, None] +
+               pc[None, :] * (bj / n)[:, None])
+        pts /= np.linalg.norm(pts, axis=1, keepdims=True)
+        tris.append(pts[up])
+    tris = np.concatenate(tris)  # (20 n^2, 3, 3), unit sphere
+    flat = tris.reshape(-1, 3)
+    r = 1.0 + amplitude * fbm(flat * 2.0, seed)
+    return (flat * r[:, None]).reshape(-1, 3, 3).astype(np.float32)
+
+
+def dense_mesh_scene(stl_path, seed=3):
+    """Dense-mesh workload: a displaced geodesic sphere (frequency 209: 873,620 triangles, the nearest
+    geodesic count to 871k) in a thin-film material (IOR 1.33, thickness U[300,600] nm), a grey 0.5
+    floor and two rectangular lights (1920x1080, 1024 spp, depth 12)."""
+    rng = np.random.default_rng(seed)
+    thickness = float(rng.uniform(300.0, 600.0))
+    mats = [
+        {"name": "iridescent", "kind": "Lambertian", "albedo": {"kind": "SolidColor", "color": [0.8, 0.8, 0.8]},
+         "thin_film": {"refractive_index": 1.33, "thickness": thickness}},
+        {"name": "floor", "kind": "Lambertian", "albedo": {"kind": "SolidColor", "color": [0.5, 0.5, 0.5]}},
+        {"name": "lamp", "kind": "DiffuseLight", "emit": {"kind": "SolidColor", "color": {"xyz_e": [8, 8, 8]}}},
+    ]
+    objects = [
+        {"kind": "Quad", "q": [-20, -1.2, -20], "u": [40, 0, 0], "v": [0, 0, 40], "material": "floor"},
+        {"kind": "STL", "path": stl_path, "center": [0, 0, 0], "scale": 1.0, "rotation": [0, 0, 0],
+         "material": "iridescent"},
+        {"kind": "Quad", "priority": True, "q": [-3, 4, -1], "u": [2, 0, 0], "v": [0, 0, 2], "material": "lamp"},
+        {"kind": "Quad", "priority": True, "q": [2, 3, 1], "u": [0, 0, 1.5], "v": [1.5, 0.5, 0], "material": "lamp"},
+    ]
+    camera = {"look_from": [0.0, 1.0, 4.5], "look_at": [0.0, 0.0, 0.0], "up": [0.0, 1.0, 0.0],
+              "vertical_fov": 40.0, "aperture": 0.0, "focus_distance": 4.5}
+    return {"time_0": 0, "time_1": 1, "camera": camera, "background_color": [0.02, 0.02, 0.03],
+            "objects": objects, "materials": mats}
+
+
+def batch_scene(index, stl_dir):
+    """Scene `index` (0..63, seed 100 + index) of the batched multi-scene workload: a displaced geodesic
+    sphere of 1k-200k triangles (log-uniform; frequency f gives 20 f^2 triangles), 0-3 constant-density
+    smoke boxes (density U[0.01, 0.2]), a Lambertian / dielectric / thin-film sphere material, a grey floor
+    and one area light.  Returns (scene dict, width, height, spp)."""
+    import os
+    rng = np.random.default_rng(100 + index)
+    ntri = float(np.exp(rng.uniform(np.log(1000.0), np.log(200000.0))))
+    freq = max(7, int(round((ntri / 20.0) ** 0.5)))
+    stl = write_binary_stl(os.path.join(stl_dir, "batch_%02d.stl" % index),
+                           displaced_icosphere(freq, seed=100 + index, amplitude=0.15))
+    kind = int(rng.integers(0, 3))
+    if kind == 0:
+        mat = {"name": "body", "kind": "Lambertian",
+               "albedo": {"kind": "SolidColor", "color": [float(x) for x in rng.uniform(0.2, 0.9, 3)]}}
+    elif kind == 1:
+        mat = {"name": "body", "kind": "Dielectric", "refractive_index": float(rng.uniform(1.3, 1.7))}
+    else:
+        mat = {"name": "body", "kind": "Lambertian", "albedo": {"kind": "SolidColor", "color": [0.8, 0.8, 0.8]},
+               "thin_film": {"refractive_index": 1.33, "thickness": float(rng.uniform(300.0, 600.0))}}
+    objects = [
+        {"kind": "Quad", "q": [-10, -1.2, -10], "u": [20, 0, 0], "v": [0, 0, 20], "material": "floor"},
+        {"kind": "STL", "path": stl, "center": [0, 0, 0], "scale": 1.0, "rotation": [0, 0, 0], "material": "body"},
+        {"kind": "Quad", "priority": True, "q": [-1.5, 3.5, -1.5], "u": [3, 0, 0], "v": [0, 0, 3], "material": "lamp"},
+    ]
+    for k in range(int(rng.integers(0, 4))):
+        c = rng.uniform(-2.5, 2.5, 3)
+        c[1] = rng.uniform(-1.0, 0.5)
+        s = rng.uniform(0.4, 1.0, 3)
+        objects.append({"kind": "ConstantMedium", "density": float(rng.uniform(0.01, 0.2)),
+                        "boundary": {"kind": "Boxy", "corner_0": [float(x) for x in c],
+                                     "corner_1": [float(x) for x in c + s]},
+                        "texture": {"kind": "SolidColor", "color": [0.9, 0.9, 0.9]}})
+    materials = [mat,
+                 {"name": "floor", "kind": "Lambertian", "albedo": {"kind": "SolidColor", "color": [0.5, 0.5, 0.5]}},
+                 {"name": "lamp", "kind": "DiffuseLight", "emit": {"kind": "SolidColor", "color": {"xyz_e": [6, 6, 6]}}}]
+    camera = {"look_from": [0.0, 1.0, 4.5], "look_at": [0.0, 0.0, 0.0], "up": [0.0, 1.0, 0.0],
+              "vertical_fov": 45.0, "aperture": 0.0, "focus_distance": 4.5}
+    side = int(2 ** rng.uniform(7, 10)) // 8 * 8
+    spp = int(2 ** int(rng.integers(4, 10)))
+    return ({"time_0": 0, "time_1": 1, "camera": camera, "background_color": [0.05, 0.05, 0.08],
+             "objects": objects, "materials": materials}, side, side, spp)

@@ -113,6 +113,16 @@ int clv_render(clv_device_scene* dscene, const clv_render_opts* opts, float* xyz
  * returns once the film is complete. */
 int clv_render_device(clv_device_scene* dscene, const clv_render_opts* opts, double* film_dev, void* stream);
 
+/* Renders n scenes in one wavefront: the (pixel, sample) work of all scenes
+ * shares one set of path slots and one sequence of kernel launches per bounce,
+ * so scenes of uneven size keep the GPU full.  Each scene adds its film sums
+ * into films[k] (width*height*3 doubles, caller-zeroed), exactly as n calls of
+ * clv_render_device with the same options would (same random streams).  The
+ * path state of the batch lives in dscenes[0].  No counterpart in the
+ * reference, which renders one scene per process. */
+int clv_render_batch(clv_device_scene* const* dscenes, const clv_render_opts* opts, double* const* films, uint32_t n,
+                     void* stream);
+
 /* No counterpart in the reference.  The same render as clv_render_device
  * (wavefront path tracing only) for callers that cannot allocate GPU memory
  * while they render -- a host that pre-reserves device memory for its own
@@ -160,6 +170,14 @@ int clv_device_status(clv_device_scene* dscene, uint32_t* flags_out);
 
 const char* clv_last_error(void);
 const char* clv_version(void);
+
+/* Device memory plumbing for callers without their own CUDA runtime binding
+ * (films and ray buffers of the *_device entry points).  clv_memcpy copies in
+ * any direction (unified addressing); both block. */
+int clv_device_alloc(uint64_t bytes, void** out);
+void clv_device_free(void* ptr);
+int clv_memcpy(void* dst, const void* src, uint64_t bytes);
+int clv_memset(void* dst, int value, uint64_t bytes);
 
 /* Number of kernels this library has launched since it was loaded. */
 uint64_t clv_kernel_launches(void);
