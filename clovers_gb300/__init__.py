@@ -27,7 +27,7 @@ from . import _lib
 from ._lib import ClvError, check, lib
 
 __all__ = ["GlobalOptions", "RenderOptions", "Scene", "DeviceScene", "initialize", "draw", "draw_batch", "render",
-           "raycast", "resolve_srgb", "ClvError", "DeviceBuffer"]
+           "raycast", "resolve_srgb", "ClvError", "DeviceBuffer", "Guide", "draw_guided"]
 
 
 @dataclasses.dataclass
@@ -205,6 +205,110 @@ def draw_batch(scenes, options, stats=None):
     for f, o in zip(films, options):
         out.append((f.to_numpy(np.float64, (o.width * o.height, 3)) / o.samples).astype(np.float32))
     return out
+
+
+GUIDE_PARAMS = 22016
+GUIDE_OUTPUTS = 40
+
+
+class Guide:
+    """The learned path guide (clv_guide_*): an MLP that maps a Lambertian path
+    vertex to an 8-lobe von Mises-Fisher mixture over incident directions,
+    trained online on the records of guided renders.  No counterpart in the
+    reference."""
+
+    def __init__(self, record_capacity=0, learning_rate=0.0, seed=0):
+        o = _lib.GuideOptsC(record_capacity, learning_rate, seed)
+        h = ctypes.c_void_p()
+        check(lib().clv_guide_create(ctypes.byref(o), ctypes.byref(h)))
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def params(self):
+        p = np.empty(GUIDE_PARAMS, np.float32)
+        check(lib().clv_guide_get_params(self._h, p.ctypes.data))
+        return p
+
+    def set_params(self, p):
+        a = np.ascontiguousarray(p, np.float32).reshape(GUIDE_PARAMS)
+        check(lib().clv_guide_set_params(self._h, a.ctypes.data))
+
+    def forward(self, queries):
+        """Raw outputs (n, 40) for normalised inputs (n, 8) = u0..u6, 0."""
+        q = np.ascontiguousarray(queries, np.float32).reshape(-1, 8)
+        out = np.empty((q.shape[0], GUIDE_OUTPUTS), np.float32)
+        check(lib().clv_guide_forward(self._h, q.ctypes.data, q.shape[0], out.ctypes.data))
+        return out
+
+    def gradient(self, records):
+        """(gradient sums (22016,), loss sum) of -f log q(w) over records (n, 12)."""
+        r = np.ascontiguousarray(records, np.float32).reshape(-1, 12)
+        g = np.empty(GUIDE_PARAMS, np.float32)
+        loss = ctypes.c_double()
+        check(lib().clv_guide_gradient(self._h, r.ctypes.data, r.shape[0], g.ctypes.data, ctypes.byref(loss)))
+        return g, loss.value
+
+    def train(self, steps, batch=0, stream=None):
+        """Adam steps on the records of the last guided render; returns their mean loss."""
+        loss = ctypes.c_double()
+        check(lib().clv_guide_train(self._h, steps, batch, ctypes.byref(loss), stream))
+        return loss.value
+
+    def records(self):
+        """Training records (n, 12) of the last guided render: u0..u6, 0, w.xyz, f."""
+        n = ctypes.c_uint64()
+        check(lib().clv_guide_record_count(self._h, ctypes.byref(n)))
+        out = np.empty((n.value, 12), np.float32)
+        check(lib().clv_guide_get_records(self._h, out.ctypes.data, n.value))
+        return out
+
+    def status(self):
+        f = ctypes.c_uint32()
+        check(lib().clv_guide_status(self._h, ctypes.byref(f)))
+        return f.value
+
+    def close(self):
+        if self._h and self._h.value:
+            lib().clv_guide_free(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def render_guided(scene: DeviceScene, render_options: RenderOptions, guide: Guide, alpha, film: "DeviceBuffer",
+                  sample_offset=0, stream=None):
+    """One guided render pass adding its film sums into `film` (clv_render_guided)."""
+    o = render_opts(render_options, sample_offset=sample_offset)
+    check(lib().clv_render_guided(scene.handle, ctypes.byref(o), guide.handle, alpha, film.ptr, stream))
+
+
+def draw_guided(global_options: GlobalOptions, render_options: RenderOptions, scene: DeviceScene, guide=None,
+                pass_spp=16, alpha=0.5, train_steps=8, train_batch=0, warmup_passes=1):
+    """draw() with online path guiding: passes of `pass_spp` samples per pixel,
+    the first `warmup_passes` with alpha 0 (the reference's estimator), each
+    followed by `train_steps` Adam steps on the pass's records.  Returns the
+    (height*width, 3) float32 XYZ(E) means, like draw()."""
+    del global_options
+    guide = guide or Guide()
+    w, h, spp = render_options.width, render_options.height, render_options.samples
+    film = DeviceBuffer(w * h * 3 * 8).zero()
+    done, k = 0, 0
+    while done < spp:
+        n = min(pass_spp, spp - done)
+        opts = dataclasses.replace(render_options, samples=n)
+        render_guided(scene, opts, guide, 0.0 if k < warmup_passes else alpha, film, sample_offset=done)
+        if train_steps:
+            guide.train(train_steps, train_batch)
+        done += n
+        k += 1
+    return (film.to_numpy(np.float64, (w * h, 3)) / spp).astype(np.float32)
 
 
 def raycast(scene: DeviceScene, rays, with_counts=False):

@@ -35,6 +35,10 @@ class StatsC(ctypes.Structure):
     _fields_ = [("gpu_ms", c_f64), ("samples", c_u64), ("device_errors", c_u32), ("kernel_launches", c_u32)]
 
 
+class GuideOptsC(ctypes.Structure):
+    _fields_ = [("record_capacity", c_u32), ("learning_rate", c_f32), ("seed", c_u64)]
+
+
 class RenderProfileC(ctypes.Structure):
     _fields_ = [("ms_init", c_f64), ("ms_intersect", c_f64), ("ms_shade", c_f64), ("intersect_launches", c_u64),
                 ("shade_launches", c_u64), ("paths", c_u64), ("path_segments", c_u64), ("node_visits", c_u64),
@@ -71,6 +75,19 @@ SIGNATURES = {
     "clv_memset": (c_i32, [ctypes.c_void_p, ctypes.c_int, c_u64]),
     "clv_render_profile_run": (c_i32, [ctypes.c_void_p, P(RenderOptsC), ctypes.c_void_p, ctypes.c_void_p,
                                        P(RenderProfileC)]),
+    "clv_guide_create": (c_i32, [P(GuideOptsC), P(ctypes.c_void_p)]),
+    "clv_guide_free": (None, [ctypes.c_void_p]),
+    "clv_guide_get_params": (c_i32, [ctypes.c_void_p, ctypes.c_void_p]),
+    "clv_guide_set_params": (c_i32, [ctypes.c_void_p, ctypes.c_void_p]),
+    "clv_render_guided": (c_i32, [ctypes.c_void_p, P(RenderOptsC), ctypes.c_void_p, c_f32, ctypes.c_void_p,
+                                  ctypes.c_void_p]),
+    "clv_guide_train": (c_i32, [ctypes.c_void_p, c_u32, c_u32, P(c_f64), ctypes.c_void_p]),
+    "clv_guide_record_count": (c_i32, [ctypes.c_void_p, P(c_u64)]),
+    "clv_guide_get_records": (c_i32, [ctypes.c_void_p, ctypes.c_void_p, c_u64]),
+    "clv_guide_forward": (c_i32, [ctypes.c_void_p, ctypes.c_void_p, c_u64, ctypes.c_void_p]),
+    "clv_guide_gradient": (c_i32, [ctypes.c_void_p, ctypes.c_void_p, c_u64, ctypes.c_void_p, P(c_f64)]),
+    "clv_guide_status": (c_i32, [ctypes.c_void_p, P(c_u32)]),
+    "clv_guide_selftest_mma": (c_i32, [c_u32, c_u32, c_u64, ctypes.c_void_p, P(c_f32)]),
     "clv_last_error": (ctypes.c_char_p, []),
     "clv_version": (ctypes.c_char_p, []),
 }

@@ -407,6 +407,9 @@ int sm_count() {
 
 }  // namespace
 
+int clv_internal_fail(int code, const char* msg) { return fail(code, msg); }
+void clv_internal_count_launches(unsigned long long n) { g_launches += n; }
+
 struct clv_scene {
   clv::HostScene host;
 };
@@ -492,9 +495,13 @@ struct clv_device_scene {
     W.key = reinterpret_cast<uint2*>(p); p += n * 8;
     W.queue = reinterpret_cast<uint32_t*>(p);
     W.Q = q;
+    W.gslot = nullptr;
+    W.grec = nullptr;
+    W.grec_count = nullptr;
+    W.grec_cap = 0;
     return W;
   }
-  static constexpr size_t kWfSlotBytes = 16 * 5 + 48 + 8 + 12;
+  static constexpr size_t kWfSlotBytes = 16 * 5 + 48 + 8 + 16;
   void* ensure_scratch(size_t bytes) {
     if (bytes > scratch_bytes) {
       if (scratch) cudaFree(scratch);
@@ -576,7 +583,7 @@ int clv_memset(void* dst, int value, uint64_t bytes) {
 }
 
 static int render_wavefront(clv_device_scene* d, const clv_render_opts* o, double* film, cudaStream_t st,
-                            clv_render_profile* prof);
+                            clv_render_profile* prof, clv_guide* guide = nullptr, float alpha = 0.0f);
 
 int clv_render_profile_run(clv_device_scene* d, const clv_render_opts* o, double* film_dev, void* stream,
                            clv_render_profile* out) {
@@ -796,8 +803,10 @@ int clv_raycast(clv_device_scene* d, const float* rays, uint64_t n, uint32_t* pr
 
 // Wavefront render loop.  With `prof` set, each intersect and shade launch is
 // bracketed by events and the traversal work is counted (diagnostic runs).
+// With `guide` set, Lambertian bounces go through the guided kernels (a share
+// alpha drawn from the guide network) and leave training records.
 static int render_wavefront(clv_device_scene* d, const clv_render_opts* o, double* film, cudaStream_t st,
-                            clv_render_profile* prof) {
+                            clv_render_profile* prof, clv_guide* guide, float alpha) {
   std::vector<cudaEvent_t> evs;
   unsigned long long* dcnt = nullptr;
   auto cleanup = [&]() {
@@ -819,8 +828,20 @@ static int render_wavefront(clv_device_scene* d, const clv_render_opts* o, doubl
     q = std::min<uint64_t>(q, P.total);
     q = (q + 127) / 128 * 128;
     WfState W = d->wavefront_state((uint32_t)q);
-    WfCounters c0{std::min<uint64_t>(q, P.total), 0u, {0u, 0u, 0u}};
+    WfCounters c0{std::min<uint64_t>(q, P.total), 0u, {0u, 0u, 0u, 0u}};
     ck(cudaMemcpyAsync(d->wf_counters, &c0, sizeof c0, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync");
+    GuideDev G{};
+    GdQueue GQ{};
+    if (guide) {
+      W.gslot = guide->ensure_slots((uint32_t)q);
+      W.grec = guide->rec;
+      W.grec_count = guide->rec_count;
+      W.grec_cap = guide->rec_cap;
+      gd_reset_records(guide, st);
+      G = gd_view(guide, d->view.root_box, alpha);
+      GQ = GdQueue{W.queue + (size_t)WF_Q_GUIDE * q, &d->wf_counters->queue[WF_Q_GUIDE], W.full, W.d_lambda, W.hit,
+                   W.meta, W.key};
+    }
     const int block = 128;
     const uint32_t grid = (uint32_t)((q + block - 1) / block);
     const uint32_t level = d->view.compound_level;
@@ -847,7 +868,7 @@ static int render_wavefront(clv_device_scene* d, const clv_render_opts* o, doubl
     }
     for (uint64_t it = 0;; it += batch) {
       for (int k = 0; k < batch; ++k) {
-        cudaMemsetAsync(&d->wf_counters->live, 0, 4 * sizeof(unsigned int), st);  // live + 3 queue lengths
+        cudaMemsetAsync(&d->wf_counters->live, 0, 5 * sizeof(unsigned int), st);  // live + 4 queue lengths
         if (prof) cudaEventRecord(evs[4 * k], st);
         switch (level * 2 + (prof ? 1 : 0)) {
           case 0: wf_intersect<0, false, false><<<grid, block, 0, st>>>(d->view, W, C, d->err, nullptr, WfBatch{}); break;
@@ -861,6 +882,12 @@ static int render_wavefront(clv_device_scene* d, const clv_render_opts* o, doubl
         if (prof) cudaEventRecord(evs[4 * k + 2], st);
         wf_shade_specular<false><<<qgrid, block, 0, st>>>(d->view, P, W, C, d->err, WfBatch{});
         wf_shade_diffuse<false><<<qgrid, block, 0, st>>>(d->view, P, W, C, d->err, WfBatch{});
+        if (guide) {
+          wf_guide_pre<<<qgrid, block, 0, st>>>(d->view, W, C, alpha);
+          if (alpha > 0.0f) gd_launch_queue(G, GQ, (uint32_t)q, st);
+          wf_guide_post<<<qgrid, block, 0, st>>>(d->view, P, W, C, d->err, G);
+          g_launches += 2;
+        }
         wf_finish<false><<<qgrid, block, 0, st>>>(d->view, P, W, C, film, WfBatch{});
         if (prof) cudaEventRecord(evs[4 * k + 3], st);
       }
@@ -960,7 +987,7 @@ int clv_render_batch(clv_device_scene* const* ds, const clv_render_opts* opts, d
     q = std::min<uint64_t>(q, total);
     q = (q + 127) / 128 * 128;
     WfState W = d0->wavefront_state((uint32_t)q);
-    WfCounters c0{std::min<unsigned long long>(q, total), 0u, {0u, 0u, 0u}};
+    WfCounters c0{std::min<unsigned long long>(q, total), 0u, {0u, 0u, 0u, 0u}};
     ck(cudaMemcpyAsync(d0->wf_counters, &c0, sizeof c0, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync");
     WfCounters* C = d0->wf_counters;
     const int block = 128;
@@ -975,7 +1002,7 @@ int clv_render_batch(clv_device_scene* const* ds, const clv_render_opts* opts, d
     const int batch = 8;
     for (uint64_t it = 0;; it += batch) {
       for (int k = 0; k < batch; ++k) {
-        cudaMemsetAsync(&C->live, 0, 4 * sizeof(unsigned int), st);
+        cudaMemsetAsync(&C->live, 0, 5 * sizeof(unsigned int), st);
         switch (level) {
           case 0: wf_intersect<0, false, true><<<grid, block, 0, st>>>(S0, W, C, d0->err, nullptr, B); break;
           case 1: wf_intersect<1, false, true><<<grid, block, 0, st>>>(S0, W, C, d0->err, nullptr, B); break;
@@ -1002,6 +1029,26 @@ int clv_render_batch(clv_device_scene* const* ds, const clv_render_opts* opts, d
     }
     return fail(CLV_E_CUDA, e.what());
   }
+}
+
+int clv_render_guided(clv_device_scene* d, const clv_render_opts* o, clv_guide* g, float alpha, double* film_dev,
+                      void* stream) {
+  int rc = check_opts(d, o);
+  if (rc) return rc;
+  if (!g || !film_dev) return fail(CLV_E_INVALID, "null argument");
+  if (o->mode != CLV_MODE_PATH_TRACING || o->engine != 0)
+    return fail(CLV_E_INVALID, "guided renders use the wavefront path tracer");
+  if (!(alpha >= 0.0f && alpha <= 1.0f)) return fail(CLV_E_INVALID, "alpha must lie in [0, 1]");
+  rc = render_wavefront(d, o, film_dev, (cudaStream_t)stream, nullptr, g, alpha);
+  if (rc) return rc;
+  uint32_t e = 0;
+  if (cudaMemcpy(&e, g->err, sizeof e, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return fail(CLV_E_CUDA, "cudaMemcpy D2H");
+  if (e) {
+    cudaMemset(g->err, 0, sizeof e);
+    return fail(CLV_E_DEVICE, "guide kernel timed out waiting for the tensor cores");
+  }
+  return CLV_OK;
 }
 
 int clv_render_device(clv_device_scene* d, const clv_render_opts* o, double* film_dev, void* stream) {
@@ -1166,7 +1213,7 @@ static int noalloc_scratch_address(void** out) {
 __global__ void noalloc_counters_init(WfCounters* C, unsigned long long first_work) {
   C->next_work = first_work;
   C->live = 0u;
-  C->queue[0] = C->queue[1] = C->queue[2] = 0u;
+  C->queue[0] = C->queue[1] = C->queue[2] = C->queue[3] = 0u;
 }
 
 extern "C" int clv_render_device_noalloc(clv_device_scene* d, const clv_render_opts* o, double* film_dev,
@@ -1209,6 +1256,10 @@ extern "C" int clv_render_device_noalloc(clv_device_scene* d, const clv_render_o
   W.key = reinterpret_cast<uint2*>(p); p += n * 8;
   W.queue = reinterpret_cast<uint32_t*>(p);
   W.Q = (uint32_t)q;
+  W.gslot = nullptr;
+  W.grec = nullptr;
+  W.grec_count = nullptr;
+  W.grec_cap = 0;
   const int block = 128;
   const uint32_t grid = (uint32_t)((q + block - 1) / block);
   const uint32_t qgrid = std::min<uint32_t>(grid, (uint32_t)sm_count() * 16);
@@ -1221,7 +1272,7 @@ extern "C" int clv_render_device_noalloc(clv_device_scene* d, const clv_render_o
   const int batch = 8;
   for (uint64_t it = 0;; it += batch) {
     for (int k = 0; k < batch; ++k) {
-      cudaMemsetAsync(&C->live, 0, 4 * sizeof(unsigned int), st);
+      cudaMemsetAsync(&C->live, 0, 5 * sizeof(unsigned int), st);
       switch (level) {
         case 0: wf_intersect<0, false, false><<<grid, block, 0, st>>>(d->view, W, C, d->err, nullptr, WfBatch{}); break;
         case 1: wf_intersect<1, false, false><<<grid, block, 0, st>>>(d->view, W, C, d->err, nullptr, WfBatch{}); break;

@@ -15,11 +15,12 @@
 #pragma once
 
 #include "clv_device.cuh"
+#include "guide.cuh"
 
 namespace clvd {
 
 struct WfState {
-  uint32_t* queue;   // 3 * Q slot indices, one segment per class
+  uint32_t* queue;   // 4 * Q slot indices, one segment per class
   float4* o_time;    // origin.xyz, time
   float4* d_lambda;  // direction.xyz, wavelength (int bits)
   float4* beta;      // throughput per wavelength (only lights and the background
@@ -29,15 +30,22 @@ struct WfState {
   float4* hit;       // t, ref bits, a, b
   float4* full;      // 3 per slot: p.xyz u | n.xyz v | front, material
   uint32_t Q;
+  // guided renders only (null otherwise): per slot the training-record ids of
+  // the path's first two guided vertices and its hero throughput before each
+  uint4* gslot;
+  float4* grec;
+  unsigned int* grec_count;
+  uint32_t grec_cap;
 };
 
 #define WF_Q_FINISH 0  // misses, emitters and paths ended in the shade kernels
 #define WF_Q_SPEC 1    // metal, dielectric, dispersive
-#define WF_Q_DIFF 2    // lambertian, isotropic
+#define WF_Q_DIFF 2    // lambertian, isotropic (isotropic only in guided renders)
+#define WF_Q_GUIDE 3   // lambertian in guided renders
 struct WfCounters {
   unsigned long long next_work;  // next unassigned work item
   unsigned int live;             // live paths after the last shading pass
-  unsigned int queue[3];         // per-class queue lengths of this bounce
+  unsigned int queue[4];         // per-class queue lengths of this bounce
 };
 
 struct WfParams {
@@ -104,6 +112,7 @@ __device__ __forceinline__ void wf_start_path(const ClvDeviceScene& S, const WfP
   W.beta[i] = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
   W.meta[i] = make_uint4(pixel, 0u, rng.counter, 1u | (sid << 8));
   W.key[i] = make_uint2((uint32_t)rng.key, (uint32_t)(rng.key >> 32));
+  if (W.gslot) W.gslot[i] = make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u);
 }
 
 template <bool BATCH>
@@ -154,9 +163,10 @@ __device__ __forceinline__ void wf_enqueue(const WfState& W, WfCounters* C, int 
   W.queue[(size_t)cls * W.Q + base + __popc(peers & ((1u << lane) - 1u))] = i;
 }
 
-__device__ __forceinline__ int material_class(const ClvDeviceScene& S, uint32_t mat) {
+__device__ __forceinline__ int material_class(const ClvDeviceScene& S, uint32_t mat, bool guided) {
   const uint32_t k = S.materials[mat].kind;
-  if (k == CLV_MAT_LAMBERTIAN || k == CLV_MAT_ISOTROPIC) return WF_Q_DIFF;
+  if (k == CLV_MAT_LAMBERTIAN) return guided ? WF_Q_GUIDE : WF_Q_DIFF;
+  if (k == CLV_MAT_ISOTROPIC) return WF_Q_DIFF;
   if (k == CLV_MAT_DIFFUSELIGHT || k == CLV_MAT_CONELIGHT) return WF_Q_FINISH;
   return WF_Q_SPEC;
 }
@@ -185,7 +195,7 @@ __device__ __forceinline__ void intersect_slot(const ClvDeviceScene& S, const Wf
     else if (kind == CLV_REF_QUAD) mat = S.quad_mat[idx];
     else if (kind == CLV_REF_SPHERE) mat = S.sphere_mat[idx];
     else mat = full.mat;
-    cls = material_class(S, mat);
+    cls = material_class(S, mat, W.gslot != nullptr);
     if (CPLX && kind == CLV_REF_OBJ) {
       W.full[3 * i] = make_float4(full.p.x, full.p.y, full.p.z, full.u);
       W.full[3 * i + 1] = make_float4(full.n.x, full.n.y, full.n.z, full.v);
@@ -419,6 +429,133 @@ __global__ void __launch_bounds__(128) wf_shade_diffuse(ClvDeviceScene S, WfPara
   }
 }
 
+// ---- guided Lambertian bounces: pre -> guide network (guide.cu) -> post ----
+// pre: the hit record goes to the slot's record area (W.full) and a coin picks
+// the strategy; bounces that use the reference's MixturePDF (probability
+// 1 - alpha) draw their direction here, exactly as diffuse_slot does.
+// W.hit then holds {direction, 0} or {-, 1} (guide to sample).
+__device__ __forceinline__ void guide_pre_slot(const ClvDeviceScene& S, const WfState& W, float alpha, uint32_t i) {
+  WfPath p;
+  wf_load(W, i, p);
+  Hit h;
+  Rec rec;
+  wf_hit_record(S, W, i, p.ray, h, rec);
+  W.full[3 * i] = make_float4(rec.p.x, rec.p.y, rec.p.z, rec.u);
+  W.full[3 * i + 1] = make_float4(rec.n.x, rec.n.y, rec.n.z, rec.v);
+  W.full[3 * i + 2] = make_float4(rec.front ? 1.0f : 0.0f, __uint_as_float(rec.mat), 0.0f, 0.0f);
+  float4 out = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
+  if (!(p.rng.f32() < alpha)) {
+    V gen;
+    if (p.rng.boolean()) {
+      gen = mis_random(S, rec.p, p.rng);
+    } else {
+      const V w = rec.n;
+      const V a = fabsf(w.x) > 0.9f ? unit(mk(0.0f, 1.0f, 0.0f)) : unit(mk(1.0f, 0.0f, 0.0f));
+      const V vv = unit(cross(w, a));
+      const V uu = unit(cross(w, vv));
+      const V c = random_cosine_direction(p.rng);
+      gen = unit(add(add(scl(c.x, uu), scl(c.y, vv)), scl(c.z, w)));
+    }
+    const V nd = unit(gen);
+    out = make_float4(nd.x, nd.y, nd.z, 0.0f);
+  }
+  W.hit[i] = out;
+  W.meta[i].z = p.rng.counter;
+}
+
+__global__ void __launch_bounds__(128) wf_guide_pre(ClvDeviceScene S, WfState W, WfCounters* C, float alpha) {
+  const uint32_t n = C->queue[WF_Q_GUIDE];
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += stride)
+    guide_pre_slot(S, W, alpha, W.queue[(size_t)WF_Q_GUIDE * W.Q + q]);
+}
+
+// post: W.hit = {direction, guide density}.  One-sample MIS over the guide
+// (alpha) and the reference's MixturePDF (1 - alpha): the bounce is weighted
+// by attenuation * scattering_pdf / (alpha q + (1 - alpha) p_mixture).  The
+// first two guided vertices of a path leave a training record.
+__device__ __forceinline__ bool guide_post_slot(const ClvDeviceScene& S, const WfParams& P, const WfState& W,
+                                                WfCounters* C, uint32_t* err, const GuideDev& G, uint32_t i) {
+  WfPath p;
+  wf_load(W, i, p);
+  const float4 f0 = W.full[3 * i], f1 = W.full[3 * i + 1], f2 = W.full[3 * i + 2];
+  Rec rec;
+  rec.t = 0.0f;
+  rec.p = mk(f0.x, f0.y, f0.z);
+  rec.u = f0.w;
+  rec.n = mk(f1.x, f1.y, f1.z);
+  rec.v = f1.w;
+  rec.front = f2.x != 0.0f;
+  rec.mat = __float_as_uint(f2.y);
+  const float4 hv = W.hit[i];
+  const V nd = mk(hv.x, hv.y, hv.z);
+  const float q = G.alpha > 0.0f ? hv.w : 0.0f;
+  const float light_v = mis_pdf(S, rec.p, nd, p.ray.lambda, p.ray.time, err);
+  const float cosine = dot(unit(nd), rec.n);
+  const float bsdf_v = cosine <= 0.0f ? 0.0f : cosine / CLV_PI;
+  const float pdf = G.alpha * q + (1.0f - G.alpha) * (0.5f * light_v + 0.5f * bsdf_v);
+  const float cs = dot(rec.n, unit(nd));
+  // training record of this vertex (warp-aggregated slot reservation)
+  uint4 gs = W.gslot[i];
+  const bool want = gs.y == 0xFFFFFFFFu && !(cs < 0.0f);
+  const unsigned act = __activemask();
+  const unsigned wm = __ballot_sync(act, want);
+  if (wm) {
+    const int lane = threadIdx.x & 31, leader = __ffs(wm) - 1;
+    unsigned base = 0;
+    if (lane == leader) base = atomicAdd(W.grec_count, (unsigned)__popc(wm));
+    base = __shfl_sync(act, base, leader);
+    if (want) {
+      const unsigned r = base + __popc(wm & ((1u << lane) - 1u));
+      if (r < W.grec_cap) {
+        const float4 dl = W.d_lambda[i];
+        float4* out = W.grec + GD_REC_F4 * (size_t)r;
+        out[0] = make_float4(fminf(1.0f, fmaxf(0.0f, (rec.p.x - G.bmin[0]) * G.binv[0])),
+                             fminf(1.0f, fmaxf(0.0f, (rec.p.y - G.bmin[1]) * G.binv[1])),
+                             fminf(1.0f, fmaxf(0.0f, (rec.p.z - G.bmin[2]) * G.binv[2])),
+                             fminf(1.0f, fmaxf(0.0f, 0.5f - 0.5f * dl.x)));
+        out[1] = make_float4(fminf(1.0f, fmaxf(0.0f, 0.5f - 0.5f * dl.y)),
+                             fminf(1.0f, fmaxf(0.0f, 0.5f - 0.5f * dl.z)),
+                             ((float)__float_as_int(dl.w) - 380.0f) * 0.0025f, 0.0f);
+        out[2] = make_float4(nd.x, nd.y, nd.z, 0.0f);
+        if (gs.x == 0xFFFFFFFFu) {
+          gs.x = r;
+          gs.z = __float_as_uint(p.beta[0]);
+        } else {
+          gs.y = r;
+          gs.w = __float_as_uint(p.beta[0]);
+        }
+        W.gslot[i] = gs;
+      }
+    }
+  }
+  if (cs < 0.0f) {  // Lambertian::scattering_pdf is None below the surface
+    wf_enqueue(W, C, WF_Q_FINISH, i);
+    return false;
+  }
+  const float spdf = cs / CLV_PI;
+  const ClvMaterial& m = S.materials[rec.mat];
+  float atten[4];
+  wf_attenuation(S, m, p.ray, rec, atten);
+#pragma unroll
+  for (int j = 0; j < 4; ++j) p.beta[j] = p.beta[j] * (atten[j] * spdf / pdf);
+  return wf_advance(P, W, C, i, p, rec.p, nd);
+}
+
+__global__ void __launch_bounds__(128) wf_guide_post(ClvDeviceScene S, WfParams P, WfState W, WfCounters* C,
+                                                     uint32_t* err, GuideDev G) {
+  const uint32_t n = C->queue[WF_Q_GUIDE];
+  const uint32_t stride = gridDim.x * blockDim.x;
+  const uint32_t first = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t rounds = (n + stride - 1) / stride;
+  for (uint32_t r = 0; r < rounds; ++r) {
+    const uint32_t q = first + r * stride;
+    bool live = false;
+    if (q < n) live = guide_post_slot(S, P, W, C, err, G, W.queue[(size_t)WF_Q_GUIDE * W.Q + q]);
+    wf_count_live(C, live);
+  }
+}
+
 // film rule of draw_cpu.rs:131-142, deposited as f64 sums
 __device__ __forceinline__ void film_deposit(const ClvDeviceScene& S, double* film, uint32_t pixel, int hero,
                                              const float p[4]) {
@@ -471,6 +608,17 @@ __device__ __forceinline__ void finish_slot(const ClvDeviceScene& S, const WfSta
     // paths that ended in the shade kernels (depth limit, no scatter) add nothing here
   }
   film_deposit(S, film, W.meta[i].x, ray.lambda, L);
+  if (W.gslot) {  // training weights: hero power of the path / hero throughput before each recorded vertex
+    const uint4 gs = W.gslot[i];
+    if (gs.x != 0xFFFFFFFFu) {
+      const float b = __uint_as_float(gs.z);
+      reinterpret_cast<float*>(W.grec + GD_REC_F4 * (size_t)gs.x + 2)[3] = b > 0.0f ? L[0] / b : 0.0f;
+    }
+    if (gs.y != 0xFFFFFFFFu) {
+      const float b = __uint_as_float(gs.w);
+      reinterpret_cast<float*>(W.grec + GD_REC_F4 * (size_t)gs.y + 2)[3] = b > 0.0f ? L[0] / b : 0.0f;
+    }
+  }
 }
 
 // Ends paths, then each slot takes the next work item (one atomic per warp).

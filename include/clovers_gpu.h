@@ -128,7 +128,7 @@ int clv_render_batch(clv_device_scene* const* dscenes, const clv_render_opts* op
  * while they render -- a host that pre-reserves device memory for its own
  * pool, or a real-time caller that must not hit out-of-memory mid-frame.  It
  * calls no cudaMalloc/cudaFree: path state, queues and counters live in one
- * static device array of 65536 path slots (about 9.7 MB, reserved on every GPU
+ * static device array of 65536 path slots (about 10 MB, reserved on every GPU
  * that loads the library until the process exits).  opts->path_slots above
  * 65536 is rejected with CLV_E_INVALID; 0 means 65536.  The first call on a
  * device looks up the array's address on that device (cudaGetSymbolAddress),
@@ -162,6 +162,60 @@ int clv_raycast(clv_device_scene* dscene, const float* rays, uint64_t n, uint32_
 /* Device variant, asynchronous on `stream`. */
 int clv_raycast_device(const clv_device_scene* dscene, const float* rays_dev, uint64_t n, uint32_t* prim_id_dev,
                        float* t_dev, uint32_t* node_visits_dev, uint32_t* prim_tests_dev, void* stream);
+
+/* ---- learned path guiding (no counterpart in the reference) -------------
+ *
+ * A small MLP (inputs: position in the scene box, outgoing direction, hero
+ * wavelength; 12-frequency sin/cos encoding; three hidden layers of 64; BF16
+ * weights with FP32 accumulation on the tensor cores) outputs an 8-lobe von
+ * Mises-Fisher mixture over incident directions at Lambertian vertices.  A
+ * guided render draws a share `alpha` of its Lambertian bounces from that
+ * mixture and the rest from the reference's MixturePDF, and weights each
+ * bounce by the blended density, so the image stays an unbiased estimate for
+ * any network.  It also stores training records (inputs, sampled direction,
+ * integrand / density of the hero wavelength) of the first two Lambertian
+ * vertices of each path; clv_guide_train takes Adam steps on them. */
+typedef struct clv_guide clv_guide;
+typedef struct clv_guide_opts {
+  uint32_t record_capacity; /* training records kept per render call, 0 = 2^20 */
+  float learning_rate;      /* Adam step size, 0 = 5e-3 */
+  uint64_t seed;            /* weight initialisation */
+} clv_guide_opts;
+#define CLV_GUIDE_PARAMS 22016  /* fp32 weights: W1 64x176, W2 64x64, W3 64x64, W4 40x64, row-major */
+#define CLV_GUIDE_OUTPUTS 40    /* raw outputs: 8 lobes x (mean direction xyz, log concentration, logit) */
+
+int clv_guide_create(const clv_guide_opts* opts, clv_guide** out);
+void clv_guide_free(clv_guide* guide);
+int clv_guide_get_params(const clv_guide* guide, float* params);
+int clv_guide_set_params(clv_guide* guide, const float* params);
+
+/* Path tracing like clv_render_device, with a share alpha in [0, 1] of the
+ * Lambertian bounces drawn from the guide.  Replaces the guide's training
+ * records with those of this call.  alpha = 0 renders the reference's
+ * estimator (other random streams than clv_render_device) and still records. */
+int clv_render_guided(clv_device_scene* dscene, const clv_render_opts* opts, clv_guide* guide, float alpha,
+                      double* film_dev, void* stream);
+
+/* `steps` Adam steps on consecutive batches of `batch` records (0 = 65536)
+ * of the last guided render; mean_loss (optional) receives the mean of
+ * -f log q over the records used. */
+int clv_guide_train(clv_guide* guide, uint32_t steps, uint32_t batch, double* mean_loss, void* stream);
+int clv_guide_record_count(const clv_guide* guide, uint64_t* n);
+/* records: n x 12 floats {u0..u6, 0, w.x, w.y, w.z, f} (u: normalised inputs) */
+int clv_guide_get_records(const clv_guide* guide, float* records, uint64_t n);
+
+/* Network on host arrays (tests, diagnostics).  queries: n x 8 floats {u0..u6,
+ * 0}, inputs already normalised to [0, 1]; out: n x 40 raw outputs. */
+int clv_guide_forward(clv_guide* guide, const float* queries, uint64_t n, float* out);
+/* Sum over the records (n x 12 floats as above) of the gradient of -f log q(w)
+ * with respect to the fp32 weights (CLV_GUIDE_PARAMS floats); loss = the sum
+ * of -f log q.  No weight update. */
+int clv_guide_gradient(clv_guide* guide, const float* records, uint64_t n, float* grads, double* loss);
+/* Error bits of the guide kernels since the last call (clears them). */
+int clv_guide_status(clv_guide* guide, uint32_t* flags);
+/* One 128 x n x k BF16 tensor-core product through the guide's operand
+ * layouts, against a CUDA-core sum of the same products: max |difference|. */
+int clv_guide_selftest_mma(uint32_t n, uint32_t k, uint64_t seed, float* d_out, float* max_abs_err);
 
 /* ---- status ------------------------------------------------------------ */
 

@@ -15,7 +15,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "liboracle.so")
-_SRC = [os.path.join(HERE, "oracle.cpp"), os.path.join(HERE, "..", "clovers_gb300", "csrc", "json.hpp"),
+_SRC = [os.path.join(HERE, "oracle.cpp"), os.path.join(HERE, "guide.cpp"), os.path.join(HERE, "..", "clovers_gb300", "csrc", "json.hpp"),
         os.path.join(HERE, "..", "clovers_gb300", "csrc", "spectral_tables.h")]
 _L = None
 _LOCK = threading.Lock()
@@ -61,6 +61,10 @@ def lib():
                 "orc_raycast": (i32, [vp, vp, u64, vp, vp, vp, vp, i32]),
                 "orc_render": (i32, [vp, u32, u32, u32, u32, u64, u32, u32, u32, u32, u32, vp, i32]),
                 "orc_trace_sample": (i32, [vp, u32, u32, u32, u32, u32, u32, u64, vp, vp, vp]),
+                "orc_guide_forward": (None, [vp, vp, u64, i32, vp]),
+                "orc_guide_gradient": (ctypes.c_double, [vp, vp, u64, i32, vp]),
+                "orc_guide_pdf": (ctypes.c_double, [vp, vp]),
+                "orc_guide_sample": (None, [vp, f32, f32, f32, vp]),
             }
             for name, (res, args) in sig.items():
                 fn = getattr(L, name)
@@ -221,3 +225,39 @@ class Scene:
                                   _buf(ray)) != 0:
             raise RuntimeError(_err())
         return p, w, ray
+
+
+# ---- path guide (specification restated in oracle/guide.cpp) ----------------
+GUIDE_PARAMS = 22016
+GUIDE_OUTPUTS = 40
+
+
+def guide_forward(params, queries, bf16=True):
+    """Raw network outputs (n, 40) for queries (n, 8) = normalised inputs u0..u6, 0."""
+    p = np.ascontiguousarray(params, np.float32).reshape(GUIDE_PARAMS)
+    q = np.ascontiguousarray(queries, np.float32).reshape(-1, 8)
+    out = np.empty((q.shape[0], GUIDE_OUTPUTS), np.float32)
+    lib().orc_guide_forward(p.ctypes.data, q.ctypes.data, q.shape[0], 1 if bf16 else 0, out.ctypes.data)
+    return out
+
+
+def guide_gradient(params, records, bf16=True):
+    """(gradient sums (22016,) float64, loss sum) of -f log q(w) over records (n, 12)."""
+    p = np.ascontiguousarray(params, np.float32).reshape(GUIDE_PARAMS)
+    r = np.ascontiguousarray(records, np.float32).reshape(-1, 12)
+    g = np.empty(GUIDE_PARAMS, np.float64)
+    loss = lib().orc_guide_gradient(p.ctypes.data, r.ctypes.data, r.shape[0], 1 if bf16 else 0, g.ctypes.data)
+    return g, loss
+
+
+def guide_pdf(out40, w):
+    o = np.ascontiguousarray(out40, np.float32).reshape(GUIDE_OUTPUTS)
+    d = np.ascontiguousarray(w, np.float32).reshape(3)
+    return lib().orc_guide_pdf(o.ctypes.data, d.ctypes.data)
+
+
+def guide_sample(out40, u0, u1, u2):
+    o = np.ascontiguousarray(out40, np.float32).reshape(GUIDE_OUTPUTS)
+    w = np.empty(3, np.float32)
+    lib().orc_guide_sample(o.ctypes.data, u0, u1, u2, w.ctypes.data)
+    return w
