@@ -433,7 +433,9 @@ __global__ void __launch_bounds__(128) wf_shade_diffuse(ClvDeviceScene S, WfPara
 // pre: the hit record goes to the slot's record area (W.full) and a coin picks
 // the strategy; bounces that use the reference's MixturePDF (probability
 // 1 - alpha) draw their direction here, exactly as diffuse_slot does.
-// W.hit then holds {direction, 0} or {-, 1} (guide to sample).
+// W.hit then holds {direction, 0} or {-, 1} (guide to sample); the hit's t and
+// reference move to W.full[3i+2].zw so a path that ends in guide_post can hand
+// wf_finish its hit again.
 __device__ __forceinline__ void guide_pre_slot(const ClvDeviceScene& S, const WfState& W, float alpha, uint32_t i) {
   WfPath p;
   wf_load(W, i, p);
@@ -442,7 +444,7 @@ __device__ __forceinline__ void guide_pre_slot(const ClvDeviceScene& S, const Wf
   wf_hit_record(S, W, i, p.ray, h, rec);
   W.full[3 * i] = make_float4(rec.p.x, rec.p.y, rec.p.z, rec.u);
   W.full[3 * i + 1] = make_float4(rec.n.x, rec.n.y, rec.n.z, rec.v);
-  W.full[3 * i + 2] = make_float4(rec.front ? 1.0f : 0.0f, __uint_as_float(rec.mat), 0.0f, 0.0f);
+  W.full[3 * i + 2] = make_float4(rec.front ? 1.0f : 0.0f, __uint_as_float(rec.mat), h.t, __uint_as_float(h.ref));
   float4 out = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
   if (!(p.rng.f32() < alpha)) {
     V gen;
@@ -495,6 +497,9 @@ __device__ __forceinline__ bool guide_post_slot(const ClvDeviceScene& S, const W
   const float bsdf_v = cosine <= 0.0f ? 0.0f : cosine / CLV_PI;
   const float pdf = G.alpha * q + (1.0f - G.alpha) * (0.5f * light_v + 0.5f * bsdf_v);
   const float cs = dot(rec.n, unit(nd));
+  // a path ending here goes to wf_finish, which reads its hit (a Lambertian
+  // surface: no emission) from W.hit
+  if (cs < 0.0f || p.meta.y + 1 > P.max_depth) W.hit[i] = make_float4(f2.z, f2.w, 0.0f, 0.0f);
   // training record of this vertex (warp-aggregated slot reservation)
   uint4 gs = W.gslot[i];
   const bool want = gs.y == 0xFFFFFFFFu && !(cs < 0.0f);
