@@ -334,22 +334,76 @@ def run_config(args):
         g = np.load(gpath)
         x0, r0, x1, r1 = [int(v) for v in g["window"]]
         ref = g["mean"]
+        where = "oracle, 65536 spp, crop %s of %dx%d (tests/golden/%s_ref.npz)" % ([x0, r0, x1, r1], w, h, gold)
+
+        def crop_relmse(total_spp):
+            img = (film.view(h, w, 3)[r0:r1, x0:x1].reshape(-1, 3) / total_spp).cpu().numpy()
+            return float(np.mean((img - ref) ** 2 / (ref ** 2 + 1e-2)))
+
         film.zero_()
         total_ms, total_spp, chunk = 0.0, 0, args.chunk_spp
         relmse = None
         while total_spp < args.max_spp:
             total_ms += render(chunk, total_spp, seed=SEED + 1000)
             total_spp += chunk
-            img = (film.view(h, w, 3)[r0:r1, x0:x1].reshape(-1, 3) / total_spp).cpu().numpy()
-            relmse = float(np.mean((img - ref) ** 2 / (ref ** 2 + 1e-2)))
+            relmse = crop_relmse(total_spp)
             if relmse <= 1e-3:
                 break
         line["time_to_relmse"] = {"target": 1e-3, "reached": bool(relmse is not None and relmse <= 1e-3),
                                   "gpu_ms": round(total_ms, 2), "spp": total_spp, "relmse": relmse,
-                                  "reference": "oracle, 65536 spp, crop %s of %dx%d (tests/golden/%s_ref.npz)" % (
-                                      [x0, r0, x1, r1], w, h, gold),
-                                  "epsilon": 1e-2, "estimator": "plain (BSDF + light mixture MIS)"}
+                                  "reference": where, "epsilon": 1e-2,
+                                  "estimator": "plain (BSDF + light mixture MIS)"}
+        if args.guided:
+            line["time_to_relmse_guided"] = run_guided(args, d, w, h, depth, film, stream, crop_relmse, where)
+            line["time_to_relmse_guided"]["vs_plain_time"] = round(
+                line["time_to_relmse_guided"]["gpu_ms"] / max(total_ms, 1e-9), 4)
     print(json.dumps(line), flush=True)
+
+
+def run_guided(args, d, w, h, depth, film, stream, crop_relmse, where):
+    """Progressive guided render until the crop's relMSE reaches 1e-3: training
+    passes of --guide-pass-spp samples per pixel (the first with alpha 0), each
+    followed by --guide-steps Adam steps on its records, then passes of
+    --chunk-spp with the trained guide.  Every pass adds to the film (all are
+    unbiased); the GPU time includes rendering and training."""
+    import torch
+    import clovers_gb300 as cg
+    from clovers_gb300 import _lib
+    L = _lib.lib()
+    sp = stream.cuda_stream
+    guide = cg.Guide(seed=args.guide_seed, learning_rate=args.guide_lr)
+    film.zero_()
+    total_ms, total_spp, train_ms, k = 0.0, 0, 0.0, 0
+    relmse = None
+    while total_spp < args.max_spp:
+        training = k < args.guide_passes
+        n = args.guide_pass_spp if training else args.chunk_spp
+        alpha = 0.0 if k == 0 else args.guide_alpha
+        o = cg.render_opts(cg.RenderOptions(width=w, height=h, samples=n, max_depth=depth, seed=SEED + 2000))
+        o.sample_offset = total_spp
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0.record(stream)
+        _lib.check(L.clv_render_guided(d.handle, ctypes.byref(o), guide.handle, alpha, film.data_ptr(), sp))
+        e1.record(stream)
+        if training:
+            _lib.check(L.clv_guide_train(guide.handle, args.guide_steps, args.guide_batch, None, sp))
+        e2.record(stream)
+        e2.synchronize()
+        total_ms += e0.elapsed_time(e2)
+        train_ms += e1.elapsed_time(e2)
+        total_spp += n
+        k += 1
+        relmse = crop_relmse(total_spp)
+        if relmse <= 1e-3:
+            break
+    if guide.status():
+        raise RuntimeError("guide kernels reported an error")
+    return {"target": 1e-3, "reached": bool(relmse is not None and relmse <= 1e-3), "gpu_ms": round(total_ms, 2),
+            "train_ms": round(train_ms, 2), "spp": total_spp, "relmse": relmse, "reference": where,
+            "estimator": "guided: alpha %.2f of Lambertian bounces from the vMF-mixture MLP (one-sample MIS with "
+                         "the plain mixture); %d training passes of %d spp, %d Adam steps of %d records each" % (
+                             args.guide_alpha, args.guide_passes, args.guide_pass_spp, args.guide_steps,
+                             args.guide_batch)}
 
 
 def main():
@@ -373,6 +427,14 @@ def main():
     ap.add_argument("--batch", action="store_true", help="measure the batched multi-scene workload")
     ap.add_argument("--batch-scenes", type=int, default=64)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline legs")
+    ap.add_argument("--guided", action="store_true", help="with --config: also the guided time to relMSE 1e-3")
+    ap.add_argument("--guide-alpha", type=float, default=0.5)
+    ap.add_argument("--guide-passes", type=int, default=32)
+    ap.add_argument("--guide-pass-spp", type=int, default=4)
+    ap.add_argument("--guide-steps", type=int, default=64)
+    ap.add_argument("--guide-batch", type=int, default=32768)
+    ap.add_argument("--guide-lr", type=float, default=5e-3)
+    ap.add_argument("--guide-seed", type=int, default=7)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     W_IMG = H_IMG = args.size

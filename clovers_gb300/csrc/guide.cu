@@ -680,6 +680,31 @@ __global__ void __launch_bounds__(128, 1) guide_train_kernel(const unsigned char
   }
 }
 
+// Gathers the records that carry light (f > 0); the others add nothing to the
+// gradient.  Warp-aggregated append, order not preserved.
+__global__ void guide_compact_kernel(const float4* __restrict__ rec, uint32_t n, float4* __restrict__ out,
+                                     unsigned int* __restrict__ count) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  bool keep = false;
+  float4 c = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  if (i < n) {
+    c = rec[GD_REC_F4 * (size_t)i + 2];
+    keep = c.w > 0.0f && c.w < 3.0e38f;
+  }
+  const unsigned m = __ballot_sync(0xFFFFFFFFu, keep);
+  if (!m) return;
+  const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+  unsigned base = 0;
+  if (lane == leader) base = atomicAdd(count, (unsigned)__popc(m));
+  base = __shfl_sync(0xFFFFFFFFu, base, leader);
+  if (keep) {
+    float4* o = out + GD_REC_F4 * (size_t)(base + __popc(m & ((1u << lane) - 1u)));
+    o[0] = rec[GD_REC_F4 * (size_t)i];
+    o[1] = rec[GD_REC_F4 * (size_t)i + 1];
+    o[2] = c;
+  }
+}
+
 // bf16 copies of parameter i in the operand blob (forward and transposed)
 __device__ __forceinline__ void blob_store(unsigned char* blob, uint32_t i, float w) {
   const __nv_bfloat16 b = __float2bfloat16_rn(w);
@@ -851,7 +876,7 @@ void launch_train(clv_guide* g, const float4* rec, uint32_t n, cudaStream_t st) 
 
 clv_guide::~clv_guide() {
   for (void* p : {(void*)params, (void*)adam_m, (void*)adam_v, (void*)grad, (void*)wblob, (void*)rec,
-                  (void*)rec_count, (void*)slot, (void*)err, (void*)loss})
+                  (void*)rec_count, (void*)rec_keep, (void*)keep_count, (void*)slot, (void*)err, (void*)loss})
     if (p) cudaFree(p);
 }
 
@@ -902,7 +927,7 @@ int clv_guide_create(const clv_guide_opts* o, clv_guide** out) {
   *out = nullptr;
   clv_guide_opts d{};
   if (o) d = *o;
-  if (d.record_capacity == 0) d.record_capacity = 1u << 20;
+  if (d.record_capacity == 0) d.record_capacity = 1u << 21;
   if (d.record_capacity > (1u << 26)) return clv_internal_fail(CLV_E_INVALID, "record capacity above 2^26");
   clv_guide* g = new clv_guide();
   try {
@@ -916,6 +941,8 @@ int clv_guide_create(const clv_guide_opts* o, clv_guide** out) {
     ckg(cudaMalloc(&g->wblob, GD_B_ALL), "cudaMalloc");
     ckg(cudaMalloc(&g->rec, (size_t)g->rec_cap * GD_REC_F4 * sizeof(float4)), "cudaMalloc guide records");
     ckg(cudaMalloc(&g->rec_count, sizeof(unsigned int)), "cudaMalloc");
+    ckg(cudaMalloc(&g->rec_keep, (size_t)g->rec_cap * GD_REC_F4 * sizeof(float4)), "cudaMalloc guide records");
+    ckg(cudaMalloc(&g->keep_count, sizeof(unsigned int)), "cudaMalloc");
     ckg(cudaMalloc(&g->err, sizeof(uint32_t)), "cudaMalloc");
     ckg(cudaMalloc(&g->loss, sizeof(double)), "cudaMalloc");
     const std::vector<float> p = init_params(d.seed);
@@ -1050,7 +1077,17 @@ int clv_guide_train(clv_guide* g, uint32_t steps, uint32_t batch, double* mean_l
     unsigned int c = 0;
     ckg(cudaMemcpyAsync(&c, g->rec_count, sizeof c, cudaMemcpyDeviceToHost, st), "cudaMemcpyAsync");
     ckg(cudaStreamSynchronize(st), "cudaStreamSynchronize");
-    const uint32_t n = std::min<uint32_t>(c, g->rec_cap);
+    const uint32_t nrec = std::min<uint32_t>(c, g->rec_cap);
+    if (nrec == 0 || steps == 0) {
+      if (mean_loss) *mean_loss = 0.0;
+      return CLV_OK;
+    }
+    ckg(cudaMemsetAsync(g->keep_count, 0, sizeof(unsigned int), st), "cudaMemsetAsync");
+    guide_compact_kernel<<<(nrec + 255) / 256, 256, 0, st>>>(g->rec, nrec, g->rec_keep, g->keep_count);
+    clv_internal_count_launches(1);
+    ckg(cudaMemcpyAsync(&c, g->keep_count, sizeof c, cudaMemcpyDeviceToHost, st), "cudaMemcpyAsync");
+    ckg(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+    const uint32_t n = std::min<uint32_t>(c, nrec);
     if (batch == 0) batch = 1u << 16;
     if (n == 0 || steps == 0) {
       if (mean_loss) *mean_loss = 0.0;
@@ -1062,7 +1099,7 @@ int clv_guide_train(clv_guide* g, uint32_t steps, uint32_t batch, double* mean_l
     uint32_t off = 0;
     for (uint32_t s = 0; s < steps; ++s) {
       if (off + batch > n) off = 0;
-      launch_train(g, g->rec + (size_t)off * GD_REC_F4, batch, st);
+      launch_train(g, g->rec_keep + (size_t)off * GD_REC_F4, batch, st);
       off += batch;
       ++g->step;
       const float bc1 = 1.0f - std::pow(b1, (float)g->step), bc2 = 1.0f - std::pow(b2, (float)g->step);

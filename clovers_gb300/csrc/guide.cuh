@@ -107,6 +107,8 @@ struct clv_guide {
   float4* rec = nullptr;
   unsigned int* rec_count = nullptr;
   uint32_t rec_cap = 0;
+  float4* rec_keep = nullptr;          // records with f > 0, gathered before training
+  unsigned int* keep_count = nullptr;
   uint4* slot = nullptr;
   uint32_t slots = 0;
   uint32_t* err = nullptr;

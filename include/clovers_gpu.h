@@ -177,7 +177,7 @@ int clv_raycast_device(const clv_device_scene* dscene, const float* rays_dev, ui
  * vertices of each path; clv_guide_train takes Adam steps on them. */
 typedef struct clv_guide clv_guide;
 typedef struct clv_guide_opts {
-  uint32_t record_capacity; /* training records kept per render call, 0 = 2^20 */
+  uint32_t record_capacity; /* training records kept per render call, 0 = 2^21 */
   float learning_rate;      /* Adam step size, 0 = 5e-3 */
   uint64_t seed;            /* weight initialisation */
 } clv_guide_opts;
@@ -197,8 +197,9 @@ int clv_render_guided(clv_device_scene* dscene, const clv_render_opts* opts, clv
                       double* film_dev, void* stream);
 
 /* `steps` Adam steps on consecutive batches of `batch` records (0 = 65536)
- * of the last guided render; mean_loss (optional) receives the mean of
- * -f log q over the records used. */
+ * of the last guided render, taken from the records that carry light (f > 0;
+ * the others add nothing to the gradient); mean_loss (optional) receives the
+ * mean of -f log q over the records used. */
 int clv_guide_train(clv_guide* guide, uint32_t steps, uint32_t batch, double* mean_loss, void* stream);
 int clv_guide_record_count(const clv_guide* guide, uint64_t* n);
 /* records: n x 12 floats {u0..u6, 0, w.x, w.y, w.z, f} (u: normalised inputs) */

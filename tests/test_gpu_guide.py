@@ -160,11 +160,11 @@ def test_trained_guide_lowers_caustic_error():
                     cg.RenderOptions(width=w, height=h, samples=spp, max_depth=depth, seed=99), d)
     e_plain = relmse(_crop(plain.astype(np.float64), w, h, win), ref)
     guide = cg.Guide(seed=7)
-    for k in range(8):  # training passes, not part of the measured image
+    for k in range(32):  # training passes, not part of the measured image
         _render(d, w, h, 4, depth, 1000 + k, guide, 0.0 if k == 0 else 0.5)
-        guide.train(32, 32768)
+        guide.train(64, 32768)
     img = _render(d, w, h, spp, depth, 99, guide, 0.5) / spp
     e_guided = relmse(_crop(img, w, h, win), ref)
     print("prism crop at %d spp: plain relMSE %.4g, guided %.4g" % (spp, e_plain, e_guided))
-    assert e_guided < e_plain
+    assert e_guided < 0.8 * e_plain
     assert guide.status() == 0
