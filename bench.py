@@ -320,44 +320,87 @@ def run_config(args):
         film.zero_()
         render(max(1, spp // 16), 10**7 + k * spp)
     ms = []
-    for k in range(args.steps):
+    for k in range(0 if args.guided_only else args.steps):
         film.zero_()
         ms.append(render(spp, k * spp))
-    ms_step = sum(ms) / len(ms)
-    line = {"metric": "Msamples/s", "value": round(w * h * spp / (ms_step / 1e3) / 1e6, 3), "unit": "Msamples/s",
-            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3),
+    ms_step = sum(ms) / len(ms) if ms else float("nan")
+    line = {"metric": "Msamples/s", "value": round(w * h * spp / (ms_step / 1e3) / 1e6, 3) if ms else None,
+            "unit": "Msamples/s",
+            "n_gpus": 1, "steps": len(ms), "warmup": args.warmup, "ms_per_step": round(ms_step, 3) if ms else None,
             "higher_is_better": True, "dtype": "f32", "data": "synthetic (seeded generator, reference scene format)",
             "config": {"workload": desc, "scene_load_and_bvh_s": round(build_s, 3), "objects": host.info()["objects"]}}
     gold = GOLDEN.get(args.config)
-    gpath = os.path.join(ROOT, "tests", "golden", "%s_ref.npz" % gold) if gold else None
-    if gpath and os.path.exists(gpath):
-        g = np.load(gpath)
-        x0, r0, x1, r1 = [int(v) for v in g["window"]]
-        ref = g["mean"]
-        where = "oracle, 65536 spp, crop %s of %dx%d (tests/golden/%s_ref.npz)" % ([x0, r0, x1, r1], w, h, gold)
-
-        def crop_relmse(total_spp):
-            img = (film.view(h, w, 3)[r0:r1, x0:x1].reshape(-1, 3) / total_spp).cpu().numpy()
-            return float(np.mean((img - ref) ** 2 / (ref ** 2 + 1e-2)))
-
-        film.zero_()
-        total_ms, total_spp, chunk = 0.0, 0, args.chunk_spp
-        relmse = None
-        while total_spp < args.max_spp:
-            total_ms += render(chunk, total_spp, seed=SEED + 1000)
-            total_spp += chunk
-            relmse = crop_relmse(total_spp)
-            if relmse <= 1e-3:
-                break
-        line["time_to_relmse"] = {"target": 1e-3, "reached": bool(relmse is not None and relmse <= 1e-3),
-                                  "gpu_ms": round(total_ms, 2), "spp": total_spp, "relmse": relmse,
-                                  "reference": where, "epsilon": 1e-2,
-                                  "estimator": "plain (BSDF + light mixture MIS)"}
-        if args.guided:
-            line["time_to_relmse_guided"] = run_guided(args, d, w, h, depth, film, stream, crop_relmse, where)
-            line["time_to_relmse_guided"]["vs_plain_time"] = round(
-                line["time_to_relmse_guided"]["gpu_ms"] / max(total_ms, 1e-9), 4)
+    if gold:
+        plain, guided = time_to_relmse(args, gold, d, w, h, depth, film, stream, render, args.guided)
+        if plain:
+            line["time_to_relmse"] = plain
+        if guided:
+            line["time_to_relmse_guided"] = guided
     print(json.dumps(line), flush=True)
+
+
+def time_to_relmse(args, gold, d, w, h, depth, film, stream, render, guided):
+    """GPU time until the relMSE of the golden crop (tests/golden/<gold>_ref.npz,
+    the oracle at 65,536 spp) reaches 1e-3: progressive passes of --chunk-spp
+    with the plain estimator, and (guided) with the online-trained guide."""
+    gpath = os.path.join(ROOT, "tests", "golden", "%s_ref.npz" % gold)
+    if not os.path.exists(gpath):
+        return None, None
+    g = np.load(gpath)
+    x0, r0, x1, r1 = [int(v) for v in g["window"]]
+    ref = g["mean"]
+    where = "oracle, 65536 spp, crop %s of %dx%d (tests/golden/%s_ref.npz)" % ([x0, r0, x1, r1], w, h, gold)
+
+    def crop_relmse(total_spp):
+        img = (film.view(h, w, 3)[r0:r1, x0:x1].reshape(-1, 3) / total_spp).cpu().numpy()
+        return float(np.mean((img - ref) ** 2 / (ref ** 2 + 1e-2)))
+
+    film.zero_()
+    total_ms, total_spp, chunk = 0.0, 0, args.chunk_spp
+    relmse = None
+    while total_spp < (0 if getattr(args, "guided_only", False) else args.max_spp):
+        total_ms += render(chunk, total_spp, seed=SEED + 1000)
+        total_spp += chunk
+        relmse = crop_relmse(total_spp)
+        if relmse <= 1e-3:
+            break
+    plain = {"target": 1e-3, "reached": bool(relmse is not None and relmse <= 1e-3), "gpu_ms": round(total_ms, 2),
+             "spp": total_spp, "relmse": relmse, "reference": where, "epsilon": 1e-2,
+             "estimator": "plain (BSDF + light mixture MIS)"}
+    gres = None
+    if guided:
+        gres = run_guided(args, d, w, h, depth, film, stream, crop_relmse, where)
+        gres["vs_plain_time"] = round(gres["gpu_ms"] / total_ms, 4) if total_ms > 0 else None
+    return plain, gres
+
+
+def guided_vs_plain(args):
+    """The dispersive-caustic workload (prism + sphere, 1024x1024, depth 16):
+    GPU time to relMSE 1e-3 of the golden crop, plain and guided."""
+    import torch
+    import clovers_gb300 as cg
+    from clovers_gb300 import _lib
+    builder, w, h, _, depth, desc = CONFIGS["c4"]
+    L = _lib.lib()
+    stream = torch.cuda.current_stream()
+    tmp = tempfile.mkdtemp()
+    d = cg.Scene.from_json(config_scene_file(builder, tmp), w, h).upload()
+    film = torch.zeros(w * h * 3, dtype=torch.float64, device="cuda")
+
+    def render(n_spp, offset, seed=SEED):
+        o = cg.render_opts(cg.RenderOptions(width=w, height=h, samples=n_spp, max_depth=depth, seed=seed))
+        o.sample_offset = offset
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        _lib.check(L.clv_render_device(d.handle, ctypes.byref(o), film.data_ptr(), stream.cuda_stream))
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1)
+
+    render(16, 10**7)  # warm-up
+    plain, guided = time_to_relmse(args, "prism", d, w, h, depth, film, stream, render, True)
+    return {"workload": "dispersive prism + glass sphere, 1024x1024, depth 16 (C4)", "plain": plain,
+            "guided": guided, "guided_vs_plain_time": guided["vs_plain_time"] if guided else None}
 
 
 def run_guided(args, d, w, h, depth, film, stream, crop_relmse, where):
@@ -428,6 +471,9 @@ def main():
     ap.add_argument("--batch-scenes", type=int, default=64)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline legs")
     ap.add_argument("--guided", action="store_true", help="with --config: also the guided time to relMSE 1e-3")
+    ap.add_argument("--no-guided", action="store_true", help="skip the guided-vs-plain section of the default run")
+    ap.add_argument("--guided-only", action="store_true",
+                    help="with --config --guided: only the guided passes (short case for profiling)")
     ap.add_argument("--guide-alpha", type=float, default=0.5)
     ap.add_argument("--guide-passes", type=int, default=32)
     ap.add_argument("--guide-pass-spp", type=int, default=4)
@@ -629,6 +675,8 @@ def main():
         if args.no_render:
             line.update(value=trav["value"], ms_per_step=trav["ms_per_step"])
 
+    if rank == 0 and world == 1 and not args.no_guided and not args.no_render:
+        line["time_to_relmse"] = guided_vs_plain(args)
     if rank == 0 and world == 1 and not args.no_cpu and not args.no_render:
         line["cpu_baseline"] = cpu_baseline_render(path, args.cpu_baseline_spp)
     if rank == 0:
