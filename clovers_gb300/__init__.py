@@ -27,7 +27,7 @@ from . import _lib
 from ._lib import ClvError, check, lib
 
 __all__ = ["GlobalOptions", "RenderOptions", "Scene", "DeviceScene", "initialize", "draw", "draw_batch", "render",
-           "raycast", "resolve_srgb", "ClvError", "DeviceBuffer", "Guide", "draw_guided"]
+           "raycast", "resolve_srgb", "ClvError", "DeviceBuffer", "Guide", "draw_guided", "render_guided"]
 
 
 @dataclasses.dataclass
@@ -290,21 +290,23 @@ def render_guided(scene: DeviceScene, render_options: RenderOptions, guide: Guid
 
 
 def draw_guided(global_options: GlobalOptions, render_options: RenderOptions, scene: DeviceScene, guide=None,
-                pass_spp=16, alpha=0.5, train_steps=8, train_batch=0, warmup_passes=1):
-    """draw() with online path guiding: passes of `pass_spp` samples per pixel,
-    the first `warmup_passes` with alpha 0 (the reference's estimator), each
-    followed by `train_steps` Adam steps on the pass's records.  Returns the
-    (height*width, 3) float32 XYZ(E) means, like draw()."""
+                alpha=0.5, train_passes=32, pass_spp=4, train_steps=64, train_batch=32768, chunk_spp=32):
+    """draw() with online path guiding: `train_passes` passes of `pass_spp`
+    samples per pixel (the first with alpha 0, the reference's estimator), each
+    followed by `train_steps` Adam steps on its records, then passes of
+    `chunk_spp` with the trained guide.  Every pass adds to the image (all are
+    unbiased).  Returns the (height*width, 3) float32 XYZ(E) means, like draw()."""
     del global_options
     guide = guide or Guide()
     w, h, spp = render_options.width, render_options.height, render_options.samples
     film = DeviceBuffer(w * h * 3 * 8).zero()
     done, k = 0, 0
     while done < spp:
-        n = min(pass_spp, spp - done)
+        training = k < train_passes
+        n = min(pass_spp if training else chunk_spp, spp - done)
         opts = dataclasses.replace(render_options, samples=n)
-        render_guided(scene, opts, guide, 0.0 if k < warmup_passes else alpha, film, sample_offset=done)
-        if train_steps:
+        render_guided(scene, opts, guide, 0.0 if k == 0 else alpha, film, sample_offset=done)
+        if training and train_steps:
             guide.train(train_steps, train_batch)
         done += n
         k += 1
