@@ -465,7 +465,16 @@ struct clv_device_scene {
   uint32_t wf_slots = 0;
   WfCounters* wf_counters = nullptr;
   unsigned int* wf_live_host = nullptr;  // pinned
+  cudaStream_t cap_stream = nullptr;     // private stream for graph capture
+  cudaStream_t capture_stream() {
+    if (!cap_stream && cudaStreamCreateWithFlags(&cap_stream, cudaStreamNonBlocking) != cudaSuccess) {
+      cudaGetLastError();
+      cap_stream = nullptr;
+    }
+    return cap_stream;
+  }
   ~clv_device_scene() {
+    if (cap_stream) cudaStreamDestroy(cap_stream);
     for (void* p : owned) cudaFree(p);
     if (err) cudaFree(err);
     if (scratch) cudaFree(scratch);
@@ -513,6 +522,50 @@ struct clv_device_scene {
     return scratch;
   }
 };
+
+// An instantiated CUDA graph, destroyed with its owner.
+struct GraphExec {
+  cudaGraphExec_t exec = nullptr;
+  GraphExec() = default;
+  GraphExec(const GraphExec&) = delete;
+  GraphExec(GraphExec&& o) noexcept : exec(o.exec) { o.exec = nullptr; }
+  GraphExec& operator=(GraphExec&& o) noexcept {
+    std::swap(exec, o.exec);
+    return *this;
+  }
+  ~GraphExec() {
+    if (exec) cudaGraphExecDestroy(exec);
+  }
+};
+
+// Captures what `enqueue` launches on the scene's private capture stream into
+// an executable graph.  Returns an empty one if capture is not possible (the
+// caller then launches directly).
+template <class F>
+static GraphExec capture_graph(clv_device_scene* d, F enqueue) {
+  GraphExec g;
+  cudaStream_t cs = d->capture_stream();
+  if (!cs) return g;
+  if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    cudaGetLastError();
+    return g;
+  }
+  enqueue(cs);
+  cudaGraph_t graph = nullptr;
+  if (cudaStreamEndCapture(cs, &graph) != cudaSuccess || !graph) {
+    cudaGetLastError();
+    return g;
+  }
+  cudaGraphExec_t ex = nullptr;
+  const cudaError_t e = cudaGraphInstantiate(&ex, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return g;
+  }
+  g.exec = ex;
+  return g;
+}
 
 static uint32_t launch_grid(uint64_t work, int block) {
   const uint64_t want = (work + block - 1) / block;
@@ -866,32 +919,45 @@ static int render_wavefront(clv_device_scene* d, const clv_render_opts* o, doubl
       cudaEventElapsedTime(&ms, evs[4 * batch], evs[4 * batch + 1]);
       prof->ms_init = ms;
     }
-    for (uint64_t it = 0;; it += batch) {
-      for (int k = 0; k < batch; ++k) {
-        cudaMemsetAsync(&d->wf_counters->live, 0, 5 * sizeof(unsigned int), st);  // live + 4 queue lengths
-        if (prof) cudaEventRecord(evs[4 * k], st);
-        switch (level * 2 + (prof ? 1 : 0)) {
-          case 0: wf_intersect<0, false, false><<<grid, block, 0, st>>>(d->view, W, C, d->err, nullptr, WfBatch{}); break;
-          case 1: wf_intersect<0, true, false><<<grid, block, 0, st>>>(d->view, W, C, d->err, dcnt, WfBatch{}); break;
-          case 2: wf_intersect<1, false, false><<<grid, block, 0, st>>>(d->view, W, C, d->err, nullptr, WfBatch{}); break;
-          case 3: wf_intersect<1, true, false><<<grid, block, 0, st>>>(d->view, W, C, d->err, dcnt, WfBatch{}); break;
-          case 4: wf_intersect<2, false, false><<<grid, block, 0, st>>>(d->view, W, C, d->err, nullptr, WfBatch{}); break;
-          default: wf_intersect<2, true, false><<<grid, block, 0, st>>>(d->view, W, C, d->err, dcnt, WfBatch{}); break;
-        }
-        if (prof) cudaEventRecord(evs[4 * k + 1], st);
-        if (prof) cudaEventRecord(evs[4 * k + 2], st);
-        wf_shade_specular<false><<<qgrid, block, 0, st>>>(d->view, P, W, C, d->err, WfBatch{});
-        wf_shade_diffuse<false><<<qgrid, block, 0, st>>>(d->view, P, W, C, d->err, WfBatch{});
-        if (guide) {
-          wf_guide_pre<<<qgrid, block, 0, st>>>(d->view, W, C, alpha);
-          if (alpha > 0.0f) gd_launch_queue(G, GQ, (uint32_t)q, st);
-          wf_guide_post<<<qgrid, block, 0, st>>>(d->view, P, W, C, d->err, G);
-          g_launches += 2;
-        }
-        wf_finish<false><<<qgrid, block, 0, st>>>(d->view, P, W, C, film, WfBatch{});
-        if (prof) cudaEventRecord(evs[4 * k + 3], st);
+    // one bounce: counters, closest hits, the shading passes, path ends
+    auto bounce = [&](cudaStream_t s, int k) {
+      cudaMemsetAsync(&d->wf_counters->live, 0, 5 * sizeof(unsigned int), s);  // live + 4 queue lengths
+      if (prof) cudaEventRecord(evs[4 * k], s);
+      switch (level * 2 + (prof ? 1 : 0)) {
+        case 0: wf_intersect<0, false, false><<<grid, block, 0, s>>>(d->view, W, C, d->err, nullptr, WfBatch{}); break;
+        case 1: wf_intersect<0, true, false><<<grid, block, 0, s>>>(d->view, W, C, d->err, dcnt, WfBatch{}); break;
+        case 2: wf_intersect<1, false, false><<<grid, block, 0, s>>>(d->view, W, C, d->err, nullptr, WfBatch{}); break;
+        case 3: wf_intersect<1, true, false><<<grid, block, 0, s>>>(d->view, W, C, d->err, dcnt, WfBatch{}); break;
+        case 4: wf_intersect<2, false, false><<<grid, block, 0, s>>>(d->view, W, C, d->err, nullptr, WfBatch{}); break;
+        default: wf_intersect<2, true, false><<<grid, block, 0, s>>>(d->view, W, C, d->err, dcnt, WfBatch{}); break;
       }
-      g_launches += 4 * batch;
+      if (prof) cudaEventRecord(evs[4 * k + 1], s);
+      if (prof) cudaEventRecord(evs[4 * k + 2], s);
+      wf_shade_specular<false><<<qgrid, block, 0, s>>>(d->view, P, W, C, d->err, WfBatch{});
+      wf_shade_diffuse<false><<<qgrid, block, 0, s>>>(d->view, P, W, C, d->err, WfBatch{});
+      if (guide) {
+        wf_guide_pre<<<qgrid, block, 0, s>>>(d->view, W, C, alpha);
+        if (alpha > 0.0f) gd_launch_queue(G, GQ, (uint32_t)q, s);
+        wf_guide_post<<<qgrid, block, 0, s>>>(d->view, P, W, C, d->err, G);
+      }
+      wf_finish<false><<<qgrid, block, 0, s>>>(d->view, P, W, C, film, WfBatch{});
+      if (prof) cudaEventRecord(evs[4 * k + 3], s);
+    };
+    const unsigned per_bounce = 4u + (guide ? (alpha > 0.0f ? 3u : 2u) : 0u);
+    if (guide) gd_prepare();
+    // the batch of bounces between polls, replayed as one CUDA graph (profiling
+    // runs launch directly: their events bracket single kernels)
+    GraphExec graph;
+    if (!prof) graph = capture_graph(d, [&](cudaStream_t s) {
+      for (int k = 0; k < batch; ++k) bounce(s, k);
+    });
+    for (uint64_t it = 0;; it += batch) {
+      if (graph.exec) {
+        ck(cudaGraphLaunch(graph.exec, st), "cudaGraphLaunch");
+      } else {
+        for (int k = 0; k < batch; ++k) bounce(st, k);
+      }
+      g_launches += per_bounce * batch;
       ck(cudaGetLastError(), "wavefront launch");
       ck(cudaMemcpyAsync(d->wf_live_host, &d->wf_counters->live, sizeof(unsigned int), cudaMemcpyDeviceToHost, st),
          "cudaMemcpyAsync");
@@ -1000,18 +1066,23 @@ int clv_render_batch(clv_device_scene* const* ds, const clv_render_opts* opts, d
     uint32_t max_depth = 0;
     for (uint32_t k = 0; k < n; ++k) max_depth = std::max(max_depth, opts[k].max_depth);
     const int batch = 8;
-    for (uint64_t it = 0;; it += batch) {
+    auto bounces = [&](cudaStream_t s) {
       for (int k = 0; k < batch; ++k) {
-        cudaMemsetAsync(&C->live, 0, 5 * sizeof(unsigned int), st);
+        cudaMemsetAsync(&C->live, 0, 5 * sizeof(unsigned int), s);
         switch (level) {
-          case 0: wf_intersect<0, false, true><<<grid, block, 0, st>>>(S0, W, C, d0->err, nullptr, B); break;
-          case 1: wf_intersect<1, false, true><<<grid, block, 0, st>>>(S0, W, C, d0->err, nullptr, B); break;
-          default: wf_intersect<2, false, true><<<grid, block, 0, st>>>(S0, W, C, d0->err, nullptr, B); break;
+          case 0: wf_intersect<0, false, true><<<grid, block, 0, s>>>(S0, W, C, d0->err, nullptr, B); break;
+          case 1: wf_intersect<1, false, true><<<grid, block, 0, s>>>(S0, W, C, d0->err, nullptr, B); break;
+          default: wf_intersect<2, false, true><<<grid, block, 0, s>>>(S0, W, C, d0->err, nullptr, B); break;
         }
-        wf_shade_specular<true><<<qgrid, block, 0, st>>>(S0, P0, W, C, d0->err, B);
-        wf_shade_diffuse<true><<<qgrid, block, 0, st>>>(S0, P0, W, C, d0->err, B);
-        wf_finish<true><<<qgrid, block, 0, st>>>(S0, P0, W, C, nullptr, B);
+        wf_shade_specular<true><<<qgrid, block, 0, s>>>(S0, P0, W, C, d0->err, B);
+        wf_shade_diffuse<true><<<qgrid, block, 0, s>>>(S0, P0, W, C, d0->err, B);
+        wf_finish<true><<<qgrid, block, 0, s>>>(S0, P0, W, C, nullptr, B);
       }
+    };
+    GraphExec graph = capture_graph(d0, bounces);
+    for (uint64_t it = 0;; it += batch) {
+      if (graph.exec) ck(cudaGraphLaunch(graph.exec, st), "cudaGraphLaunch");
+      else bounces(st);
       g_launches += 4 * batch;
       ck(cudaGetLastError(), "wavefront launch");
       ck(cudaMemcpyAsync(d0->wf_live_host, &C->live, sizeof(unsigned int), cudaMemcpyDeviceToHost, st),

@@ -820,11 +820,15 @@ uint64_t hmix(uint64_t z) {
   z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
   return z ^ (z >> 31);
 }
-int sms() {
-  int dev = 0, n = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-  return n > 0 ? n : 1;
+int sms() {  // cached: launches inside a stream capture make no device queries
+  static int n = 0;
+  if (n == 0) {
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    n = v > 0 ? v : 1;
+  }
+  return n;
 }
 template <class K>
 void smem_attr(K kernel, int bytes) {
@@ -891,12 +895,15 @@ uint4* clv_guide::ensure_slots(uint32_t q) {
   return slot;
 }
 
+void gd_prepare() {
+  sms();
+  smem_attr(guide_infer_kernel<SRC_QUEUE>, GD_SMEM_INFER);
+}
+
 void gd_launch_queue(const GuideDev& G, const GdQueue& Q, uint32_t max_queries, cudaStream_t st) {
   const uint32_t tiles = (max_queries + GD_TILE - 1) / GD_TILE;
   const uint32_t grid = std::max<uint32_t>(1, std::min<uint32_t>(tiles, 2u * (uint32_t)sms()));
-  smem_attr(guide_infer_kernel<SRC_QUEUE>, GD_SMEM_INFER);
   guide_infer_kernel<SRC_QUEUE><<<grid, 128, GD_SMEM_INFER, st>>>(G, Q, ArrayIO{nullptr, nullptr, 0u});
-  clv_internal_count_launches(1);
 }
 
 void gd_reset_records(clv_guide* g, cudaStream_t st) {

@@ -120,6 +120,9 @@ struct clv_guide {
 };
 
 // Host launchers (guide.cu); all asynchronous on `st`.
+// gd_launch_queue neither counts its launch nor sets kernel attributes, so it
+// can be captured into a graph; call gd_prepare once before.
+void gd_prepare();
 void gd_launch_queue(const GuideDev& G, const GdQueue& Q, uint32_t max_queries, cudaStream_t st);
 void gd_reset_records(clv_guide* g, cudaStream_t st);
 GuideDev gd_view(clv_guide* g, const float root_box[6], float alpha);
