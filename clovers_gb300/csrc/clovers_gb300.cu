@@ -53,6 +53,55 @@ __global__ void __launch_bounds__(128, CLV_MINB) raycast_kernel(ClvDeviceScene S
   }
 }
 
+// Persistent form of raycast_kernel: each lane takes the next ray as soon as
+// its traversal ends (one atomic per warp refill on `next`, once 8 lanes or
+// all remaining lanes are idle), so lanes do not sit out the longest ray of
+// their warp (persistent threads with dynamic fetch, Aila & Laine 2009).
+// Every ray runs the same traversal as in raycast_kernel: same results.
+template <int CPLX>
+__global__ void __launch_bounds__(128, CLV_MINB) raycast_persist_kernel(
+    ClvDeviceScene S, const float4* __restrict__ rays, uint64_t n, uint32_t* __restrict__ prim,
+    float* __restrict__ tout, uint32_t* __restrict__ nodes, uint32_t* __restrict__ tests, uint32_t* err,
+    unsigned long long* next) {
+  const bool want = nodes != nullptr || tests != nullptr;
+  const int lane = threadIdx.x & 31;
+  Trav T;
+  float4 stack[CLV_STACK];
+  Hit h;
+  Counters c{0u, 0u};
+  Ray r{};
+  Rng rng;
+  uint64_t i = 0;
+  bool have = false;
+  while (true) {
+    const unsigned act = __activemask();
+    const unsigned idle = __ballot_sync(act, !have);
+    if (idle && (__popc(idle) >= 8 || idle == act)) {
+      const int leader = __ffs(idle) - 1;
+      unsigned long long base = 0;
+      if (lane == leader) base = atomicAdd(next, (unsigned long long)__popc(idle));
+      base = __shfl_sync(act, base, leader);
+      if (!have) {
+        i = base + __popc(idle & ((1u << lane) - 1u));
+        if (i >= n) break;  // no rays left
+        const float4 a = __ldcs(rays + 2 * i), b = __ldcs(rays + 2 * i + 1);
+        r = Ray{mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), 0.0f, 600};
+        c = Counters{0u, 0u};
+        rng.init(0, (uint32_t)i, 0);
+        trav_begin(S, r, a.w, b.w, T, h);
+        have = true;
+      }
+    }
+    if (have && !trav_step<CPLX>(S, r, T, stack, &rng, h, nullptr, want ? &c : nullptr, err)) {
+      __stcs(prim + i, T.found ? hit_gid(S, h.ref) : 0xFFFFFFFFu);
+      __stcs(tout + i, T.found ? h.t : 0.0f);
+      if (nodes) nodes[i] = c.nodes;
+      if (tests) tests[i] = c.prims;
+      have = false;
+    }
+  }
+}
+
 struct RenderParams {
   uint32_t width, height, spp, max_depth;
   uint32_t sample_offset, spt, chunks;
@@ -466,6 +515,7 @@ struct clv_device_scene {
   WfCounters* wf_counters = nullptr;
   unsigned int* wf_live_host = nullptr;  // pinned
   cudaStream_t cap_stream = nullptr;     // private stream for graph capture
+  unsigned long long* ray_next = nullptr;  // work counter of the persistent ray casts
   cudaStream_t capture_stream() {
     if (!cap_stream && cudaStreamCreateWithFlags(&cap_stream, cudaStreamNonBlocking) != cudaSuccess) {
       cudaGetLastError();
@@ -475,6 +525,7 @@ struct clv_device_scene {
   }
   ~clv_device_scene() {
     if (cap_stream) cudaStreamDestroy(cap_stream);
+    if (ray_next) cudaFree(ray_next);
     for (void* p : owned) cudaFree(p);
     if (err) cudaFree(err);
     if (scratch) cudaFree(scratch);
@@ -778,6 +829,7 @@ int clv_scene_upload(const clv_scene* s, clv_device_scene** out) {
     v.mis_depth = h.mis_depth;
     v.camera = h.camera;
     ck(cudaMalloc(&d->err, sizeof(uint32_t)), "cudaMalloc");
+    ck(cudaMalloc(&d->ray_next, sizeof(unsigned long long)), "cudaMalloc");
     ck(cudaMemset(d->err, 0, sizeof(uint32_t)), "cudaMemset");
     d->width = h.width;
     d->height = h.height;
@@ -809,15 +861,20 @@ int clv_raycast_device(const clv_device_scene* d, const float* rays_dev, uint64_
   if ((reinterpret_cast<uintptr_t>(rays_dev) & 15u) != 0) return fail(CLV_E_INVALID, "rays must be 16-byte aligned");
   const int block = 128;
   g_launches += 1;
-  const uint32_t grid = launch_grid(n, block);
+  // persistent grid: every resident block of the launch bound on every SM
+  const uint32_t grid = (uint32_t)std::max<uint64_t>(
+      1, std::min<uint64_t>((n + block - 1) / block, (uint64_t)sm_count() * CLV_MINB));
   const float4* r4 = reinterpret_cast<const float4*>(rays_dev);
   cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e = cudaMemsetAsync(d->ray_next, 0, sizeof(unsigned long long), st);
+  if (e != cudaSuccess) return fail(CLV_E_CUDA, std::string("cudaMemsetAsync: ") + cudaGetErrorString(e));
+  unsigned long long* nx = d->ray_next;
   switch (d->view.compound_level) {
-    case 0: raycast_kernel<0><<<grid, block, 0, st>>>(d->view, r4, n, prim_dev, t_dev, nodes_dev, tests_dev, d->err); break;
-    case 1: raycast_kernel<1><<<grid, block, 0, st>>>(d->view, r4, n, prim_dev, t_dev, nodes_dev, tests_dev, d->err); break;
-    default: raycast_kernel<2><<<grid, block, 0, st>>>(d->view, r4, n, prim_dev, t_dev, nodes_dev, tests_dev, d->err);
+    case 0: raycast_persist_kernel<0><<<grid, block, 0, st>>>(d->view, r4, n, prim_dev, t_dev, nodes_dev, tests_dev, d->err, nx); break;
+    case 1: raycast_persist_kernel<1><<<grid, block, 0, st>>>(d->view, r4, n, prim_dev, t_dev, nodes_dev, tests_dev, d->err, nx); break;
+    default: raycast_persist_kernel<2><<<grid, block, 0, st>>>(d->view, r4, n, prim_dev, t_dev, nodes_dev, tests_dev, d->err, nx);
   }
-  const cudaError_t e = cudaGetLastError();
+  e = cudaGetLastError();
   if (e != cudaSuccess) return fail(CLV_E_CUDA, std::string("raycast launch: ") + cudaGetErrorString(e));
   return CLV_OK;
 }

@@ -654,8 +654,8 @@ __device__ __forceinline__ bool leaf_test(const ClvDeviceScene& S, uint32_t ref,
   return false;
 }
 
-// BVHNode::hit over the flattened tree, one "call" (node or leaf) per loop
-// iteration so that warps reconverge every iteration.
+// BVHNode::hit over the flattened tree, one "call" (node or leaf) per step so
+// that warps reconverge every step.
 //
 // Stack entries are the deferred far children of the nodes on the current
 // path (ref, entry distance, slab interval).  Whether a node's near subtree
@@ -663,102 +663,123 @@ __device__ __forceinline__ bool leaf_test(const ClvDeviceScene& S, uint32_t ref,
 // stack belongs to an ancestor whose near subtree is being traversed, so when
 // a hit is accepted all current entries are marked, which keeps the marked
 // entries a prefix [0, marked) of the stack.
-template <int CPLX>
-__device__ bool closest_hit(const ClvDeviceScene& S, const Ray& r, float tmin, float tmax, Rng* rng, Hit& hit,
-                            Rec* full, Counters* cnt, uint32_t* err) {
+// The scalar state (kept in registers); the stack array lives apart from it
+// because an indexed array forces its enclosing object into local memory.
+struct Trav {
+  RayPre R;
+  float tmin, tmax;
+  int sp, marked;
+  uint32_t ref;
+  float N, F;
+  bool found;
+};
+__device__ __forceinline__ void trav_begin(const ClvDeviceScene& S, const Ray& r, float tmin, float tmax, Trav& T,
+                                           Hit& hit) {
   hit.ref = CLV_REF_EMPTY;
   hit.t = 0.0f;
-  RayPre R;
-  R.o = r.o;
-  R.d = r.d;
-  R.inv = mk(1.0f / r.d.x, 1.0f / r.d.y, 1.0f / r.d.z);
-  R.fast = S.boxes_div_safe && dir_ok(r.d.x) && dir_ok(r.d.y) && dir_ok(r.d.z) && coord_ok(r.o.x) &&
-           coord_ok(r.o.y) && coord_ok(r.o.z);
-  float4 stack[CLV_STACK];
-  int sp = 0, marked = 0;
-  uint32_t ref = S.root;
-  float N, F;
-  slab(S.root_box, r.o, R.inv, N, F);
-  bool found = false;
-  while (true) {
-    bool descend = false;
-    if (CLV_REF_KIND(ref) == CLV_REF_NODE) {
-      if (cnt) cnt->nodes++;
-      if (slab_pass(N, F, tmin, tmax)) {
-        const float4* p4 = reinterpret_cast<const float4*>(S.nodes + CLV_REF_INDEX(ref));
-        const float4 q0 = __ldg(p4), q1 = __ldg(p4 + 1), q2 = __ldg(p4 + 2), q3 = __ldg(p4 + 3);
-        const float lb[6] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y};
-        const float rb[6] = {q1.z, q1.w, q2.x, q2.y, q2.z, q2.w};
-        const uint32_t L = __float_as_uint(q3.x), Rr = __float_as_uint(q3.y);
-        uint32_t next = CLV_REF_EMPTY;
-        bool left_next = true;
-        if (L != CLV_REF_EMPTY && Rr != CLV_REF_EMPTY) {
-          float ld, rd;
-          const bool lh = box_distance_pre(lb, R, ld), rh = box_distance_pre(rb, R, rd);
-          if (lh && rh) {
-            left_next = ld < rd;
-            next = left_next ? L : Rr;
-            const uint32_t far = left_next ? Rr : L;
-            float fN = 0.0f, fF = 0.0f;
-            if (CLV_REF_KIND(far) == CLV_REF_NODE) {
-              float fb[6];
+  T.R.o = r.o;
+  T.R.d = r.d;
+  T.R.inv = mk(1.0f / r.d.x, 1.0f / r.d.y, 1.0f / r.d.z);
+  T.R.fast = S.boxes_div_safe && dir_ok(r.d.x) && dir_ok(r.d.y) && dir_ok(r.d.z) && coord_ok(r.o.x) &&
+             coord_ok(r.o.y) && coord_ok(r.o.z);
+  T.tmin = tmin;
+  T.tmax = tmax;
+  T.sp = 0;
+  T.marked = 0;
+  T.ref = S.root;
+  slab(S.root_box, r.o, T.R.inv, T.N, T.F);
+  T.found = false;
+}
+// One node visit or leaf test, then the next reference (descend, or pop the
+// next deferred far child whose visit the reference would make).  Returns
+// false when the traversal is over (result in hit / T.found).
+template <int CPLX>
+__device__ __forceinline__ bool trav_step(const ClvDeviceScene& S, const Ray& r, Trav& T, float4* stack, Rng* rng,
+                                          Hit& hit, Rec* full, Counters* cnt, uint32_t* err) {
+  const RayPre& R = T.R;
+  uint32_t ref = T.ref;
+  if (CLV_REF_KIND(ref) == CLV_REF_NODE) {
+    if (cnt) cnt->nodes++;
+    if (slab_pass(T.N, T.F, T.tmin, T.tmax)) {
+      const float4* p4 = reinterpret_cast<const float4*>(S.nodes + CLV_REF_INDEX(ref));
+      const float4 q0 = __ldg(p4), q1 = __ldg(p4 + 1), q2 = __ldg(p4 + 2), q3 = __ldg(p4 + 3);
+      const float lb[6] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y};
+      const float rb[6] = {q1.z, q1.w, q2.x, q2.y, q2.z, q2.w};
+      const uint32_t L = __float_as_uint(q3.x), Rr = __float_as_uint(q3.y);
+      uint32_t next = CLV_REF_EMPTY;
+      bool left_next = true;
+      if (L != CLV_REF_EMPTY && Rr != CLV_REF_EMPTY) {
+        float ld, rd;
+        const bool lh = box_distance_pre(lb, R, ld), rh = box_distance_pre(rb, R, rd);
+        if (lh && rh) {
+          left_next = ld < rd;
+          next = left_next ? L : Rr;
+          const uint32_t far = left_next ? Rr : L;
+          float fN = 0.0f, fF = 0.0f;
+          if (CLV_REF_KIND(far) == CLV_REF_NODE) {
+            float fb[6];
 #pragma unroll
-              for (int k = 0; k < 6; ++k) fb[k] = left_next ? rb[k] : lb[k];
-              slab(fb, r.o, R.inv, fN, fF);
-            }
-            if (sp < CLV_STACK) {
-              stack[sp++] = make_float4(__uint_as_float(far), fmaxf(ld, rd), fN, fF);
-            } else if (err) {
-              atomicOr(err, CLV_ERR_STACK);
-            }
-          } else if (lh) {
-            next = L;
-          } else if (rh) {
-            next = Rr;
-            left_next = false;
+            for (int k = 0; k < 6; ++k) fb[k] = left_next ? rb[k] : lb[k];
+            slab(fb, r.o, R.inv, fN, fF);
           }
-        } else if (L != CLV_REF_EMPTY) {
+          if (T.sp < CLV_STACK) {
+            stack[T.sp++] = make_float4(__uint_as_float(far), fmaxf(ld, rd), fN, fF);
+          } else if (err) {
+            atomicOr(err, CLV_ERR_STACK);
+          }
+        } else if (lh) {
           next = L;
-        } else if (Rr != CLV_REF_EMPTY) {
+        } else if (rh) {
           next = Rr;
           left_next = false;
         }
-        if (next != CLV_REF_EMPTY) {
-          if (CLV_REF_KIND(next) == CLV_REF_NODE) {
-            float nb[6];
+      } else if (L != CLV_REF_EMPTY) {
+        next = L;
+      } else if (Rr != CLV_REF_EMPTY) {
+        next = Rr;
+        left_next = false;
+      }
+      if (next != CLV_REF_EMPTY) {
+        if (CLV_REF_KIND(next) == CLV_REF_NODE) {
+          float nb[6];
 #pragma unroll
-            for (int k = 0; k < 6; ++k) nb[k] = left_next ? lb[k] : rb[k];
-            slab(nb, r.o, R.inv, N, F);
-          }
-          ref = next;
-          descend = true;
+          for (int k = 0; k < 6; ++k) nb[k] = left_next ? lb[k] : rb[k];
+          slab(nb, r.o, R.inv, T.N, T.F);
         }
-      }
-    } else {
-      if (leaf_test<CPLX>(S, ref, r, tmin, tmax, rng, hit, full, cnt, err)) {
-        tmax = hit.t;
-        found = true;
-        marked = sp;
+        T.ref = next;
+        return true;
       }
     }
-    if (descend) continue;
-    // pop the next deferred far child whose visit the reference would make
-    bool popped = false;
-    while (sp > 0) {
-      --sp;
-      const float4 e = stack[sp];
-      const bool near_hit = sp < marked;
-      if (marked > sp) marked = sp;
-      if (near_hit && hit.t < e.y) continue;  // near subtree's hit is closer than the far box
-      ref = __float_as_uint(e.x);
-      N = e.z;
-      F = e.w;
-      popped = true;
-      break;
+  } else {
+    if (leaf_test<CPLX>(S, ref, r, T.tmin, T.tmax, rng, hit, full, cnt, err)) {
+      T.tmax = hit.t;
+      T.found = true;
+      T.marked = T.sp;
     }
-    if (!popped) break;
   }
-  return found;
+  // pop the next deferred far child whose visit the reference would make
+  while (T.sp > 0) {
+    --T.sp;
+    const float4 e = stack[T.sp];
+    const bool near_hit = T.sp < T.marked;
+    if (T.marked > T.sp) T.marked = T.sp;
+    if (near_hit && hit.t < e.y) continue;  // near subtree's hit is closer than the far box
+    T.ref = __float_as_uint(e.x);
+    T.N = e.z;
+    T.F = e.w;
+    return true;
+  }
+  return false;
+}
+template <int CPLX>
+__device__ bool closest_hit(const ClvDeviceScene& S, const Ray& r, float tmin, float tmax, Rng* rng, Hit& hit,
+                            Rec* full, Counters* cnt, uint32_t* err) {
+  Trav T;
+  float4 stack[CLV_STACK];
+  trav_begin(S, r, tmin, tmax, T, hit);
+  while (trav_step<CPLX>(S, r, T, stack, rng, hit, full, cnt, err)) {
+  }
+  return T.found;
 }
 
 // Full record of the closest hit (deterministic rebuild for primitives).
