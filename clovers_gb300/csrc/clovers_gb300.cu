@@ -19,7 +19,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/clovers_gpu.h"
+#include "clovers_gpu.h"
 #include "clv_device.cuh"
 #include "scene.hpp"
 #include "wavefront.cuh"
