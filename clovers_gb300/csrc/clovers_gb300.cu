@@ -54,16 +54,18 @@ __global__ void __launch_bounds__(128, CLV_MINB) raycast_kernel(ClvDeviceScene S
 }
 
 // Persistent form of raycast_kernel: each lane takes the next ray as soon as
-// its traversal ends (one atomic per warp refill on `next`, once 8 lanes or
-// all remaining lanes are idle), so lanes do not sit out the longest ray of
-// their warp (persistent threads with dynamic fetch, Aila & Laine 2009).
-// Every ray runs the same traversal as in raycast_kernel: same results.
-template <int CPLX>
-__global__ void __launch_bounds__(128, CLV_MINB) raycast_persist_kernel(
+// its traversal ends (one atomic per warp and step in which lanes are idle),
+// so lanes do not sit out the longest ray of their warp (persistent threads
+// with dynamic fetch, Aila & Laine 2009).  Every ray runs the same traversal
+// as in raycast_kernel: same results.  COUNT: per-ray visit counts wanted.
+#ifndef CLV_MINB_RAY
+#define CLV_MINB_RAY CLV_MINB
+#endif
+template <int CPLX, bool COUNT>
+__global__ void __launch_bounds__(128, CLV_MINB_RAY) raycast_persist_kernel(
     ClvDeviceScene S, const float4* __restrict__ rays, uint64_t n, uint32_t* __restrict__ prim,
     float* __restrict__ tout, uint32_t* __restrict__ nodes, uint32_t* __restrict__ tests, uint32_t* err,
     unsigned long long* next) {
-  const bool want = nodes != nullptr || tests != nullptr;
   const int lane = threadIdx.x & 31;
   Trav T;
   float4 stack[CLV_STACK];
@@ -76,7 +78,7 @@ __global__ void __launch_bounds__(128, CLV_MINB) raycast_persist_kernel(
   while (true) {
     const unsigned act = __activemask();
     const unsigned idle = __ballot_sync(act, !have);
-    if (idle && (__popc(idle) >= 8 || idle == act)) {
+    if (idle) {
       const int leader = __ffs(idle) - 1;
       unsigned long long base = 0;
       if (lane == leader) base = atomicAdd(next, (unsigned long long)__popc(idle));
@@ -92,11 +94,13 @@ __global__ void __launch_bounds__(128, CLV_MINB) raycast_persist_kernel(
         have = true;
       }
     }
-    if (have && !trav_step<CPLX>(S, r, T, stack, &rng, h, nullptr, want ? &c : nullptr, err)) {
+    if (have && !trav_step<CPLX>(S, r, T, stack, &rng, h, nullptr, COUNT ? &c : nullptr, err)) {
       __stcs(prim + i, T.found ? hit_gid(S, h.ref) : 0xFFFFFFFFu);
       __stcs(tout + i, T.found ? h.t : 0.0f);
-      if (nodes) nodes[i] = c.nodes;
-      if (tests) tests[i] = c.prims;
+      if (COUNT) {
+        if (nodes) nodes[i] = c.nodes;
+        if (tests) tests[i] = c.prims;
+      }
       have = false;
     }
   }
@@ -863,16 +867,20 @@ int clv_raycast_device(const clv_device_scene* d, const float* rays_dev, uint64_
   g_launches += 1;
   // persistent grid: every resident block of the launch bound on every SM
   const uint32_t grid = (uint32_t)std::max<uint64_t>(
-      1, std::min<uint64_t>((n + block - 1) / block, (uint64_t)sm_count() * CLV_MINB));
+      1, std::min<uint64_t>((n + block - 1) / block, (uint64_t)sm_count() * CLV_MINB_RAY));
   const float4* r4 = reinterpret_cast<const float4*>(rays_dev);
   cudaStream_t st = (cudaStream_t)stream;
   cudaError_t e = cudaMemsetAsync(d->ray_next, 0, sizeof(unsigned long long), st);
   if (e != cudaSuccess) return fail(CLV_E_CUDA, std::string("cudaMemsetAsync: ") + cudaGetErrorString(e));
   unsigned long long* nx = d->ray_next;
-  switch (d->view.compound_level) {
-    case 0: raycast_persist_kernel<0><<<grid, block, 0, st>>>(d->view, r4, n, prim_dev, t_dev, nodes_dev, tests_dev, d->err, nx); break;
-    case 1: raycast_persist_kernel<1><<<grid, block, 0, st>>>(d->view, r4, n, prim_dev, t_dev, nodes_dev, tests_dev, d->err, nx); break;
-    default: raycast_persist_kernel<2><<<grid, block, 0, st>>>(d->view, r4, n, prim_dev, t_dev, nodes_dev, tests_dev, d->err, nx);
+  const bool count = nodes_dev || tests_dev;
+  switch (d->view.compound_level * 2 + (count ? 1 : 0)) {
+    case 0: raycast_persist_kernel<0, false><<<grid, block, 0, st>>>(d->view, r4, n, prim_dev, t_dev, nodes_dev, tests_dev, d->err, nx); break;
+    case 1: raycast_persist_kernel<0, true><<<grid, block, 0, st>>>(d->view, r4, n, prim_dev, t_dev, nodes_dev, tests_dev, d->err, nx); break;
+    case 2: raycast_persist_kernel<1, false><<<grid, block, 0, st>>>(d->view, r4, n, prim_dev, t_dev, nodes_dev, tests_dev, d->err, nx); break;
+    case 3: raycast_persist_kernel<1, true><<<grid, block, 0, st>>>(d->view, r4, n, prim_dev, t_dev, nodes_dev, tests_dev, d->err, nx); break;
+    case 4: raycast_persist_kernel<2, false><<<grid, block, 0, st>>>(d->view, r4, n, prim_dev, t_dev, nodes_dev, tests_dev, d->err, nx); break;
+    default: raycast_persist_kernel<2, true><<<grid, block, 0, st>>>(d->view, r4, n, prim_dev, t_dev, nodes_dev, tests_dev, d->err, nx);
   }
   e = cudaGetLastError();
   if (e != cudaSuccess) return fail(CLV_E_CUDA, std::string("raycast launch: ") + cudaGetErrorString(e));
