@@ -53,6 +53,76 @@ __global__ void __launch_bounds__(128, CLV_MINB) raycast_kernel(ClvDeviceScene S
   }
 }
 
+// ---- ray order -----------------------------------------------------------
+// Ray casts traverse their rays in the order of a Morton code of the origin
+// (6 bits per axis of the scene box): warps then start from nearby points and
+// share the nodes near the origins in L1/L2.  A counting sort (histogram,
+// exclusive scan, scatter) gives the permutation; results go back to each
+// ray's own index, so the order changes nothing but speed.
+#define CLV_SORT_AXIS_BITS 6
+#define CLV_SORT_BINS (1u << (3 * CLV_SORT_AXIS_BITS))
+__device__ __forceinline__ uint32_t spread3(uint32_t x) {  // bit k of x -> bit 3k
+  x = (x | (x << 16)) & 0x030000FFu;
+  x = (x | (x << 8)) & 0x0300F00Fu;
+  x = (x | (x << 4)) & 0x030C30C3u;
+  x = (x | (x << 2)) & 0x09249249u;
+  return x;
+}
+__device__ __forceinline__ uint32_t cell_of(float v, float lo, float scale) {
+  const float c = (v - lo) * scale;
+  return c > 0.0f ? (uint32_t)fminf(c, (float)((1u << CLV_SORT_AXIS_BITS) - 1)) : 0u;
+}
+__global__ void ray_key_hist(const float4* __restrict__ rays, uint64_t n, float3 lo, float3 scale,
+                             uint32_t* __restrict__ key, uint32_t* __restrict__ hist) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const float4 o = __ldg(rays + 2 * i);
+    const uint32_t k = spread3(cell_of(o.x, lo.x, scale.x)) | (spread3(cell_of(o.y, lo.y, scale.y)) << 1) |
+                       (spread3(cell_of(o.z, lo.z, scale.z)) << 2);
+    key[i] = k;
+    atomicAdd(hist + k, 1u);
+  }
+}
+// Exclusive scan of CLV_SORT_BINS counts in place; one block of 1024 threads.
+__global__ void __launch_bounds__(1024) ray_bins_scan(uint32_t* __restrict__ hist) {
+  constexpr uint32_t per = CLV_SORT_BINS / 1024;
+  __shared__ uint32_t warp_sum[32];
+  const uint32_t t = threadIdx.x, lane = t & 31, w = t >> 5;
+  uint32_t* h = hist + t * per;
+  uint32_t sum = 0;
+  for (uint32_t k = 0; k < per; ++k) sum += h[k];
+  uint32_t incl = sum;  // inclusive scan over the block: warps, then warp totals
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, off);
+    if (lane >= (uint32_t)off) incl += v;
+  }
+  if (lane == 31) warp_sum[w] = incl;
+  __syncthreads();
+  if (w == 0) {
+    uint32_t v = warp_sum[lane], x = v;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, off);
+      if (lane >= (uint32_t)off) x += y;
+    }
+    warp_sum[lane] = x - v;  // exclusive prefix of the warp totals
+  }
+  __syncthreads();
+  uint32_t run = warp_sum[w] + incl - sum;
+  for (uint32_t k = 0; k < per; ++k) {
+    const uint32_t c = h[k];
+    h[k] = run;
+    run += c;
+  }
+}
+__global__ void ray_scatter(const uint32_t* __restrict__ key, uint64_t n, uint32_t* __restrict__ offs,
+                            uint32_t* __restrict__ perm) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    perm[atomicAdd(offs + key[i], 1u)] = (uint32_t)i;
+}
+
 // Persistent form of raycast_kernel: each lane takes the next ray as soon as
 // its traversal ends (one atomic per warp and step in which lanes are idle),
 // so lanes do not sit out the longest ray of their warp (persistent threads
@@ -65,7 +135,7 @@ template <int CPLX, bool COUNT>
 __global__ void __launch_bounds__(128, CLV_MINB_RAY) raycast_persist_kernel(
     ClvDeviceScene S, const float4* __restrict__ rays, uint64_t n, uint32_t* __restrict__ prim,
     float* __restrict__ tout, uint32_t* __restrict__ nodes, uint32_t* __restrict__ tests, uint32_t* err,
-    unsigned long long* next) {
+    unsigned long long* next, const uint32_t* __restrict__ perm) {
   const int lane = threadIdx.x & 31;
   Trav T;
   float4 stack[CLV_STACK];
@@ -84,8 +154,9 @@ __global__ void __launch_bounds__(128, CLV_MINB_RAY) raycast_persist_kernel(
       if (lane == leader) base = atomicAdd(next, (unsigned long long)__popc(idle));
       base = __shfl_sync(act, base, leader);
       if (!have) {
-        i = base + __popc(idle & ((1u << lane) - 1u));
-        if (i >= n) break;  // no rays left
+        const uint64_t k = base + __popc(idle & ((1u << lane) - 1u));
+        if (k >= n) break;  // no rays left
+        i = perm ? (uint64_t)__ldg(perm + k) : k;
         const float4 a = __ldcs(rays + 2 * i), b = __ldcs(rays + 2 * i + 1);
         r = Ray{mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), 0.0f, 600};
         c = Counters{0u, 0u};
@@ -520,6 +591,18 @@ struct clv_device_scene {
   unsigned int* wf_live_host = nullptr;  // pinned
   cudaStream_t cap_stream = nullptr;     // private stream for graph capture
   unsigned long long* ray_next = nullptr;  // work counter of the persistent ray casts
+  uint32_t* ray_sort = nullptr;            // ray order: histogram, keys, permutation
+  uint64_t ray_sort_cap = 0;               // rays the sort scratch holds
+  uint32_t* ray_sort_scratch(uint64_t n) {
+    if (n > ray_sort_cap) {
+      if (ray_sort) cudaFree(ray_sort);
+      ray_sort = nullptr;
+      ray_sort_cap = 0;
+      ck(cudaMalloc(&ray_sort, (CLV_SORT_BINS + 2 * n) * sizeof(uint32_t)), "cudaMalloc ray order");
+      ray_sort_cap = n;
+    }
+    return ray_sort;
+  }
   cudaStream_t capture_stream() {
     if (!cap_stream && cudaStreamCreateWithFlags(&cap_stream, cudaStreamNonBlocking) != cudaSuccess) {
       cudaGetLastError();
@@ -530,6 +613,7 @@ struct clv_device_scene {
   ~clv_device_scene() {
     if (cap_stream) cudaStreamDestroy(cap_stream);
     if (ray_next) cudaFree(ray_next);
+    if (ray_sort) cudaFree(ray_sort);
     for (void* p : owned) cudaFree(p);
     if (err) cudaFree(err);
     if (scratch) cudaFree(scratch);
@@ -874,13 +958,37 @@ int clv_raycast_device(const clv_device_scene* d, const float* rays_dev, uint64_
   if (e != cudaSuccess) return fail(CLV_E_CUDA, std::string("cudaMemsetAsync: ") + cudaGetErrorString(e));
   unsigned long long* nx = d->ray_next;
   const bool count = nodes_dev || tests_dev;
+  // traversal order (small batches go in their own order)
+  const uint32_t* perm = nullptr;
+  if (n >= (1u << 16) && n <= 0xFFFFFFFFull) {
+    uint32_t* hist = nullptr;
+    try {
+      hist = const_cast<clv_device_scene*>(d)->ray_sort_scratch(n);
+    } catch (std::exception& ex) {
+      return fail(CLV_E_CUDA, ex.what());
+    }
+    uint32_t* keys = hist + CLV_SORT_BINS;
+    uint32_t* order = keys + n;
+    const float* b = d->view.root_box;
+    const float side = (float)(1u << CLV_SORT_AXIS_BITS);
+    auto sc = [&](int a) { return b[2 * a + 1] > b[2 * a] ? side / (b[2 * a + 1] - b[2 * a]) : 0.0f; };
+    const float3 lo = make_float3(b[0], b[2], b[4]), scale = make_float3(sc(0), sc(1), sc(2));
+    const uint32_t sg = launch_grid(n, 256);
+    e = cudaMemsetAsync(hist, 0, CLV_SORT_BINS * sizeof(uint32_t), st);
+    if (e != cudaSuccess) return fail(CLV_E_CUDA, std::string("cudaMemsetAsync: ") + cudaGetErrorString(e));
+    ray_key_hist<<<sg, 256, 0, st>>>(r4, n, lo, scale, keys, hist);
+    ray_bins_scan<<<1, 1024, 0, st>>>(hist);
+    ray_scatter<<<sg, 256, 0, st>>>(keys, n, hist, order);
+    g_launches += 3;
+    perm = order;
+  }
   switch (d->view.compound_level * 2 + (count ? 1 : 0)) {
-    case 0: raycast_persist_kernel<0, false><<<grid, block, 0, st>>>(d->view, r4, n, prim_dev, t_dev, nodes_dev, tests_dev, d->err, nx); break;
-    case 1: raycast_persist_kernel<0, true><<<grid, block, 0, st>>>(d->view, r4, n, prim_dev, t_dev, nodes_dev, tests_dev, d->err, nx); break;
-    case 2: raycast_persist_kernel<1, false><<<grid, block, 0, st>>>(d->view, r4, n, prim_dev, t_dev, nodes_dev, tests_dev, d->err, nx); break;
-    case 3: raycast_persist_kernel<1, true><<<grid, block, 0, st>>>(d->view, r4, n, prim_dev, t_dev, nodes_dev, tests_dev, d->err, nx); break;
-    case 4: raycast_persist_kernel<2, false><<<grid, block, 0, st>>>(d->view, r4, n, prim_dev, t_dev, nodes_dev, tests_dev, d->err, nx); break;
-    default: raycast_persist_kernel<2, true><<<grid, block, 0, st>>>(d->view, r4, n, prim_dev, t_dev, nodes_dev, tests_dev, d->err, nx);
+    case 0: raycast_persist_kernel<0, false><<<grid, block, 0, st>>>(d->view, r4, n, prim_dev, t_dev, nodes_dev, tests_dev, d->err, nx, perm); break;
+    case 1: raycast_persist_kernel<0, true><<<grid, block, 0, st>>>(d->view, r4, n, prim_dev, t_dev, nodes_dev, tests_dev, d->err, nx, perm); break;
+    case 2: raycast_persist_kernel<1, false><<<grid, block, 0, st>>>(d->view, r4, n, prim_dev, t_dev, nodes_dev, tests_dev, d->err, nx, perm); break;
+    case 3: raycast_persist_kernel<1, true><<<grid, block, 0, st>>>(d->view, r4, n, prim_dev, t_dev, nodes_dev, tests_dev, d->err, nx, perm); break;
+    case 4: raycast_persist_kernel<2, false><<<grid, block, 0, st>>>(d->view, r4, n, prim_dev, t_dev, nodes_dev, tests_dev, d->err, nx, perm); break;
+    default: raycast_persist_kernel<2, true><<<grid, block, 0, st>>>(d->view, r4, n, prim_dev, t_dev, nodes_dev, tests_dev, d->err, nx, perm);
   }
   e = cudaGetLastError();
   if (e != cudaSuccess) return fail(CLV_E_CUDA, std::string("raycast launch: ") + cudaGetErrorString(e));

@@ -159,7 +159,11 @@ int clv_resolve_srgb(const float* xyz, uint32_t width, uint32_t height, uint8_t*
 int clv_raycast(clv_device_scene* dscene, const float* rays, uint64_t n, uint32_t* prim_id, float* t,
                 uint32_t* node_visits, uint32_t* prim_tests);
 
-/* Device variant, asynchronous on `stream`. */
+/* Device variant, asynchronous on `stream`.  Batches of 65536 rays or more
+ * are traversed in the order of a Morton code of their origins (a counting
+ * sort on the device; results still go to each ray's own index); the sort's
+ * scratch (8 bytes per ray) is kept by the scene and grown on demand, so a
+ * call with more rays than any before it allocates. */
 int clv_raycast_device(const clv_device_scene* dscene, const float* rays_dev, uint64_t n, uint32_t* prim_id_dev,
                        float* t_dev, uint32_t* node_visits_dev, uint32_t* prim_tests_dev, void* stream);
 
