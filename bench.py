@@ -657,9 +657,9 @@ def main():
                 "e2e": {"value": round(RAYS / r_e2e / 1e9, 4), "unit": "Grays/s", "h2d_bytes_per_step": RAYS * 32,
                         "d2h_bytes_per_step": RAYS * 8},
                 "nodes_per_ray": round(nv / RAYS, 2), "prims_per_ray": round(pt / RAYS, 2),
-                "roofline": {"kernel": "raycast_kernel", "bound": "hbm", "achieved": round(r_ach, 1),
+                "roofline": {"kernel": "raycast_persist_kernel", "bound": "hbm", "achieved": round(r_ach, 1),
                              "peak": hbm_peak, "unit": "GB/s", "frac": round(r_ach / hbm_peak, 4),
-                             "traffic": traffic.get("raycast_kernel.bytes_per_launch"),
+                             "traffic": traffic.get("raycast_persist_kernel.bytes_per_launch"),
                              "algorithmic_bytes_per_launch": int(rbytes)}}
         if rank == 0 and world == 1 and not args.no_cpu:
             import oracle

@@ -1,6 +1,7 @@
 // Kernels and the C ABI (include/clovers_gpu.h) of the GB300 render path.
 //
-//  raycast_kernel  closest-hit ray casts (the parity path), one thread per ray
+//  raycast_persist_kernel  closest-hit ray casts (the parity path), persistent
+//                  threads over rays sorted by origin
 //  render_kernel   path tracing: one thread per (pixel, chunk of samples);
 //                  camera ray -> trace (clovers-cli/src/trace.rs:21-122, as a
 //                  loop) -> film rule (draw_cpu.rs:131-142) -> f64 sums
@@ -28,30 +29,6 @@
 using namespace clvd;
 
 // ------------------------------------------------------------------ kernels --
-
-template <int CPLX>
-__global__ void __launch_bounds__(128, CLV_MINB) raycast_kernel(ClvDeviceScene S, const float4* __restrict__ rays, uint64_t n,
-                                                      uint32_t* __restrict__ prim, float* __restrict__ tout,
-                                                      uint32_t* __restrict__ nodes, uint32_t* __restrict__ tests,
-                                                      uint32_t* err) {
-  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  const bool want = nodes != nullptr || tests != nullptr;
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-    const float4 a = __ldcs(rays + 2 * i), b = __ldcs(rays + 2 * i + 1);
-    const Ray r{mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), 0.0f, 600};
-    Hit h;
-    Counters c{0u, 0u};
-    Rng rng;
-    rng.init(0, (uint32_t)i, 0);
-    const bool any = closest_hit<CPLX>(S, r, a.w, b.w, &rng, h, nullptr, want ? &c : nullptr, err);
-    __stcs(prim + i, any ? hit_gid(S, h.ref) : 0xFFFFFFFFu);
-    __stcs(tout + i, any ? h.t : 0.0f);
-    if (want) {
-      if (nodes) nodes[i] = c.nodes;
-      if (tests) tests[i] = c.prims;
-    }
-  }
-}
 
 // ---- ray order -----------------------------------------------------------
 // Ray casts traverse their rays in the order of a Morton code of the origin
@@ -123,11 +100,11 @@ __global__ void ray_scatter(const uint32_t* __restrict__ key, uint64_t n, uint32
     perm[atomicAdd(offs + key[i], 1u)] = (uint32_t)i;
 }
 
-// Persistent form of raycast_kernel: each lane takes the next ray as soon as
-// its traversal ends (one atomic per warp and step in which lanes are idle),
-// so lanes do not sit out the longest ray of their warp (persistent threads
-// with dynamic fetch, Aila & Laine 2009).  Every ray runs the same traversal
-// as in raycast_kernel: same results.  COUNT: per-ray visit counts wanted.
+// Closest-hit ray casts (the parity path), persistent: each lane takes the
+// next ray as soon as its traversal ends (one atomic per warp and step in
+// which lanes are idle), so lanes do not sit out the longest ray of their
+// warp (persistent threads with dynamic fetch, Aila & Laine 2009).  Every ray
+// runs closest_hit's exact traversal.  COUNT: per-ray visit counts wanted.
 #ifndef CLV_MINB_RAY
 #define CLV_MINB_RAY 9  // 56 registers, no spills: 36 warps per SM (measured best of 6..16)
 #endif
