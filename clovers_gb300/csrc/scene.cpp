@@ -9,6 +9,7 @@
 #include "scene.hpp"
 
 #include <algorithm>
+#include <cctype>
 #include <cmath>
 #include <cstring>
 #include <fstream>
@@ -263,6 +264,216 @@ void color_xyz(const Value& v, float out[3]) {
   }
 }
 
+// PLY reader for objects/ply.rs: the vertex element's x, y, z and the face
+// element's vertex_indices, from an ASCII or binary (either byte order) body.
+// Value conversions follow ply.rs's property_to_float / property_to_vec_u32.
+class PlyReader {
+ public:
+  std::vector<float> verts;     // x, y, z per vertex
+  std::vector<uint64_t> faces;  // first three indices of each face
+  PlyReader(const std::vector<char>& d, const std::string& path) : d_(d), path_(path) { parse(); }
+
+ private:
+  enum Type { I8, U8, I16, U16, I32, U32, F32, F64, NONE };
+  struct Prop {
+    std::string name;
+    Type type = NONE, count = NONE;
+    bool list = false;
+  };
+  struct Elem {
+    std::string name;
+    uint64_t count = 0;
+    std::vector<Prop> props;
+  };
+  const std::vector<char>& d_;
+  std::string path_;
+  size_t pos_ = 0;
+  int format_ = 0;  // 0 ascii, 1 binary little endian, 2 binary big endian
+
+  [[noreturn]] void bad(const std::string& m) const { throw std::runtime_error("PLY file `" + path_ + "`: " + m); }
+  static Type type_of(const std::string& t) {
+    if (t == "char" || t == "int8") return I8;
+    if (t == "uchar" || t == "uint8") return U8;
+    if (t == "short" || t == "int16") return I16;
+    if (t == "ushort" || t == "uint16") return U16;
+    if (t == "int" || t == "int32") return I32;
+    if (t == "uint" || t == "uint32") return U32;
+    if (t == "float" || t == "float32") return F32;
+    if (t == "double" || t == "float64") return F64;
+    return NONE;
+  }
+  static int size_of(Type t) { return t <= U8 ? 1 : t <= U16 ? 2 : t <= F32 ? 4 : 8; }
+  std::string line() {
+    if (pos_ >= d_.size()) bad("header ends early");
+    size_t e = pos_;
+    while (e < d_.size() && d_[e] != '\n') ++e;
+    std::string l(d_.data() + pos_, e - pos_);
+    pos_ = e < d_.size() ? e + 1 : e;
+    if (!l.empty() && l.back() == '\r') l.pop_back();
+    return l;
+  }
+  static std::vector<std::string> words(const std::string& l) {
+    std::vector<std::string> w;
+    size_t i = 0;
+    while (i < l.size()) {
+      while (i < l.size() && (l[i] == ' ' || l[i] == '\t')) ++i;
+      size_t j = i;
+      while (j < l.size() && l[j] != ' ' && l[j] != '\t') ++j;
+      if (j > i) w.emplace_back(l.substr(i, j - i));
+      i = j;
+    }
+    return w;
+  }
+  std::string token() {  // ASCII body
+    while (pos_ < d_.size() && std::isspace((unsigned char)d_[pos_])) ++pos_;
+    const size_t b = pos_;
+    while (pos_ < d_.size() && !std::isspace((unsigned char)d_[pos_])) ++pos_;
+    if (b == pos_) bad("body ends early");
+    return std::string(d_.data() + b, pos_ - b);
+  }
+  void raw(Type t, unsigned char* out) {  // binary body, host byte order
+    const int n = size_of(t);
+    if (pos_ + n > d_.size()) bad("body ends early");
+    unsigned char b[8];
+    std::memcpy(b, d_.data() + pos_, n);
+    pos_ += n;
+    const uint16_t one = 1;
+    const bool host_le = *reinterpret_cast<const unsigned char*>(&one) == 1;
+    const bool file_le = format_ == 1;
+    for (int k = 0; k < n; ++k) out[k] = b[host_le == file_le ? k : n - 1 - k];
+  }
+  // an integer-valued property (list counts, indices); signed values as read
+  int64_t integer(Type t) {
+    if (t == F32 || t == F64 || t == NONE) bad("non-integer list count or index");
+    if (format_ == 0) return std::strtoll(token().c_str(), nullptr, 10);
+    unsigned char b[8];
+    raw(t, b);
+    switch (t) {
+      case I8: { int8_t v; std::memcpy(&v, b, 1); return v; }
+      case U8: return b[0];
+      case I16: { int16_t v; std::memcpy(&v, b, 2); return v; }
+      case U16: { uint16_t v; std::memcpy(&v, b, 2); return v; }
+      case I32: { int32_t v; std::memcpy(&v, b, 4); return v; }
+      default: { uint32_t v; std::memcpy(&v, b, 4); return v; }
+    }
+  }
+  // property_to_float: int, uint, float and double properties, as f32
+  float coord(Type t) {
+    if (t == F32) {
+      if (format_ == 0) return std::strtof(token().c_str(), nullptr);
+      float v;
+      unsigned char b[4];
+      raw(t, b);
+      std::memcpy(&v, b, 4);
+      return v;
+    }
+    if (t == F64) {
+      if (format_ == 0) return (float)std::strtod(token().c_str(), nullptr);
+      double v;
+      unsigned char b[8];
+      raw(t, b);
+      std::memcpy(&v, b, 8);
+      return (float)v;
+    }
+    if (t == I32 || t == U32) return (float)integer(t);
+    bad("unsupported vertex coordinate type");
+  }
+  void skip(Type t) {
+    if (format_ == 0) token();
+    else {
+      unsigned char b[8];
+      raw(t, b);
+    }
+  }
+  void parse() {
+    if (line() != "ply") bad("not a PLY file");
+    std::vector<Elem> elems;
+    while (true) {
+      const std::vector<std::string> w = words(line());
+      if (w.empty()) continue;
+      if (w[0] == "end_header") break;
+      if (w[0] == "comment" || w[0] == "obj_info") continue;
+      if (w[0] == "format") {
+        if (w.size() < 2) bad("bad format line");
+        format_ = w[1] == "ascii" ? 0 : w[1] == "binary_little_endian" ? 1 : w[1] == "binary_big_endian" ? 2 : -1;
+        if (format_ < 0) bad("unknown format " + w[1]);
+      } else if (w[0] == "element") {
+        if (w.size() < 3) bad("bad element line");
+        Elem e;
+        e.name = w[1];
+        e.count = std::strtoull(w[2].c_str(), nullptr, 10);
+        elems.push_back(e);
+      } else if (w[0] == "property") {
+        if (elems.empty()) bad("property before element");
+        Prop p;
+        if (w.size() >= 5 && w[1] == "list") {
+          p.list = true;
+          p.count = type_of(w[2]);
+          p.type = type_of(w[3]);
+          p.name = w[4];
+        } else if (w.size() >= 3) {
+          p.type = type_of(w[1]);
+          p.name = w[2];
+        } else {
+          bad("bad property line");
+        }
+        if (p.type == NONE || (p.list && p.count == NONE)) bad("unknown property type");
+        elems.back().props.push_back(p);
+      } else {
+        bad("unknown header line `" + w[0] + "`");
+      }
+    }
+    bool have_v = false, have_f = false;
+    for (const Elem& e : elems) {
+      const bool vert = e.name == "vertex", face = e.name == "face";
+      int xyz[3] = {-1, -1, -1}, vi = -1;
+      for (size_t k = 0; k < e.props.size(); ++k) {
+        const Prop& p = e.props[k];
+        if (vert && !p.list && (p.name == "x" || p.name == "y" || p.name == "z")) xyz[p.name[0] - 'x'] = (int)k;
+        if (face && p.list && p.name == "vertex_indices") vi = (int)k;
+      }
+      if (vert) {
+        if (xyz[0] < 0 || xyz[1] < 0 || xyz[2] < 0) bad("vertex element without x, y, z");
+        if (e.count > (1ull << 32)) bad("too many vertices");
+        verts.assign(3 * e.count, 0.0f);
+        have_v = true;
+      }
+      if (face) {
+        if (vi < 0) bad("face element without vertex_indices");
+        const Type it = e.props[vi].type;
+        if (it == I8 || it == F32 || it == F64) bad("unsupported vertex_indices type");
+        if (e.count > (1ull << 32)) bad("too many faces");
+        faces.reserve(3 * e.count);
+        have_f = true;
+      }
+      for (uint64_t r = 0; r < e.count; ++r) {
+        for (size_t k = 0; k < e.props.size(); ++k) {
+          const Prop& p = e.props[k];
+          if (p.list) {
+            const int64_t n = integer(p.count);
+            if (n < 0) bad("negative list length");
+            const bool take = face && (int)k == vi;
+            if (take && n < 3) bad("face with fewer than 3 vertices");
+            for (int64_t j = 0; j < n; ++j) {
+              if (take && j < 3) {
+                const int64_t v = integer(p.type);
+                faces.push_back((uint64_t)(v < 0 ? -v : v));  // signed lists: unsigned_abs
+              } else {
+                skip(p.type);
+              }
+            }
+          } else if (vert && ((int)k == xyz[0] || (int)k == xyz[1] || (int)k == xyz[2])) {
+            verts[3 * r + (p.name[0] - 'x')] = coord(p.type);
+          } else {
+            skip(p.type);
+          }
+        }
+      }
+    }
+    if (!have_v || !have_f) bad("vertex or face element missing");
+  }
+};
+
 struct Emitted {
   uint32_t ref = CLV_REF_EMPTY;
   bool has_box = false;
@@ -474,12 +685,54 @@ class Builder {
     return o;
   }
 
-  void stl_triangles(const Value& o, std::vector<Emitted>& out) {  // objects/stl.rs:52-104
-    const std::string path = o.at("path").as_string("path");
+  // Rotation3::from_euler_angles(roll, pitch, yaw) in degrees, row-major
+  static void euler_matrix(const V3& rot, float R[9]) {
+    const float sr = std::sin(rot.x * kDegToRad), cr = std::cos(rot.x * kDegToRad);
+    const float sp = std::sin(rot.y * kDegToRad), cp = std::cos(rot.y * kDegToRad);
+    const float sy = std::sin(rot.z * kDegToRad), cy = std::cos(rot.z * kDegToRad);
+    const float M[9] = {cy * cp, cy * sp * sr - sy * cr, cy * sp * cr + sy * sr,
+                        sy * cp, sy * sp * sr + cy * cr, sy * sp * cr - cy * sr,
+                        -sp,     cp * sr,                cp * cr};
+    std::memcpy(R, M, sizeof M);
+  }
+
+  std::vector<char> read_file(const std::string& path, const char* what) {
     std::ifstream f(path, std::ios::binary);
     if (!f && !base_dir.empty()) f.open(base_dir + "/" + path, std::ios::binary);
-    if (!f) throw std::runtime_error("cannot open STL file `" + path + "`");
-    std::vector<char> data((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+    if (!f) throw std::runtime_error(std::string("cannot open ") + what + " file `" + path + "`");
+    return std::vector<char>((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+  }
+
+  // objects/ply.rs:55-118: vertices x, y, z (int, uint, float or double
+  // properties), faces from the first three `vertex_indices` of each face
+  // (unsigned lists as read, signed lists by absolute value), rotated, scaled
+  // and offset like STL triangles.  Binary (either byte order) and ASCII bodies.
+  void ply_triangles(const Value& o, std::vector<Emitted>& out) {
+    const std::string path = o.at("path").as_string("path");
+    const std::vector<char> data = read_file(path, "PLY");
+    PlyReader ply(data, path);
+    const uint32_t mat = material_ref(o.find("material"), true);
+    const float scale = o.at("scale").as_f32("scale");
+    const V3 center = vec3_of(o.at("center"), "center");
+    float R[9];
+    euler_matrix(vec3_of(o.at("rotation"), "rotation"), R);
+    for (size_t f = 0; f < ply.faces.size(); f += 3) {
+      V3 p[3];
+      for (int k = 0; k < 3; ++k) {
+        const uint64_t vi = ply.faces[f + k];
+        if (vi >= ply.verts.size() / 3) throw std::runtime_error("PLY face index out of range in `" + path + "`");
+        const V3 a(ply.verts[3 * vi], ply.verts[3 * vi + 1], ply.verts[3 * vi + 2]);
+        const V3 r(R[0] * a.x + R[1] * a.y + R[2] * a.z, R[3] * a.x + R[4] * a.y + R[5] * a.z,
+                   R[6] * a.x + R[7] * a.y + R[8] * a.z);
+        p[k] = V3(r.x * scale, r.y * scale, r.z * scale) + center;
+      }
+      out.push_back(planar(p[0], p[1] - p[0], p[2] - p[0], mat, true, false));
+    }
+  }
+
+  void stl_triangles(const Value& o, std::vector<Emitted>& out) {  // objects/stl.rs:52-104
+    const std::string path = o.at("path").as_string("path");
+    const std::vector<char> data = read_file(path, "STL");
     if (data.size() < 84) throw std::runtime_error("STL file too short");
     uint32_t n;
     std::memcpy(&n, data.data() + 80, 4);
@@ -487,14 +740,8 @@ class Builder {
     const uint32_t mat = material_ref(o.find("material"), true);
     const float scale = o.at("scale").as_f32("scale");
     const V3 center = vec3_of(o.at("center"), "center");
-    const V3 rot = vec3_of(o.at("rotation"), "rotation");
-    const float sr = std::sin(rot.x * kDegToRad), cr = std::cos(rot.x * kDegToRad);
-    const float sp = std::sin(rot.y * kDegToRad), cp = std::cos(rot.y * kDegToRad);
-    const float sy = std::sin(rot.z * kDegToRad), cy = std::cos(rot.z * kDegToRad);
-    // Rotation3::from_euler_angles(roll, pitch, yaw) as a row-major matrix
-    const float R[9] = {cy * cp, cy * sp * sr - sy * cr, cy * sp * cr + sy * sr,
-                        sy * cp, sy * sp * sr + cy * cr, sy * sp * cr - cy * sr,
-                        -sp,     cp * sr,                cp * cr};
+    float R[9];
+    euler_matrix(vec3_of(o.at("rotation"), "rotation"), R);
     for (uint32_t i = 0; i < n; ++i) {
       const char* rec = data.data() + 84 + (size_t)i * 50;
       V3 p[3];
@@ -557,10 +804,11 @@ class Builder {
       e.c = c0 + ((0.5f - 0.0f) / (1.0f - 0.0f)) * (c1 - c0);
       return e;
     }
-    if (kind == "ObjectList" || kind == "STL") {
+    if (kind == "ObjectList" || kind == "STL" || kind == "PLY") {
       Emitted e;
       e.is_list = true;
       if (kind == "STL") stl_triangles(o, e.items);
+      else if (kind == "PLY") ply_triangles(o, e.items);
       else
         for (auto& c : o.at("objects").arr) e.items.push_back(object(c));
       // HitableList::new (hitable.rs:139-143)

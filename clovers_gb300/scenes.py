@@ -156,6 +156,44 @@ def write_binary_stl(path, triangles):
     return path
 
 
+def write_ply(path, vertices, faces, fmt="binary_little_endian", coord_type="float", index_type="int",
+              extra_vertex_props=0):
+    """PLY mesh in the layout of the reference's ply/ files: vertex x, y, z (+ extra
+    float properties, written as zero), face list uchar <index_type> vertex_indices.
+    fmt: ascii, binary_little_endian or binary_big_endian."""
+    v = np.asarray(vertices, np.float64).reshape(-1, 3)
+    f = np.asarray(faces, np.int64).reshape(-1, 3)
+    ctype = {"float": "f4", "double": "f8", "int": "i4", "uint": "u4"}[coord_type]
+    itype = {"int": "i4", "uint": "u4", "short": "i2", "ushort": "u2", "uchar": "u1"}[index_type]
+    head = ["ply", "format %s 1.0" % fmt, "comment clovers_gb300 test mesh", "element vertex %d" % len(v)]
+    head += ["property %s %s" % (coord_type, c) for c in "xyz"]
+    head += ["property float extra%d" % k for k in range(extra_vertex_props)]
+    head += ["element face %d" % len(f), "property list uchar %s vertex_indices" % index_type, "end_header"]
+    with open(path, "wb") as out:
+        out.write(("\n".join(head) + "\n").encode())
+        if fmt == "ascii":
+            lines = []
+            for row in v:
+                vals = [repr(float(np.float32(x))) if coord_type == "float" else
+                        (repr(float(x)) if coord_type == "double" else str(int(x))) for x in row]
+                lines.append(" ".join(vals + ["0"] * extra_vertex_props))
+            lines += ["3 %d %d %d" % tuple(r) for r in f]
+            out.write(("\n".join(lines) + "\n").encode())
+            return path
+        e = "<" if fmt == "binary_little_endian" else ">"
+        vt = np.dtype([(c, e + ctype) for c in "xyz"] + [("extra%d" % k, e + "f4") for k in range(extra_vertex_props)])
+        va = np.zeros(len(v), vt)
+        for k, c in enumerate("xyz"):
+            va[c] = v[:, k]
+        out.write(va.tobytes())
+        ft = np.dtype([("n", "u1"), ("i", e + itype, (3,))])
+        fa = np.zeros(len(f), ft)
+        fa["n"] = 3
+        fa["i"] = f
+        out.write(fa.tobytes())
+    return path
+
+
 def prism_triangles():
     """A triangular prism as 8 triangles (2 end caps, 3 rectangular sides split in two)."""
     a = np.array([[0, 0, 0], [1, 0, 0], [0.5, 0.866, 0]], np.float32)

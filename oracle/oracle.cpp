@@ -1422,6 +1422,123 @@ struct Loader {
     }
   }
 
+  // clovers/src/objects/ply.rs:55-118 with ply-rs's reading of the file:
+  // vertex x/y/z (int, uint, float, double -> f32), face vertex_indices (the
+  // first three; unsigned lists as read, signed lists by absolute value).
+  void load_ply(const Value& o, std::vector<HPtr>& out) {
+    std::string path = o.at("path").as_string("path");
+    std::ifstream f(path, std::ios::binary);
+    if (!f && !base_dir.empty()) f.open(base_dir + "/" + path, std::ios::binary);
+    if (!f) throw std::runtime_error("cannot open PLY file " + path);
+    std::string blob((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+    const size_t hend = blob.find("end_header");
+    if (blob.compare(0, 3, "ply") != 0 || hend == std::string::npos) throw std::runtime_error("not a PLY file");
+    size_t body = blob.find('\n', hend);
+    body = body == std::string::npos ? blob.size() : body + 1;
+    struct P { std::string name, type, count; bool list; };
+    struct E { std::string name; unsigned long long n; std::vector<P> props; };
+    std::vector<E> elems;
+    std::string fmt;
+    std::istringstream hs(blob.substr(0, hend));
+    std::string ln;
+    while (std::getline(hs, ln)) {
+      if (!ln.empty() && ln.back() == '\r') ln.pop_back();
+      std::istringstream ls(ln);
+      std::string w;
+      ls >> w;
+      if (w == "format") ls >> fmt;
+      else if (w == "element") { E e; ls >> e.name >> e.n; elems.push_back(e); }
+      else if (w == "property") {
+        P p;
+        std::string t;
+        ls >> t;
+        p.list = t == "list";
+        if (p.list) ls >> p.count >> p.type >> p.name;
+        else { p.type = t; ls >> p.name; }
+        elems.back().props.push_back(p);
+      }
+    }
+    auto width = [](const std::string& t) -> int {
+      if (t == "char" || t == "int8" || t == "uchar" || t == "uint8") return 1;
+      if (t == "short" || t == "int16" || t == "ushort" || t == "uint16") return 2;
+      if (t == "double" || t == "float64") return 8;
+      return 4;
+    };
+    const bool ascii = fmt == "ascii", big = fmt == "binary_big_endian";
+    std::istringstream as(ascii ? blob.substr(body) : std::string());
+    size_t pos = body;
+    // one value as (double, is floating type); integers exactly as int64
+    auto next = [&](const std::string& t, long long& iv) -> double {
+      const bool fl = t == "float" || t == "float32" || t == "double" || t == "float64";
+      if (ascii) {
+        std::string tok;
+        if (!(as >> tok)) throw std::runtime_error("PLY body ends early");
+        if (t == "float" || t == "float32") return (double)std::strtof(tok.c_str(), nullptr);
+        if (fl) return std::strtod(tok.c_str(), nullptr);
+        iv = std::strtoll(tok.c_str(), nullptr, 10);
+        return (double)iv;
+      }
+      const int n = width(t);
+      if (pos + n > blob.size()) throw std::runtime_error("PLY body ends early");
+      unsigned char b[8];
+      for (int k = 0; k < n; ++k) b[k] = (unsigned char)blob[pos + (big ? n - 1 - k : k)];  // little-endian host
+      pos += n;
+      if (t == "float" || t == "float32") { float v; std::memcpy(&v, b, 4); return v; }
+      if (fl) { double v; std::memcpy(&v, b, 8); return v; }
+      const bool sg = t == "char" || t == "int8" || t == "short" || t == "int16" || t == "int" || t == "int32";
+      unsigned long long u = 0;
+      std::memcpy(&u, b, n);
+      if (sg && n < 8 && (u >> (8 * n - 1)) & 1ull) u |= ~0ull << (8 * n);
+      iv = (long long)u;
+      return (double)iv;
+    };
+    std::vector<Vec3> verts;
+    std::vector<unsigned long long> idx;
+    for (const E& e : elems)
+      for (unsigned long long r = 0; r < e.n; ++r) {
+        Float xyz[3] = {0, 0, 0};
+        for (const P& p : e.props) {
+          long long iv = 0;
+          if (p.list) {
+            next(p.count, iv);
+            const long long cnt = iv;
+            for (long long j = 0; j < cnt; ++j) {
+              const double v = next(p.type, iv);
+              (void)v;
+              if (e.name == "face" && p.name == "vertex_indices" && j < 3) idx.push_back(iv < 0 ? -iv : iv);
+            }
+          } else {
+            const double v = next(p.type, iv);
+            if (e.name == "vertex" && (p.name == "x" || p.name == "y" || p.name == "z")) {
+              const bool is_f32 = p.type == "float" || p.type == "float32";
+              xyz[p.name[0] - 'x'] = is_f32 ? (Float)v : (Float)v;  // f64 and ints: one rounding to f32
+            }
+          }
+        }
+        if (e.name == "vertex") verts.emplace_back(xyz[0], xyz[1], xyz[2]);
+      }
+    const Material* mat = material_ref(o.find("material"));
+    Float scale = o.at("scale").as_f32();
+    Vec3 center = json_vec3(o.at("center"), "center");
+    Vec3 rot = json_vec3(o.at("rotation"), "rotation");
+    Float sr = std::sin(rot.x * RADS_PER_DEG), cr = std::cos(rot.x * RADS_PER_DEG);
+    Float sp = std::sin(rot.y * RADS_PER_DEG), cp = std::cos(rot.y * RADS_PER_DEG);
+    Float sy = std::sin(rot.z * RADS_PER_DEG), cy = std::cos(rot.z * RADS_PER_DEG);
+    Float R[9] = {cy * cp, cy * sp * sr - sy * cr, cy * sp * cr + sy * sr,
+                  sy * cp, sy * sp * sr + cy * cr, sy * sp * cr - cy * sr,
+                  -sp,     cp * sr,                cp * cr};
+    for (size_t i = 0; i + 2 < idx.size(); i += 3) {
+      Vec3 p[3];
+      for (int k = 0; k < 3; ++k) {
+        const Vec3 a = verts.at(idx[i + k]);
+        Vec3 r(R[0] * a.x + R[1] * a.y + R[2] * a.z, R[3] * a.x + R[4] * a.y + R[5] * a.z,
+               R[6] * a.x + R[7] * a.y + R[8] * a.z);
+        p[k] = r * scale + center;
+      }
+      out.emplace_back(new Planar(p[0], p[1] - p[0], p[2] - p[0], mat, true));
+    }
+  }
+
   HPtr object(const Value& o, std::vector<HPtr>* flat_list) {
     const std::string& kind = o.at("kind").as_string("object kind");
     if (kind == "Sphere")
@@ -1444,9 +1561,10 @@ struct Loader {
     if (kind == "RotateY") return HPtr(new RotateY(object(o.at("object"), nullptr), o.at("angle").as_f32()));
     if (kind == "Translate")
       return HPtr(new Translate(object(o.at("object"), nullptr), json_vec3(o.at("offset"), "offset")));
-    if (kind == "ObjectList" || kind == "STL") {
+    if (kind == "ObjectList" || kind == "STL" || kind == "PLY") {
       std::unique_ptr<HitableList> l(new HitableList());
       if (kind == "STL") load_stl(o, l->items);
+      else if (kind == "PLY") load_ply(o, l->items);
       else
         for (auto& c : o.at("objects").arr) l->items.push_back(object(c, nullptr));
       if (!vec_bounding_box(l->items, l->box)) throw std::runtime_error("No bounding box for hitables");

@@ -99,3 +99,23 @@ def test_fast_slab_division_is_ieee_division():
     bad = ctypes.c_uint64()
     _lib.check(_lib.lib().clv_selftest_division(1 << 28, 12345, ctypes.byref(bad)))
     assert bad.value == 0
+
+
+def test_ply_mesh_scene_parity(tmp_path):
+    # a PLY mesh (big-endian binary body) in a scene with lights and a floor, origins around the mesh
+    rng = np.random.default_rng(12)
+    n = 48
+    xs, zs = np.meshgrid(np.linspace(-1, 1, n), np.linspace(-1, 1, n), indexing="ij")
+    v = np.stack([xs, 0.3 * rng.random((n, n)), zs], -1).reshape(-1, 3).astype(np.float32)
+    f = np.array([(i * n + j, (i + 1) * n + j, (i + 1) * n + j + 1) for i in range(n - 1) for j in range(n - 1)] +
+                 [(i * n + j, (i + 1) * n + j + 1, i * n + j + 1) for i in range(n - 1) for j in range(n - 1)])
+    ply = scenes.write_ply(str(tmp_path / "m.ply"), v, f, fmt="binary_big_endian")
+    sc = scenes.dense_mesh_scene("unused.stl")
+    for o in sc["objects"]:
+        if o.get("kind") == "STL":
+            o.update({"kind": "PLY", "path": ply, "scale": 2.0, "center": [0.0, 1.0, 0.0], "rotation": [5, 40, 0]})
+    path = scenes.write_scene(sc, str(tmp_path / "s.json"))
+    rays = scenes.random_rays(131072, seed=13)
+    rays[:, :3] = rays[:, :3] * 6.0 - 3.0
+    frac = _compare(cg.Scene.from_json(path, 64, 36).upload(), oracle.Scene.from_json(path, 64, 36), rays)
+    assert frac > 0.2
