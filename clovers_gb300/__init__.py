@@ -88,6 +88,11 @@ class Scene:
         check(lib().clv_scene_from_mesh(v.ctypes.data, v.shape[0], i.ctypes.data, i.shape[0], ctypes.byref(out)))
         return cls(out.value)
 
+    def set_watertight(self, on=True):
+        """Watertight triangle test (CLV_OPT_WATERTIGHT) for the next upload."""
+        check(lib().clv_scene_set_option(self._h, _lib.CLV_OPT_WATERTIGHT, 1 if on else 0))
+        return self
+
     def info(self):
         inf = _lib.SceneInfoC()
         check(lib().clv_scene_info_get(self._h, ctypes.byref(inf)))

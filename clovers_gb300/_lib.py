@@ -16,6 +16,7 @@ P = ctypes.POINTER
 
 CLV_OK, CLV_E_INVALID, CLV_E_SCENE, CLV_E_CUDA, CLV_E_DEVICE = 0, -1, -2, -3, -4
 CLV_BVH_LAM, CLV_BVH_SAH = 0, 1
+CLV_OPT_WATERTIGHT = 1
 MODES = {"path-tracing": 0, "normal-map": 1, "bvh-test-count": 2, "primitive-test-count": 3}
 
 
@@ -52,6 +53,7 @@ SIGNATURES = {
                                          P(ctypes.c_void_p)]),
     "clv_scene_from_mesh": (c_i32, [ctypes.c_void_p, c_u32, ctypes.c_void_p, c_u32, P(ctypes.c_void_p)]),
     "clv_scene_info_get": (c_i32, [ctypes.c_void_p, P(SceneInfoC)]),
+    "clv_scene_set_option": (c_i32, [ctypes.c_void_p, c_u32, c_u32]),
     "clv_scene_free": (None, [ctypes.c_void_p]),
     "clv_scene_upload": (c_i32, [ctypes.c_void_p, P(ctypes.c_void_p)]),
     "clv_device_scene_free": (None, [ctypes.c_void_p]),

@@ -513,6 +513,7 @@ void clv_internal_count_launches(unsigned long long n) { g_launches += n; }
 
 struct clv_scene {
   clv::HostScene host;
+  uint32_t watertight = 0;  // CLV_OPT_WATERTIGHT
 };
 
 // Whether every coordinate of every BVH box is 0 or of magnitude in
@@ -847,6 +848,16 @@ int clv_scene_info_get(const clv_scene* s, clv_scene_info* out) {
 
 void clv_scene_free(clv_scene* s) { delete s; }
 
+int clv_scene_set_option(clv_scene* s, uint32_t option, uint32_t value) {
+  if (!s) return fail(CLV_E_INVALID, "null argument");
+  if (option == CLV_OPT_WATERTIGHT) {
+    if (value > 1) return fail(CLV_E_INVALID, "CLV_OPT_WATERTIGHT takes 0 or 1");
+    s->watertight = value;
+    return CLV_OK;
+  }
+  return fail(CLV_E_INVALID, "unknown scene option");
+}
+
 int clv_scene_upload(const clv_scene* s, clv_device_scene** out) {
   if (!s || !out) return fail(CLV_E_INVALID, "null argument");
   try {
@@ -893,6 +904,10 @@ int clv_scene_upload(const clv_scene* s, clv_device_scene** out) {
     v.boxes_div_safe = boxes_div_safe(h) ? 1u : 0u;
     v.mis_depth = h.mis_depth;
     v.camera = h.camera;
+    v.watertight = s->watertight;
+    v.tri_verts = nullptr;
+    if (s->watertight && !h.tri_verts.empty())
+      v.tri_verts = upload(h.tri_verts, o);
     ck(cudaMalloc(&d->err, sizeof(uint32_t)), "cudaMalloc");
     ck(cudaMalloc(&d->ray_next, sizeof(unsigned long long)), "cudaMalloc");
     ck(cudaMemset(d->err, 0, sizeof(uint32_t)), "cudaMemset");

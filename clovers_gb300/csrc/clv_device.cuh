@@ -174,6 +174,56 @@ __device__ __forceinline__ bool planar_test(const float f[16], bool tri, const R
   if (tri) in = in && (alpha + beta <= 1.0f);
   return in;
 }
+// Watertight ray/triangle test (Woop, Benthin & Wald 2013, "Watertight
+// Ray/Triangle Intersection", JCGT 2(1)): edge functions in a ray-aligned
+// shear frame, redone in double when one is exactly 0, so a ray through a
+// shared edge or vertex hits at least one of the triangles that share it.
+// Two-sided like Triangle::hit, t in [tmin, tmax]; alpha / beta are the
+// barycentric weights of the second and third vertex (Triangle::hit's plane
+// coordinates along u and v).  Not the reference's test: used only in scenes
+// loaded with CLV_OPT_WATERTIGHT.
+__device__ __forceinline__ bool tri_watertight(const float4* vtx, const Ray& r, float tmin, float tmax, float& t,
+                                               float& alpha, float& beta) {
+  const float4 p0 = __ldg(vtx), p1 = __ldg(vtx + 1), p2 = __ldg(vtx + 2);
+  const float ax = fabsf(r.d.x), ay = fabsf(r.d.y), az = fabsf(r.d.z);
+  const int kz = ax > ay ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
+  int kx = kz == 2 ? 0 : kz + 1, ky = kx == 2 ? 0 : kx + 1;
+  const float dz = comp(r.d, kz);
+  if (dz < 0.0f) {  // keep the winding
+    const int tmp = kx;
+    kx = ky;
+    ky = tmp;
+  }
+  const float sx = comp(r.d, kx) / dz, sy = comp(r.d, ky) / dz, sz = 1.0f / dz;
+  const V A = sub(mk(p0.x, p0.y, p0.z), r.o), B = sub(mk(p1.x, p1.y, p1.z), r.o), C = sub(mk(p2.x, p2.y, p2.z), r.o);
+  const float Ax = comp(A, kx) - sx * comp(A, kz), Ay = comp(A, ky) - sy * comp(A, kz);
+  const float Bx = comp(B, kx) - sx * comp(B, kz), By = comp(B, ky) - sy * comp(B, kz);
+  const float Cx = comp(C, kx) - sx * comp(C, kz), Cy = comp(C, ky) - sy * comp(C, kz);
+  float U = Cx * By - Cy * Bx, W1 = Ax * Cy - Ay * Cx, W2 = Bx * Ay - By * Ax;
+  if (U == 0.0f || W1 == 0.0f || W2 == 0.0f) {
+    U = (float)((double)Cx * (double)By - (double)Cy * (double)Bx);
+    W1 = (float)((double)Ax * (double)Cy - (double)Ay * (double)Cx);
+    W2 = (float)((double)Bx * (double)Ay - (double)By * (double)Ax);
+  }
+  if ((U < 0.0f || W1 < 0.0f || W2 < 0.0f) && (U > 0.0f || W1 > 0.0f || W2 > 0.0f)) return false;
+  const float det = U + W1 + W2;
+  if (det == 0.0f) return false;
+  const float T = U * (sz * comp(A, kz)) + W1 * (sz * comp(B, kz)) + W2 * (sz * comp(C, kz));
+  t = T / det;
+  if (!(t >= tmin && t <= tmax)) return false;
+  alpha = W1 / det;
+  beta = W2 / det;
+  return true;
+}
+// A triangle or quad of the scene: its plane record in f and the hit test of
+// the scene's triangle mode.
+__device__ __forceinline__ bool planar_hit(const ClvDeviceScene& S, bool tri, uint32_t idx, float f[16], const Ray& r,
+                                           float tmin, float tmax, float& t, float& alpha, float& beta) {
+  load_planar(tri ? S.tris : S.quads, idx, f);
+  if (tri && S.watertight)
+    return tri_watertight(reinterpret_cast<const float4*>(S.tri_verts) + 3 * (size_t)idx, r, tmin, tmax, t, alpha, beta);
+  return planar_test(f, tri, r, tmin, tmax, t, alpha, beta);
+}
 __device__ __forceinline__ void face(Rec& rec, const Ray& r, V outward) {
   rec.front = dot(r.d, outward) < 0.0f;
   rec.n = rec.front ? outward : neg(outward);
@@ -247,8 +297,7 @@ __device__ __noinline__ bool ObjEval<LEVEL>::hit(const ClvDeviceScene& S, uint32
   if (kind == CLV_REF_TRI || kind == CLV_REF_QUAD) {
     if (cnt) cnt->prims++;
     float f[16], t, a, b;
-    load_planar(kind == CLV_REF_TRI ? S.tris : S.quads, idx, f);
-    if (!planar_test(f, kind == CLV_REF_TRI, r, tmin, tmax, t, a, b)) return false;
+    if (!planar_hit(S, kind == CLV_REF_TRI, idx, f, r, tmin, tmax, t, a, b)) return false;
     planar_record(f, r, t, a, b, rec);
     rec.mat = kind == CLV_REF_TRI ? S.tri_mat[idx] : S.quad_mat[idx];
     return true;
@@ -443,8 +492,7 @@ __device__ __forceinline__ int chain_hit(const ClvDeviceScene& S, uint32_t top, 
   } else if (kind == CLV_REF_TRI || kind == CLV_REF_QUAD) {
     if (cnt) cnt->prims++;
     float f[16], t, a, b;
-    load_planar(kind == CLV_REF_TRI ? S.tris : S.quads, idx, f);
-    if (planar_test(f, kind == CLV_REF_TRI, r, tmin, tmax, t, a, b)) {
+    if (planar_hit(S, kind == CLV_REF_TRI, idx, f, r, tmin, tmax, t, a, b)) {
       planar_record(f, r, t, a, b, rec);
       rec.mat = kind == CLV_REF_TRI ? S.tri_mat[idx] : S.quad_mat[idx];
       any = true;
@@ -500,9 +548,8 @@ __device__ __noinline__ bool compound_leaf(const ClvDeviceScene& S, uint32_t ref
 // pdf_value of one MIS leaf object (HitableTrait::pdf_value of each type).
 __device__ __forceinline__ float planar_pdf(const ClvDeviceScene& S, bool tri, uint32_t idx, V origin, V dir) {
   float f[16], t, a, b;
-  load_planar(tri ? S.tris : S.quads, idx, f);
   Ray r{origin, dir, 0.0f, 0};
-  if (!planar_test(f, tri, r, CLV_EPS_ACNE, CLV_FLT_MAX * 2.0f, t, a, b)) return 0.0f;
+  if (!planar_hit(S, tri, idx, f, r, CLV_EPS_ACNE, CLV_FLT_MAX * 2.0f, t, a, b)) return 0.0f;
   Rec rec;
   planar_record(f, r, t, a, b, rec);
   float dist2 = t * t * nsq(dir);
@@ -594,6 +641,48 @@ __device__ __forceinline__ float divc(const RayPre& R, float a, int axis) {
   const float d = comp(R.d, axis), inv = comp(R.inv, axis);
   return R.fast ? div_fast(a, d, inv) : a / d;
 }
+// Exit distance of a box widened by 4 gamma_3 (gamma_n = n u / (1 - n u),
+// u = 2^-24) toward +infinity, the conservative box test of Ize 2013
+// ("Robust BVH Ray Traversal", JCGT 2(2)) that keeps watertight triangles
+// from being culled with their boxes.  Watertight scenes only.
+__device__ __forceinline__ float widen_exit(float f) { return fmaxf(f, f + fabsf(f) * 7.1525574e-7f); }
+// The box tests of watertight scenes: the exit distance widened, and a zero
+// direction component constraining nothing while the origin lies within that
+// slab (inclusive) and missing otherwise, where the reference's forms compute
+// 0 * inf = NaN and reject a ray that runs along a box face.
+__device__ __forceinline__ void slab_wide(const float* b, const RayPre& R, float& N, float& F) {
+  float n = -CLV_FLT_MAX * 2.0f, f = CLV_FLT_MAX * 2.0f;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const float o = comp(R.o, a);
+    if (comp(R.d, a) == 0.0f) {
+      if (o < b[2 * a] || o > b[2 * a + 1]) f = -CLV_FLT_MAX * 2.0f;
+      continue;
+    }
+    const float t0 = (b[2 * a] - o) * comp(R.inv, a), t1 = (b[2 * a + 1] - o) * comp(R.inv, a);
+    n = fmaxf(n, fminf(t0, t1));
+    f = fminf(f, fmaxf(t0, t1));
+  }
+  N = n;
+  F = widen_exit(f);
+}
+__device__ __forceinline__ bool box_distance_wide(const float* b, const RayPre& R, float& out) {
+  float tmin = -CLV_FLT_MAX * 2.0f, tmax = CLV_FLT_MAX * 2.0f;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const float o = comp(R.o, a);
+    if (comp(R.d, a) == 0.0f) {
+      if (o < b[2 * a] || o > b[2 * a + 1]) return false;
+      continue;
+    }
+    const float t1 = divc(R, b[2 * a] - o, a), t2 = divc(R, b[2 * a + 1] - o, a);
+    tmin = fmaxf(tmin, fminf(t1, t2));
+    tmax = fminf(tmax, fmaxf(t1, t2));
+  }
+  out = tmin;
+  tmax = widen_exit(tmax);
+  return tmax >= tmin && tmax > 0.0f;
+}
 // AABB::distance with div_rn
 __device__ __forceinline__ bool box_distance_pre(const float* b, const RayPre& R, float& out) {
   float tx1 = divc(R, b[0] - R.o.x, 0), tx2 = divc(R, b[1] - R.o.x, 0);
@@ -617,8 +706,7 @@ __device__ __forceinline__ bool leaf_test(const ClvDeviceScene& S, uint32_t ref,
   if (kind == CLV_REF_TRI || kind == CLV_REF_QUAD) {
     if (cnt) cnt->prims++;
     float f[16], t, a, b;
-    load_planar(kind == CLV_REF_TRI ? S.tris : S.quads, idx, f);
-    if (!planar_test(f, kind == CLV_REF_TRI, r, tmin, tmax, t, a, b)) return false;
+    if (!planar_hit(S, kind == CLV_REF_TRI, idx, f, r, tmin, tmax, t, a, b)) return false;
     hit.t = t;
     hit.ref = ref;
     hit.a = a;
@@ -687,7 +775,8 @@ __device__ __forceinline__ void trav_begin(const ClvDeviceScene& S, const Ray& r
   T.sp = 0;
   T.marked = 0;
   T.ref = S.root;
-  slab(S.root_box, r.o, T.R.inv, T.N, T.F);
+  if (S.watertight) slab_wide(S.root_box, T.R, T.N, T.F);
+  else slab(S.root_box, r.o, T.R.inv, T.N, T.F);
   T.found = false;
 }
 // One node visit or leaf test, then the next reference (descend, or pop the
@@ -710,7 +799,9 @@ __device__ __forceinline__ bool trav_step(const ClvDeviceScene& S, const Ray& r,
       bool left_next = true;
       if (L != CLV_REF_EMPTY && Rr != CLV_REF_EMPTY) {
         float ld, rd;
-        const bool lh = box_distance_pre(lb, R, ld), rh = box_distance_pre(rb, R, rd);
+        const bool wide = S.watertight != 0;
+        const bool lh = wide ? box_distance_wide(lb, R, ld) : box_distance_pre(lb, R, ld);
+        const bool rh = wide ? box_distance_wide(rb, R, rd) : box_distance_pre(rb, R, rd);
         if (lh && rh) {
           left_next = ld < rd;
           next = left_next ? L : Rr;
@@ -720,7 +811,8 @@ __device__ __forceinline__ bool trav_step(const ClvDeviceScene& S, const Ray& r,
             float fb[6];
 #pragma unroll
             for (int k = 0; k < 6; ++k) fb[k] = left_next ? rb[k] : lb[k];
-            slab(fb, r.o, R.inv, fN, fF);
+            if (wide) slab_wide(fb, R, fN, fF);
+            else slab(fb, r.o, R.inv, fN, fF);
           }
           if (T.sp < CLV_STACK) {
             stack[T.sp++] = make_float4(__uint_as_float(far), fmaxf(ld, rd), fN, fF);
@@ -744,7 +836,8 @@ __device__ __forceinline__ bool trav_step(const ClvDeviceScene& S, const Ray& r,
           float nb[6];
 #pragma unroll
           for (int k = 0; k < 6; ++k) nb[k] = left_next ? lb[k] : rb[k];
-          slab(nb, r.o, R.inv, T.N, T.F);
+          if (S.watertight) slab_wide(nb, R, T.N, T.F);
+          else slab(nb, r.o, R.inv, T.N, T.F);
         }
         T.ref = next;
         return true;

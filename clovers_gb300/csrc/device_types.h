@@ -128,5 +128,7 @@ struct ClvDeviceScene {
   uint32_t compound_level;  // 0 primitives only, 1 wrapper chains, 2 media / lists present
   uint32_t boxes_div_safe;  // every BVH box coordinate is 0 or of magnitude in [2^-70, 2^59]
   uint32_t mis_depth;
+  uint32_t watertight;      // triangles use the watertight test (tri_verts set)
+  const float* tri_verts;   // 12 per triangle: the vertices as given, xyz0 (watertight test only)
   ClvCamera camera;
 };

@@ -623,7 +623,9 @@ class Builder {
     return material(*v);
   }
 
-  Emitted planar(V3 q, V3 u, V3 v, uint32_t mat, bool tri, bool top) {
+  // corners: a triangle's vertices as given (from_coordinates); otherwise q,
+  // q + u, q + v.  They feed only the optional watertight test.
+  Emitted planar(V3 q, V3 u, V3 v, uint32_t mat, bool tri, bool top, const V3* corners = nullptr) {
     // triangle.rs:61-101 / quad.rs:61-83
     const V3 n = cross(u, v);
     const V3 nn = unit(n);
@@ -640,6 +642,13 @@ class Builder {
       e.box.b[4] = std::fmin(std::fmin(c1.z, c2.z), c3.z); e.box.b[5] = std::fmax(std::fmax(c1.z, c2.z), c3.z);
       e.c = q + (u / 4.0f) + (v / 4.0f);
       S.tris.push_back(r);
+      const V3 vs[3] = {corners ? corners[0] : c1, corners ? corners[1] : c2, corners ? corners[2] : c3};
+      for (const V3& p : vs) {
+        S.tri_verts.push_back(p.x);
+        S.tri_verts.push_back(p.y);
+        S.tri_verts.push_back(p.z);
+        S.tri_verts.push_back(0.0f);
+      }
       S.tri_mat.push_back(mat);
       S.tri_gid.push_back(CLV_REF_EMPTY);
       S.tri_area.push_back(length(n) / 2.0f);
@@ -726,7 +735,7 @@ class Builder {
                    R[6] * a.x + R[7] * a.y + R[8] * a.z);
         p[k] = V3(r.x * scale, r.y * scale, r.z * scale) + center;
       }
-      out.push_back(planar(p[0], p[1] - p[0], p[2] - p[0], mat, true, false));
+      out.push_back(planar(p[0], p[1] - p[0], p[2] - p[0], mat, true, false, p));
     }
   }
 
@@ -753,7 +762,7 @@ class Builder {
                    R[6] * a.x + R[7] * a.y + R[8] * a.z);
         p[k] = V3(r.x * scale, r.y * scale, r.z * scale) + center;
       }
-      out.push_back(planar(p[0], p[1] - p[0], p[2] - p[0], mat, true, false));
+      out.push_back(planar(p[0], p[1] - p[0], p[2] - p[0], mat, true, false, p));
     }
   }
 
@@ -1076,7 +1085,8 @@ HostScene mesh_scene(const float* verts, uint32_t nverts, const uint32_t* idx, u
     const V3 a(verts[3 * (size_t)ia], verts[3 * (size_t)ia + 1], verts[3 * (size_t)ia + 2]);
     const V3 b(verts[3 * (size_t)ib], verts[3 * (size_t)ib + 1], verts[3 * (size_t)ib + 2]);
     const V3 c(verts[3 * (size_t)ic], verts[3 * (size_t)ic + 1], verts[3 * (size_t)ic + 2]);
-    tops.push_back(B.planar(a, b - a, c - a, mat, true, true));
+    const V3 corners[3] = {a, b, c};
+    tops.push_back(B.planar(a, b - a, c - a, mat, true, true, corners));
     S.tri_gid.back() = i;
   }
   S.object_count = ntris;

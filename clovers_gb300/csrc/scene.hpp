@@ -19,6 +19,7 @@ struct HostScene {
   std::vector<uint32_t> tri_gid, quad_gid, sphere_gid, obj_gid;
   std::vector<uint32_t> tri_mat, quad_mat, sphere_mat;
   std::vector<float> tri_area, quad_area;
+  std::vector<float> tri_verts;  // 12 per triangle: the three vertices as given (x, y, z, 0)
   std::vector<ClvMaterial> materials;
   std::vector<float> spd;  // 400 floats per table
   std::vector<ClvMisNode> mis_nodes;

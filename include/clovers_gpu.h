@@ -91,6 +91,18 @@ int clv_scene_load_json_text(const char* json, const char* base_dir, uint32_t wi
 int clv_scene_from_mesh(const float* verts, uint32_t nverts, const uint32_t* indices, uint32_t ntris,
                         clv_scene** out);
 
+/* Scene options, set before clv_scene_upload.  No counterpart in the
+ * reference (the benchmark spec's precision item).
+ * CLV_OPT_WATERTIGHT 1: triangles use the watertight test of Woop, Benthin
+ * and Wald 2013 (shear-frame edge functions, double-precision fallback on a
+ * zero edge function) on their vertices as given, so rays through shared
+ * edges and vertices of a closed mesh never slip through.  It also drops the
+ * reference's rejection of rays within 1e-4 of the plane.  Results then
+ * differ from the reference's Triangle::hit on edge and grazing hits; the
+ * default 0 keeps the reference's test and its bit-exact hit ids. */
+#define CLV_OPT_WATERTIGHT 1u
+int clv_scene_set_option(clv_scene* scene, uint32_t option, uint32_t value);
+
 int clv_scene_info_get(const clv_scene* scene, clv_scene_info* out);
 void clv_scene_free(clv_scene* scene);
 

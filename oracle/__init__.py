@@ -54,6 +54,7 @@ def lib():
                 "orc_scene_load_json": (vp, [ctypes.c_char_p, u32, u32]),
                 "orc_scene_from_mesh": (vp, [vp, u32, vp, u32]),
                 "orc_scene_free": (None, [vp]),
+                "orc_scene_set_watertight": (None, [vp, i32]),
                 "orc_scene_object_count": (u64, [vp]),
                 "orc_scene_tree_stats": (None, [vp, vp]),
                 "orc_camera_ray": (None, [vp, f32, f32, f32, f32, vp]),
@@ -177,6 +178,11 @@ class Scene:
                 lib().orc_scene_free(self.h)
         except Exception:
             pass
+
+    def set_watertight(self, on=True):
+        """Watertight triangle test on every triangle (no counterpart in the reference)."""
+        lib().orc_scene_set_watertight(self.h, 1 if on else 0)
+        return self
 
     def object_count(self):
         return lib().orc_scene_object_count(self.h)

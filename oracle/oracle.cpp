@@ -366,7 +366,28 @@ struct AABB {
     return AABB(Interval(a.x, b.x), Interval(a.y, b.y), Interval(a.z, b.z));
   }
   const Interval& axis(int n) const { return n == 0 ? x : (n == 1 ? y : z); }
-  bool hit(const Ray& ray, Float tmin, Float tmax) const {
+  // wide: the exit distance widened toward +inf by 4 gamma_3 (Ize 2013),
+  // the conservative box test of watertight scenes (not the reference's)
+  // and a zero direction component constrains nothing while the origin lies
+  // within that slab (inclusive), missing otherwise
+  static Float widen_exit(Float f) { return std::fmax(f, f + std::fabs(f) * 7.1525574e-7f); }
+  bool hit(const Ray& ray, Float tmin, Float tmax, bool wide = false) const {
+    if (wide) {
+      Float n = -INFINITY, f = INFINITY;
+      for (int a = 0; a < 3; ++a) {
+        const Interval& ax = axis(a);
+        const Float o = ray.origin[a];
+        if (ray.direction[a] == 0.0f) {
+          if (o < ax.min || o > ax.max) return false;
+          continue;
+        }
+        Float adinv = 1.0f / ray.direction[a];
+        Float t0 = (ax.min - o) * adinv, t1 = (ax.max - o) * adinv;
+        n = std::fmax(n, std::fmin(t0, t1));
+        f = std::fmin(f, std::fmax(t0, t1));
+      }
+      return std::fmin(tmax, widen_exit(f)) > std::fmax(tmin, n);
+    }
     for (int a = 0; a < 3; ++a) {
       const Interval& ax = axis(a);
       Float adinv = 1.0f / ray.direction[a];
@@ -394,7 +415,24 @@ struct AABB {
     x = nx; y = ny; z = nz;
   }
   // returns false for None
-  bool distance(const Ray& ray, Float& out) const {
+  bool distance(const Ray& ray, Float& out, bool wide = false) const {
+    if (wide) {
+      Float tmin = -INFINITY, tmax = INFINITY;
+      const Interval* ax[3] = {&x, &y, &z};
+      for (int a = 0; a < 3; ++a) {
+        const Float o = ray.origin[a], d = ray.direction[a];
+        if (d == 0.0f) {
+          if (o < ax[a]->min || o > ax[a]->max) return false;
+          continue;
+        }
+        const Float t1 = (ax[a]->min - o) / d, t2 = (ax[a]->max - o) / d;
+        tmin = std::fmax(tmin, std::fmin(t1, t2));
+        tmax = std::fmin(tmax, std::fmax(t1, t2));
+      }
+      tmax = widen_exit(tmax);
+      if (tmax >= tmin && tmax > 0.0f) { out = tmin; return true; }
+      return false;
+    }
     Float tx1 = (x.min - ray.origin.x) / ray.direction.x;
     Float tx2 = (x.max - ray.origin.x) / ray.direction.x;
     Float tmin = rmin(tx1, tx2), tmax = rmax(tx1, tx2);
@@ -636,6 +674,8 @@ struct Hitable {
   virtual bool is_empty() const { return false; }
   virtual bool is_bvh() const { return false; }
   virtual bool is_list() const { return false; }
+  // the optional watertight triangle test (no counterpart in the reference)
+  virtual void set_watertight(bool) {}
   int gid = -1;  // top-level object index (set on BVH leaves)
 };
 
@@ -759,7 +799,44 @@ struct Planar : Hitable {
   const Material* material;
   AABB box;
   bool triangle;
-  Planar(Vec3 q_, Vec3 u_, Vec3 v_, const Material* m, bool tri) : q(q_), u(u_), v(v_), material(m), triangle(tri) {
+  Vec3 corner[3];           // the vertices as given (watertight test)
+  bool watertight = false;
+  void set_watertight(bool on) override { watertight = on && triangle; }
+  // Woop, Benthin & Wald 2013: edge functions in the ray's shear frame, in
+  // double when one of them is 0; two-sided; t in [dmin, dmax].
+  bool hit_watertight(const Ray& ray, Float dmin, Float dmax, Float& t, Float& alpha, Float& beta) const {
+    const Vec3 dd = ray.direction;
+    const Float ad[3] = {std::fabs(dd.x), std::fabs(dd.y), std::fabs(dd.z)};
+    const int kz = ad[0] > ad[1] ? (ad[0] > ad[2] ? 0 : 2) : (ad[1] > ad[2] ? 1 : 2);
+    int kx = (kz + 1) % 3, ky = (kx + 1) % 3;
+    auto cmp = [](const Vec3& a, int i) { return i == 0 ? a.x : (i == 1 ? a.y : a.z); };
+    if (cmp(dd, kz) < 0.0f) std::swap(kx, ky);
+    const Float sx = cmp(dd, kx) / cmp(dd, kz), sy = cmp(dd, ky) / cmp(dd, kz), sz = 1.0f / cmp(dd, kz);
+    const Vec3 A = corner[0] - ray.origin, B = corner[1] - ray.origin, C = corner[2] - ray.origin;
+    const Float Ax = cmp(A, kx) - sx * cmp(A, kz), Ay = cmp(A, ky) - sy * cmp(A, kz);
+    const Float Bx = cmp(B, kx) - sx * cmp(B, kz), By = cmp(B, ky) - sy * cmp(B, kz);
+    const Float Cx = cmp(C, kx) - sx * cmp(C, kz), Cy = cmp(C, ky) - sy * cmp(C, kz);
+    Float U = Cx * By - Cy * Bx, V = Ax * Cy - Ay * Cx, W = Bx * Ay - By * Ax;
+    if (U == 0.0f || V == 0.0f || W == 0.0f) {
+      U = (Float)((double)Cx * By - (double)Cy * Bx);
+      V = (Float)((double)Ax * Cy - (double)Ay * Cx);
+      W = (Float)((double)Bx * Ay - (double)By * Ax);
+    }
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+    const Float det = U + V + W;
+    if (det == 0.0f) return false;
+    const Float T = U * (sz * cmp(A, kz)) + V * (sz * cmp(B, kz)) + W * (sz * cmp(C, kz));
+    t = T / det;
+    if (!(t >= dmin && t <= dmax)) return false;
+    alpha = V / det;
+    beta = W / det;
+    return true;
+  }
+  Planar(Vec3 q_, Vec3 u_, Vec3 v_, const Material* m, bool tri, const Vec3* corners = nullptr)
+      : q(q_), u(u_), v(v_), material(m), triangle(tri) {
+    corner[0] = corners ? corners[0] : q;
+    corner[1] = corners ? corners[1] : q + u;
+    corner[2] = corners ? corners[2] : q + v;
     Vec3 n = cross(u, v);
     normal = normalize(n);
     d = -(dot(normal, q));
@@ -778,17 +855,24 @@ struct Planar : Hitable {
   }
   bool hit(const Ray& ray, Float dmin, Float dmax, Rng*, HitRecord& out, Counters* c) const override {
     if (c) c->prims++;
-    Float denom = dot(normal, ray.direction);
-    if (std::fabs(denom) < EPSILON_RECT_THICKNESS) return false;
-    Float t = (-d - dot(normal, ray.origin)) / denom;
-    if (t < dmin || t > dmax) return false;
-    Vec3 p = ray.evaluate(t);
-    Vec3 ph = p - q;
-    Float alpha = dot(w, cross(ph, v));
-    Float beta = dot(w, cross(u, ph));
-    bool inside = (alpha >= 0.0f && alpha <= 1.0f) && (beta >= 0.0f && beta <= 1.0f);
-    if (triangle) inside = inside && (alpha + beta <= 1.0f);
-    if (!inside) return false;
+    Float t, alpha, beta;
+    Vec3 p;
+    if (watertight) {
+      if (!hit_watertight(ray, dmin, dmax, t, alpha, beta)) return false;
+      p = ray.evaluate(t);
+    } else {
+      Float denom = dot(normal, ray.direction);
+      if (std::fabs(denom) < EPSILON_RECT_THICKNESS) return false;
+      t = (-d - dot(normal, ray.origin)) / denom;
+      if (t < dmin || t > dmax) return false;
+      p = ray.evaluate(t);
+      Vec3 ph = p - q;
+      alpha = dot(w, cross(ph, v));
+      beta = dot(w, cross(u, ph));
+      bool inside = (alpha >= 0.0f && alpha <= 1.0f) && (beta >= 0.0f && beta <= 1.0f);
+      if (triangle) inside = inside && (alpha + beta <= 1.0f);
+      if (!inside) return false;
+    }
     out.distance = t;
     out.position = p;
     out.u = alpha;
@@ -849,6 +933,9 @@ Vec3 Sphere::random(Vec3 origin, Rng& rng) const {
 
 struct Boxy : Hitable {  // clovers/src/objects/boxy.rs
   std::vector<HPtr> sides;
+  void set_watertight(bool on) override {
+    for (auto& h : sides) h->set_watertight(on);
+  }
   AABB box;
   Boxy(Vec3 c0, Vec3 c1, const Material* m) {
     Vec3 mn(rmin(c0.x, c1.x), rmin(c0.y, c1.y), rmin(c0.z, c1.z));
@@ -887,6 +974,9 @@ struct Boxy : Hitable {  // clovers/src/objects/boxy.rs
 
 struct HitableList : Hitable {  // clovers/src/hitable.rs:123-195
   std::vector<HPtr> items;
+  void set_watertight(bool on) override {
+    for (auto& h : items) h->set_watertight(on);
+  }
   AABB box;
   bool hit(const Ray& ray, Float dmin, Float dmax, Rng* rng, HitRecord& out, Counters* c) const override {
     Float distance = INFINITY;
@@ -911,6 +1001,7 @@ struct HitableList : Hitable {  // clovers/src/hitable.rs:123-195
 
 struct RotateY : Hitable {  // clovers/src/objects/rotate.rs
   HPtr object;
+  void set_watertight(bool on) override { object->set_watertight(on); }
   Float sin_t, cos_t;
   bool has_box = false;
   AABB box;
@@ -967,6 +1058,7 @@ struct RotateY : Hitable {  // clovers/src/objects/rotate.rs
 
 struct Translate : Hitable {  // clovers/src/objects/translate.rs
   HPtr object;
+  void set_watertight(bool on) override { object->set_watertight(on); }
   Vec3 offset;
   AABB box;
   Translate(HPtr obj, Vec3 off) : object(std::move(obj)), offset(off) {
@@ -993,6 +1085,7 @@ struct Translate : Hitable {  // clovers/src/objects/translate.rs
 
 struct ConstantMedium : Hitable {  // clovers/src/objects/constant_medium.rs
   HPtr boundary;
+  void set_watertight(bool on) override { boundary->set_watertight(on); }
   Material phase;  // Isotropic(texture)
   Float neg_inv_density;
   ConstantMedium(HPtr b, Float density, const Texture& tex) : boundary(std::move(b)) {
@@ -1033,17 +1126,23 @@ struct ConstantMedium : Hitable {  // clovers/src/objects/constant_medium.rs
 // ------------------------------------------------------------------- bvh --
 struct BVHNode : Hitable {  // clovers/src/bvh.rs:21-28, bvh/hitable_trait.rs
   HPtr left, right;
+  bool wide = false;  // conservative box tests of watertight scenes
+  void set_watertight(bool on) override {
+    wide = on;
+    left->set_watertight(on);
+    right->set_watertight(on);
+  }
   AABB box;
   bool hit(const Ray& ray, Float dmin, Float dmax, Rng* rng, HitRecord& out, Counters* c) const override {
     if (c) c->nodes++;
-    if (!box.hit(ray, dmin, dmax)) return false;
+    if (!box.hit(ray, dmin, dmax, wide)) return false;
     const AABB* la = left->aabb();
     const AABB* ra = right->aabb();
     if (!la && !ra) return false;
     if (la && !ra) return left->hit(ray, dmin, dmax, rng, out, c);
     if (!la && ra) return right->hit(ray, dmin, dmax, rng, out, c);
     Float ld = 0, rd = 0;
-    bool lh = la->distance(ray, ld), rh = ra->distance(ray, rd);
+    bool lh = la->distance(ray, ld, wide), rh = ra->distance(ray, rd, wide);
     if (!lh && !rh) return false;
     if (lh && !rh) return left->hit(ray, dmin, dmax, rng, out, c);
     if (!lh && rh) return right->hit(ray, dmin, dmax, rng, out, c);
@@ -1418,7 +1517,7 @@ struct Loader {
                R[6] * a.x + R[7] * a.y + R[8] * a.z);
         p[k] = r * scale + center;
       }
-      out.emplace_back(new Planar(p[0], p[1] - p[0], p[2] - p[0], mat, true));
+      out.emplace_back(new Planar(p[0], p[1] - p[0], p[2] - p[0], mat, true, p));
     }
   }
 
@@ -1535,7 +1634,7 @@ struct Loader {
                R[6] * a.x + R[7] * a.y + R[8] * a.z);
         p[k] = r * scale + center;
       }
-      out.emplace_back(new Planar(p[0], p[1] - p[0], p[2] - p[0], mat, true));
+      out.emplace_back(new Planar(p[0], p[1] - p[0], p[2] - p[0], mat, true, p));
     }
   }
 
@@ -1650,7 +1749,8 @@ static Scene* mesh_scene(const float* verts, uint32_t nverts, const uint32_t* id
     Vec3 a(verts[3 * ia], verts[3 * ia + 1], verts[3 * ia + 2]);
     Vec3 b(verts[3 * ib], verts[3 * ib + 1], verts[3 * ib + 2]);
     Vec3 c(verts[3 * ic], verts[3 * ic + 1], verts[3 * ic + 2]);
-    hs.emplace_back(new Planar(a, b - a, c - a, m, true));  // Triangle::from_coordinates
+    const Vec3 corners[3] = {a, b, c};
+    hs.emplace_back(new Planar(a, b - a, c - a, m, true, corners));  // Triangle::from_coordinates
     hs.back()->gid = (int)i;
   }
   sc->object_count = ntris;
@@ -1900,6 +2000,12 @@ void* orc_scene_from_mesh(const float* verts, uint32_t nverts, const uint32_t* i
   }
 }
 void orc_scene_free(void* s) { delete static_cast<Scene*>(s); }
+// the optional watertight triangle test on every triangle of the scene
+void orc_scene_set_watertight(void* s, int on) {
+  Scene* sc = static_cast<Scene*>(s);
+  if (sc->bvh_root) sc->bvh_root->set_watertight(on != 0);
+  if (sc->mis_root) sc->mis_root->set_watertight(on != 0);
+}
 
 static void tree_stats(const Hitable* h, uint32_t depth, uint64_t& nodes, uint32_t& max_depth) {
   if (!h->is_bvh()) return;
