@@ -108,7 +108,7 @@ __global__ void ray_scatter(const uint32_t* __restrict__ key, uint64_t n, uint32
 #ifndef CLV_MINB_RAY
 #define CLV_MINB_RAY 9  // 56 registers, no spills: 36 warps per SM (measured best of 6..16)
 #endif
-template <int CPLX, bool COUNT>
+template <int CPLX, bool COUNT, int WT>
 __global__ void __launch_bounds__(128, CLV_MINB_RAY) raycast_persist_kernel(
     ClvDeviceScene S, const float4* __restrict__ rays, uint64_t n, uint32_t* __restrict__ prim,
     float* __restrict__ tout, uint32_t* __restrict__ nodes, uint32_t* __restrict__ tests, uint32_t* err,
@@ -138,11 +138,11 @@ __global__ void __launch_bounds__(128, CLV_MINB_RAY) raycast_persist_kernel(
         r = Ray{mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), 0.0f, 600};
         c = Counters{0u, 0u};
         rng.init(0, (uint32_t)i, 0);
-        trav_begin(S, r, a.w, b.w, T, h);
+        trav_begin<WT>(S, r, a.w, b.w, T, h);
         have = true;
       }
     }
-    if (have && !trav_step<CPLX>(S, r, T, stack, &rng, h, nullptr, COUNT ? &c : nullptr, err)) {
+    if (have && !trav_step<CPLX, WT>(S, r, T, stack, &rng, h, nullptr, COUNT ? &c : nullptr, err)) {
       __stcs(prim + i, T.found ? hit_gid(S, h.ref) : 0xFFFFFFFFu);
       __stcs(tout + i, T.found ? h.t : 0.0f);
       if (COUNT) {
@@ -974,14 +974,24 @@ int clv_raycast_device(const clv_device_scene* d, const float* rays_dev, uint64_
     g_launches += 3;
     perm = order;
   }
-  switch (d->view.compound_level * 2 + (count ? 1 : 0)) {
-    case 0: raycast_persist_kernel<0, false><<<grid, block, 0, st>>>(d->view, r4, n, prim_dev, t_dev, nodes_dev, tests_dev, d->err, nx, perm); break;
-    case 1: raycast_persist_kernel<0, true><<<grid, block, 0, st>>>(d->view, r4, n, prim_dev, t_dev, nodes_dev, tests_dev, d->err, nx, perm); break;
-    case 2: raycast_persist_kernel<1, false><<<grid, block, 0, st>>>(d->view, r4, n, prim_dev, t_dev, nodes_dev, tests_dev, d->err, nx, perm); break;
-    case 3: raycast_persist_kernel<1, true><<<grid, block, 0, st>>>(d->view, r4, n, prim_dev, t_dev, nodes_dev, tests_dev, d->err, nx, perm); break;
-    case 4: raycast_persist_kernel<2, false><<<grid, block, 0, st>>>(d->view, r4, n, prim_dev, t_dev, nodes_dev, tests_dev, d->err, nx, perm); break;
-    default: raycast_persist_kernel<2, true><<<grid, block, 0, st>>>(d->view, r4, n, prim_dev, t_dev, nodes_dev, tests_dev, d->err, nx, perm);
+#define CLV_RAYCAST(C, N, W) \
+  raycast_persist_kernel<C, N, W><<<grid, block, 0, st>>>(d->view, r4, n, prim_dev, t_dev, nodes_dev, tests_dev, d->err, nx, perm)
+  const int wt = d->view.watertight ? 1 : 0;
+  switch ((d->view.compound_level * 2 + (count ? 1 : 0)) * 2 + wt) {
+    case 0: CLV_RAYCAST(0, false, CLV_WT_OFF); break;
+    case 1: CLV_RAYCAST(0, false, CLV_WT_ON); break;
+    case 2: CLV_RAYCAST(0, true, CLV_WT_OFF); break;
+    case 3: CLV_RAYCAST(0, true, CLV_WT_ON); break;
+    case 4: CLV_RAYCAST(1, false, CLV_WT_OFF); break;
+    case 5: CLV_RAYCAST(1, false, CLV_WT_ON); break;
+    case 6: CLV_RAYCAST(1, true, CLV_WT_OFF); break;
+    case 7: CLV_RAYCAST(1, true, CLV_WT_ON); break;
+    case 8: CLV_RAYCAST(2, false, CLV_WT_OFF); break;
+    case 9: CLV_RAYCAST(2, false, CLV_WT_ON); break;
+    case 10: CLV_RAYCAST(2, true, CLV_WT_OFF); break;
+    default: CLV_RAYCAST(2, true, CLV_WT_ON); break;
   }
+#undef CLV_RAYCAST
   e = cudaGetLastError();
   if (e != cudaSuccess) return fail(CLV_E_CUDA, std::string("raycast launch: ") + cudaGetErrorString(e));
   return CLV_OK;
@@ -1088,14 +1098,23 @@ static int render_wavefront(clv_device_scene* d, const clv_render_opts* o, doubl
     auto bounce = [&](cudaStream_t s, int k) {
       cudaMemsetAsync(&d->wf_counters->live, 0, 5 * sizeof(unsigned int), s);  // live + 4 queue lengths
       if (prof) cudaEventRecord(evs[4 * k], s);
-      switch (level * 2 + (prof ? 1 : 0)) {
-        case 0: wf_intersect<0, false, false><<<grid, block, 0, s>>>(d->view, W, C, d->err, nullptr, WfBatch{}); break;
-        case 1: wf_intersect<0, true, false><<<grid, block, 0, s>>>(d->view, W, C, d->err, dcnt, WfBatch{}); break;
-        case 2: wf_intersect<1, false, false><<<grid, block, 0, s>>>(d->view, W, C, d->err, nullptr, WfBatch{}); break;
-        case 3: wf_intersect<1, true, false><<<grid, block, 0, s>>>(d->view, W, C, d->err, dcnt, WfBatch{}); break;
-        case 4: wf_intersect<2, false, false><<<grid, block, 0, s>>>(d->view, W, C, d->err, nullptr, WfBatch{}); break;
-        default: wf_intersect<2, true, false><<<grid, block, 0, s>>>(d->view, W, C, d->err, dcnt, WfBatch{}); break;
+#define CLV_ISECT(L, N, T) \
+  wf_intersect<L, N, false, T><<<grid, block, 0, s>>>(d->view, W, C, d->err, N ? dcnt : nullptr, WfBatch{})
+      switch ((level * 2 + (prof ? 1 : 0)) * 2 + (d->view.watertight ? 1 : 0)) {
+        case 0: CLV_ISECT(0, false, CLV_WT_OFF); break;
+        case 1: CLV_ISECT(0, false, CLV_WT_ON); break;
+        case 2: CLV_ISECT(0, true, CLV_WT_OFF); break;
+        case 3: CLV_ISECT(0, true, CLV_WT_ON); break;
+        case 4: CLV_ISECT(1, false, CLV_WT_OFF); break;
+        case 5: CLV_ISECT(1, false, CLV_WT_ON); break;
+        case 6: CLV_ISECT(1, true, CLV_WT_OFF); break;
+        case 7: CLV_ISECT(1, true, CLV_WT_ON); break;
+        case 8: CLV_ISECT(2, false, CLV_WT_OFF); break;
+        case 9: CLV_ISECT(2, false, CLV_WT_ON); break;
+        case 10: CLV_ISECT(2, true, CLV_WT_OFF); break;
+        default: CLV_ISECT(2, true, CLV_WT_ON); break;
       }
+#undef CLV_ISECT
       if (prof) cudaEventRecord(evs[4 * k + 1], s);
       if (prof) cudaEventRecord(evs[4 * k + 2], s);
       wf_shade_specular<false><<<qgrid, block, 0, s>>>(d->view, P, W, C, d->err, WfBatch{});
@@ -1235,9 +1254,9 @@ int clv_render_batch(clv_device_scene* const* ds, const clv_render_opts* opts, d
       for (int k = 0; k < batch; ++k) {
         cudaMemsetAsync(&C->live, 0, 5 * sizeof(unsigned int), s);
         switch (level) {
-          case 0: wf_intersect<0, false, true><<<grid, block, 0, s>>>(S0, W, C, d0->err, nullptr, B); break;
-          case 1: wf_intersect<1, false, true><<<grid, block, 0, s>>>(S0, W, C, d0->err, nullptr, B); break;
-          default: wf_intersect<2, false, true><<<grid, block, 0, s>>>(S0, W, C, d0->err, nullptr, B); break;
+          case 0: wf_intersect<0, false, true, CLV_WT_SCENE><<<grid, block, 0, s>>>(S0, W, C, d0->err, nullptr, B); break;
+          case 1: wf_intersect<1, false, true, CLV_WT_SCENE><<<grid, block, 0, s>>>(S0, W, C, d0->err, nullptr, B); break;
+          default: wf_intersect<2, false, true, CLV_WT_SCENE><<<grid, block, 0, s>>>(S0, W, C, d0->err, nullptr, B); break;
         }
         wf_shade_specular<true><<<qgrid, block, 0, s>>>(S0, P0, W, C, d0->err, B);
         wf_shade_diffuse<true><<<qgrid, block, 0, s>>>(S0, P0, W, C, d0->err, B);
@@ -1509,10 +1528,13 @@ extern "C" int clv_render_device_noalloc(clv_device_scene* d, const clv_render_o
   for (uint64_t it = 0;; it += batch) {
     for (int k = 0; k < batch; ++k) {
       cudaMemsetAsync(&C->live, 0, 5 * sizeof(unsigned int), st);
-      switch (level) {
-        case 0: wf_intersect<0, false, false><<<grid, block, 0, st>>>(d->view, W, C, d->err, nullptr, WfBatch{}); break;
-        case 1: wf_intersect<1, false, false><<<grid, block, 0, st>>>(d->view, W, C, d->err, nullptr, WfBatch{}); break;
-        default: wf_intersect<2, false, false><<<grid, block, 0, st>>>(d->view, W, C, d->err, nullptr, WfBatch{}); break;
+      switch (level * 2 + (d->view.watertight ? 1 : 0)) {
+        case 0: wf_intersect<0, false, false, CLV_WT_OFF><<<grid, block, 0, st>>>(d->view, W, C, d->err, nullptr, WfBatch{}); break;
+        case 1: wf_intersect<0, false, false, CLV_WT_ON><<<grid, block, 0, st>>>(d->view, W, C, d->err, nullptr, WfBatch{}); break;
+        case 2: wf_intersect<1, false, false, CLV_WT_OFF><<<grid, block, 0, st>>>(d->view, W, C, d->err, nullptr, WfBatch{}); break;
+        case 3: wf_intersect<1, false, false, CLV_WT_ON><<<grid, block, 0, st>>>(d->view, W, C, d->err, nullptr, WfBatch{}); break;
+        case 4: wf_intersect<2, false, false, CLV_WT_OFF><<<grid, block, 0, st>>>(d->view, W, C, d->err, nullptr, WfBatch{}); break;
+        default: wf_intersect<2, false, false, CLV_WT_ON><<<grid, block, 0, st>>>(d->view, W, C, d->err, nullptr, WfBatch{}); break;
       }
       wf_shade_specular<false><<<qgrid, block, 0, st>>>(d->view, P, W, C, d->err, WfBatch{});
       wf_shade_diffuse<false><<<qgrid, block, 0, st>>>(d->view, P, W, C, d->err, WfBatch{});

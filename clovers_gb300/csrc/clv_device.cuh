@@ -215,12 +215,23 @@ __device__ __forceinline__ bool tri_watertight(const float4* vtx, const Ray& r, 
   beta = W2 / det;
   return true;
 }
+// Watertight mode of a traversal: CLV_WT_OFF / CLV_WT_ON fixed at compile
+// time (the ray-cast and single-scene intersect kernels), CLV_WT_SCENE read
+// from the scene (batches, the megakernel, the object interpreter, MIS pdfs).
+#define CLV_WT_OFF 0
+#define CLV_WT_ON 1
+#define CLV_WT_SCENE 2
+template <int WT>
+__device__ __forceinline__ bool wt_on(const ClvDeviceScene& S) {
+  return WT == CLV_WT_SCENE ? S.watertight != 0 : WT == CLV_WT_ON;
+}
 // A triangle or quad of the scene: its plane record in f and the hit test of
 // the scene's triangle mode.
+template <int WT = CLV_WT_SCENE>
 __device__ __forceinline__ bool planar_hit(const ClvDeviceScene& S, bool tri, uint32_t idx, float f[16], const Ray& r,
                                            float tmin, float tmax, float& t, float& alpha, float& beta) {
   load_planar(tri ? S.tris : S.quads, idx, f);
-  if (tri && S.watertight)
+  if (tri && wt_on<WT>(S))
     return tri_watertight(reinterpret_cast<const float4*>(S.tri_verts) + 3 * (size_t)idx, r, tmin, tmax, t, alpha, beta);
   return planar_test(f, tri, r, tmin, tmax, t, alpha, beta);
 }
@@ -432,6 +443,7 @@ __device__ __forceinline__ V chain_dir(const ClvDeviceScene& S, uint32_t ref, V 
   }
   return d;
 }
+template <int WT = CLV_WT_SCENE>
 __device__ __forceinline__ int chain_hit(const ClvDeviceScene& S, uint32_t top, const Ray& r0, float tmin, float tmax,
                                          Rec& rec, Counters* cnt) {
   int n = 0;
@@ -492,7 +504,7 @@ __device__ __forceinline__ int chain_hit(const ClvDeviceScene& S, uint32_t top, 
   } else if (kind == CLV_REF_TRI || kind == CLV_REF_QUAD) {
     if (cnt) cnt->prims++;
     float f[16], t, a, b;
-    if (planar_hit(S, kind == CLV_REF_TRI, idx, f, r, tmin, tmax, t, a, b)) {
+    if (planar_hit<WT>(S, kind == CLV_REF_TRI, idx, f, r, tmin, tmax, t, a, b)) {
       planar_record(f, r, t, a, b, rec);
       rec.mat = kind == CLV_REF_TRI ? S.tri_mat[idx] : S.quad_mat[idx];
       any = true;
@@ -699,14 +711,14 @@ __device__ __forceinline__ bool box_distance_pre(const float* b, const RayPre& R
 
 // Tests one BVH leaf with the current tmax.  CPLX: 0 primitives only,
 // 1 + wrapper chains (inline), 2 + media and lists (out-of-line interpreter).
-template <int CPLX>
+template <int CPLX, int WT>
 __device__ __forceinline__ bool leaf_test(const ClvDeviceScene& S, uint32_t ref, const Ray& r, float tmin,
                                           float tmax, Rng* rng, Hit& hit, Rec* full, Counters* cnt, uint32_t* err) {
   const uint32_t kind = CLV_REF_KIND(ref), idx = CLV_REF_INDEX(ref);
   if (kind == CLV_REF_TRI || kind == CLV_REF_QUAD) {
     if (cnt) cnt->prims++;
     float f[16], t, a, b;
-    if (!planar_hit(S, kind == CLV_REF_TRI, idx, f, r, tmin, tmax, t, a, b)) return false;
+    if (!planar_hit<WT>(S, kind == CLV_REF_TRI, idx, f, r, tmin, tmax, t, a, b)) return false;
     hit.t = t;
     hit.ref = ref;
     hit.a = a;
@@ -723,7 +735,7 @@ __device__ __forceinline__ bool leaf_test(const ClvDeviceScene& S, uint32_t ref,
   }
   if (CPLX == 1) {
     Rec rec;
-    const int c = chain_hit(S, ref, r, tmin, tmax, rec, cnt);
+    const int c = chain_hit<WT>(S, ref, r, tmin, tmax, rec, cnt);
     if (c == 2 && err) atomicOr(err, CLV_ERR_NEST);  // host routes such scenes to CPLX 2
     if (c != 1) return false;
     hit.t = rec.t;
@@ -761,6 +773,7 @@ struct Trav {
   float N, F;
   bool found;
 };
+template <int WT>
 __device__ __forceinline__ void trav_begin(const ClvDeviceScene& S, const Ray& r, float tmin, float tmax, Trav& T,
                                            Hit& hit) {
   hit.ref = CLV_REF_EMPTY;
@@ -775,14 +788,14 @@ __device__ __forceinline__ void trav_begin(const ClvDeviceScene& S, const Ray& r
   T.sp = 0;
   T.marked = 0;
   T.ref = S.root;
-  if (S.watertight) slab_wide(S.root_box, T.R, T.N, T.F);
+  if (wt_on<WT>(S)) slab_wide(S.root_box, T.R, T.N, T.F);
   else slab(S.root_box, r.o, T.R.inv, T.N, T.F);
   T.found = false;
 }
 // One node visit or leaf test, then the next reference (descend, or pop the
 // next deferred far child whose visit the reference would make).  Returns
 // false when the traversal is over (result in hit / T.found).
-template <int CPLX>
+template <int CPLX, int WT>
 __device__ __forceinline__ bool trav_step(const ClvDeviceScene& S, const Ray& r, Trav& T, float4* stack, Rng* rng,
                                           Hit& hit, Rec* full, Counters* cnt, uint32_t* err) {
   const RayPre& R = T.R;
@@ -799,7 +812,7 @@ __device__ __forceinline__ bool trav_step(const ClvDeviceScene& S, const Ray& r,
       bool left_next = true;
       if (L != CLV_REF_EMPTY && Rr != CLV_REF_EMPTY) {
         float ld, rd;
-        const bool wide = S.watertight != 0;
+        const bool wide = wt_on<WT>(S);
         const bool lh = wide ? box_distance_wide(lb, R, ld) : box_distance_pre(lb, R, ld);
         const bool rh = wide ? box_distance_wide(rb, R, rd) : box_distance_pre(rb, R, rd);
         if (lh && rh) {
@@ -836,7 +849,7 @@ __device__ __forceinline__ bool trav_step(const ClvDeviceScene& S, const Ray& r,
           float nb[6];
 #pragma unroll
           for (int k = 0; k < 6; ++k) nb[k] = left_next ? lb[k] : rb[k];
-          if (S.watertight) slab_wide(nb, R, T.N, T.F);
+          if (wt_on<WT>(S)) slab_wide(nb, R, T.N, T.F);
           else slab(nb, r.o, R.inv, T.N, T.F);
         }
         T.ref = next;
@@ -844,7 +857,7 @@ __device__ __forceinline__ bool trav_step(const ClvDeviceScene& S, const Ray& r,
       }
     }
   } else {
-    if (leaf_test<CPLX>(S, ref, r, T.tmin, T.tmax, rng, hit, full, cnt, err)) {
+    if (leaf_test<CPLX, WT>(S, ref, r, T.tmin, T.tmax, rng, hit, full, cnt, err)) {
       T.tmax = hit.t;
       T.found = true;
       T.marked = T.sp;
@@ -864,13 +877,13 @@ __device__ __forceinline__ bool trav_step(const ClvDeviceScene& S, const Ray& r,
   }
   return false;
 }
-template <int CPLX>
+template <int CPLX, int WT = CLV_WT_SCENE>
 __device__ bool closest_hit(const ClvDeviceScene& S, const Ray& r, float tmin, float tmax, Rng* rng, Hit& hit,
                             Rec* full, Counters* cnt, uint32_t* err) {
   Trav T;
   float4 stack[CLV_STACK];
-  trav_begin(S, r, tmin, tmax, T, hit);
-  while (trav_step<CPLX>(S, r, T, stack, rng, hit, full, cnt, err)) {
+  trav_begin<WT>(S, r, tmin, tmax, T, hit);
+  while (trav_step<CPLX, WT>(S, r, T, stack, rng, hit, full, cnt, err)) {
   }
   return T.found;
 }

@@ -171,7 +171,7 @@ __device__ __forceinline__ int material_class(const ClvDeviceScene& S, uint32_t 
   return WF_Q_SPEC;
 }
 
-template <int CPLX, bool COUNT>
+template <int CPLX, bool COUNT, int WT>
 __device__ __forceinline__ void intersect_slot(const ClvDeviceScene& S, const WfState& W, WfCounters* C, uint32_t* err,
                                                uint32_t i, const uint4& m, Counters& c) {
   const float4 a = W.o_time[i], b = W.d_lambda[i];
@@ -184,7 +184,7 @@ __device__ __forceinline__ void intersect_slot(const ClvDeviceScene& S, const Wf
     rng.key = (uint64_t)k.x | ((uint64_t)k.y << 32);
     rng.counter = m.z;
   }
-  const bool any = closest_hit<CPLX>(S, r, CLV_EPS_ACNE, CLV_FLT_MAX, CPLX == 2 ? &rng : nullptr, h,
+  const bool any = closest_hit<CPLX, WT>(S, r, CLV_EPS_ACNE, CLV_FLT_MAX, CPLX == 2 ? &rng : nullptr, h,
                                      CPLX ? &full : nullptr, COUNT ? &c : nullptr, err);
   if (CPLX == 2 && rng.counter != m.z) W.meta[i].z = rng.counter;
   int cls = WF_Q_FINISH;
@@ -206,7 +206,8 @@ __device__ __forceinline__ void intersect_slot(const ClvDeviceScene& S, const Wf
   wf_enqueue(W, C, cls, i);
 }
 
-template <int CPLX, bool COUNT, bool BATCH>
+// WT: CLV_WT_OFF / CLV_WT_ON for one scene, CLV_WT_SCENE for batches
+template <int CPLX, bool COUNT, bool BATCH, int WT>
 __global__ void __launch_bounds__(128, CLV_MINB) wf_intersect(ClvDeviceScene S, WfState W, WfCounters* C, uint32_t* err,
                                                               unsigned long long* cnt, WfBatch B) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -216,8 +217,8 @@ __global__ void __launch_bounds__(128, CLV_MINB) wf_intersect(ClvDeviceScene S, 
     const uint4 m = W.meta[i];
     if (m.w & 1u) {
       live = 1;
-      if constexpr (BATCH) intersect_slot<CPLX, COUNT>(B.scenes[m.w >> 8], W, C, err, i, m, c);
-      else intersect_slot<CPLX, COUNT>(S, W, C, err, i, m, c);
+      if constexpr (BATCH) intersect_slot<CPLX, COUNT, WT>(B.scenes[m.w >> 8], W, C, err, i, m, c);
+      else intersect_slot<CPLX, COUNT, WT>(S, W, C, err, i, m, c);
     }
   }
   if (COUNT) warp_add_counts(cnt, live, c.nodes, c.prims);
