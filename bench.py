@@ -472,6 +472,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline legs")
     ap.add_argument("--guided", action="store_true", help="with --config: also the guided time to relMSE 1e-3")
     ap.add_argument("--no-guided", action="store_true", help="skip the guided-vs-plain section of the default run")
+    ap.add_argument("--autotune", action="store_true", help="tune the wavefront shape before the timed render")
     ap.add_argument("--guided-only", action="store_true",
                     help="with --config --guided: only the guided passes (short case for profiling)")
     ap.add_argument("--guide-alpha", type=float, default=0.5)
@@ -525,6 +526,14 @@ def main():
             o.sample_offset = (rank * 1000003 + step) * SPP  # weak scaling: every rank renders its own samples
             return o
 
+        tune = None
+        if args.autotune:  # one-time shape search on a short render of the same scene, before the timed region
+            t0 = time.perf_counter()
+            res = dscene.autotune(cg.RenderOptions(width=W_IMG, height=H_IMG, samples=max(1, SPP // 16),
+                                                   max_depth=DEPTH, seed=SEED + 7), stream=sp)
+            best = min(res, key=lambda r: r[2])
+            tune = {"path_slots": best[0], "shade_blocks_per_sm": best[1], "candidates": len(res),
+                    "tuning_s": round(time.perf_counter() - t0, 3)}
         for w in range(args.warmup):
             film.zero_()
             _lib.check(L.clv_render_device(dscene.handle, ctypes.byref(opts_for(10**6 + w)), film.data_ptr(), sp))
@@ -607,7 +616,8 @@ def main():
             "data": "synthetic (seeded enclosed-box scene in the reference's scene format)",
             "config": {"workload": "enclosed box %dx%d, %d spp, depth %d (wavefront engine)" % (W_IMG, H_IMG, SPP, DEPTH),
                        "samples_per_step": samples_step, "l2": "flushed between steps (256 MiB write)",
-                       "parallelism": "replicas" if world > 1 else "single GPU", "wall_s_timed_loop": round(wall, 3)},
+                       "parallelism": "replicas" if world > 1 else "single GPU", "wall_s_timed_loop": round(wall, 3),
+                       "autotune": tune},
             "e2e": {"value": round(e2e_value, 3), "unit": "Msamples/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(npix * 3 * 4)},
             "gpu_launches": int(launches),

@@ -40,6 +40,10 @@ class GuideOptsC(ctypes.Structure):
     _fields_ = [("record_capacity", c_u32), ("learning_rate", c_f32), ("seed", c_u64)]
 
 
+class TuneResultC(ctypes.Structure):
+    _fields_ = [("path_slots", c_u32), ("shade_blocks_per_sm", c_u32), ("ms", c_f32)]
+
+
 class RenderProfileC(ctypes.Structure):
     _fields_ = [("ms_init", c_f64), ("ms_intersect", c_f64), ("ms_shade", c_f64), ("intersect_launches", c_u64),
                 ("shade_launches", c_u64), ("paths", c_u64), ("path_segments", c_u64), ("node_visits", c_u64),
@@ -61,6 +65,7 @@ SIGNATURES = {
     "clv_render_device": (c_i32, [ctypes.c_void_p, P(RenderOptsC), ctypes.c_void_p, ctypes.c_void_p]),
     "clv_render_batch": (c_i32, [ctypes.c_void_p, P(RenderOptsC), ctypes.c_void_p, c_u32, ctypes.c_void_p]),
     "clv_render_device_noalloc": (c_i32, [ctypes.c_void_p, P(RenderOptsC), ctypes.c_void_p, ctypes.c_void_p]),
+    "clv_autotune": (c_i32, [ctypes.c_void_p, P(RenderOptsC), ctypes.c_void_p, c_u32, P(c_u32), ctypes.c_void_p]),
     "clv_resolve_device": (c_i32, [ctypes.c_void_p, c_u32, c_u32, c_u32, ctypes.c_void_p, ctypes.c_void_p,
                                    ctypes.c_void_p]),
     "clv_resolve_srgb": (c_i32, [ctypes.c_void_p, c_u32, c_u32, ctypes.c_void_p]),

@@ -568,6 +568,9 @@ struct clv_device_scene {
   WfCounters* wf_counters = nullptr;
   unsigned int* wf_live_host = nullptr;  // pinned
   cudaStream_t cap_stream = nullptr;     // private stream for graph capture
+  // wavefront shape chosen by clv_autotune (0: the built-in defaults)
+  uint32_t tuned_slots = 0;      // paths in flight
+  uint32_t tuned_shade = 0;      // shading-kernel blocks per SM
   unsigned long long* ray_next = nullptr;  // work counter of the persistent ray casts
   uint32_t* ray_sort = nullptr;            // ray order: histogram, keys, permutation
   uint64_t ray_sort_cap = 0;               // rays the sort scratch holds
@@ -763,6 +766,76 @@ int clv_render_profile_run(clv_device_scene* d, const clv_render_opts* o, double
   if (o->mode != CLV_MODE_PATH_TRACING || o->engine != 0)
     return fail(CLV_E_INVALID, "profiling covers the wavefront path tracer only");
   return render_wavefront(d, o, film_dev, (cudaStream_t)stream, out);
+}
+
+// Times the wavefront render `o` (a short one: a few samples per pixel) for
+// every candidate shape -- paths in flight SMs x {1, 2, 4, 8, 16} x 1024 and
+// shading grids of {8, 16, 32} blocks per SM, the minimum of two runs each --
+// and keeps the fastest in the scene for later renders that leave path_slots
+// at 0 (clv_render, clv_render_device, clv_render_guided, clv_render_batch
+// with this scene first).
+int clv_autotune(clv_device_scene* d, const clv_render_opts* o, clv_tune_result* results, uint32_t max_results,
+                 uint32_t* n_results, void* stream) {
+  int rc = check_opts(d, o);
+  if (rc) return rc;
+  if (o->mode != CLV_MODE_PATH_TRACING || o->engine != 0)
+    return fail(CLV_E_INVALID, "tuning covers the wavefront path tracer only");
+  cudaStream_t st = (cudaStream_t)stream;
+  double* film = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  const uint32_t old_slots = d->tuned_slots, old_shade = d->tuned_shade;
+  auto cleanup = [&]() {
+    if (film) cudaFree(film);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+  };
+  try {
+    const size_t fb = (size_t)o->width * o->height * 3 * sizeof(double);
+    ck(cudaMalloc(&film, fb), "cudaMalloc tuning film");
+    ck(cudaEventCreate(&e0), "cudaEventCreate");
+    ck(cudaEventCreate(&e1), "cudaEventCreate");
+    const uint32_t sms = (uint32_t)sm_count();
+    const uint32_t slot_mult[5] = {1, 2, 4, 8, 16};
+    const uint32_t shade[3] = {8, 16, 32};
+    clv_render_opts t = *o;
+    t.path_slots = 0;
+    float best = 3.0e38f;
+    uint32_t best_slots = 0, best_shade = 0, n = 0;
+    for (uint32_t a = 0; a < 5; ++a)
+      for (uint32_t b = 0; b < 3; ++b) {
+        d->tuned_slots = sms * slot_mult[a] * 1024u;
+        d->tuned_shade = shade[b];
+        float ms = 3.0e38f;
+        for (int rep = 0; rep < 2; ++rep) {
+          ck(cudaMemsetAsync(film, 0, fb, st), "cudaMemsetAsync");
+          ck(cudaEventRecord(e0, st), "cudaEventRecord");
+          rc = render_wavefront(d, &t, film, st, nullptr);
+          if (rc) throw std::runtime_error(g_error);
+          ck(cudaEventRecord(e1, st), "cudaEventRecord");
+          ck(cudaEventSynchronize(e1), "cudaEventSynchronize");
+          float m = 0.0f;
+          ck(cudaEventElapsedTime(&m, e0, e1), "cudaEventElapsedTime");
+          ms = std::min(ms, m);
+        }
+        if (results && n < max_results) results[n] = clv_tune_result{d->tuned_slots, d->tuned_shade, ms};
+        ++n;
+        if (ms < best) {
+          best = ms;
+          best_slots = d->tuned_slots;
+          best_shade = d->tuned_shade;
+        }
+      }
+    d->tuned_slots = best_slots;
+    d->tuned_shade = best_shade;
+    if (n_results) *n_results = n;
+    cleanup();
+    return CLV_OK;
+  } catch (std::exception& ex) {
+    d->tuned_slots = old_slots;
+    d->tuned_shade = old_shade;
+    cleanup();
+    return fail(CLV_E_CUDA, ex.what());
+  }
 }
 
 int clv_selftest_division(uint64_t n, uint64_t seed, uint64_t* mismatches) {
@@ -1052,7 +1125,7 @@ static int render_wavefront(clv_device_scene* d, const clv_render_opts* o, doubl
     P.npix = (uint64_t)o->width * o->height;
     P.total = P.npix * o->samples;
     P.seed = o->seed;
-    uint64_t q = o->path_slots ? o->path_slots : (uint64_t)sm_count() * 2048 * 4;
+    uint64_t q = o->path_slots ? o->path_slots : d->tuned_slots ? d->tuned_slots : (uint64_t)sm_count() * 2048 * 4;
     q = std::min<uint64_t>(q, P.total);
     q = (q + 127) / 128 * 128;
     WfState W = d->wavefront_state((uint32_t)q);
@@ -1076,7 +1149,7 @@ static int render_wavefront(clv_device_scene* d, const clv_render_opts* o, doubl
     const int batch = 8;  // bounces between polls of the live-path counter
     WfCounters* C = d->wf_counters;
     // shading kernels walk their queues with a grid-stride loop over a fixed grid
-    const uint32_t qgrid = std::min<uint32_t>(grid, (uint32_t)sm_count() * 16);
+    const uint32_t qgrid = std::min<uint32_t>(grid, (uint32_t)sm_count() * (d->tuned_shade ? d->tuned_shade : 16));
     if (prof) {
       std::memset(prof, 0, sizeof *prof);
       ck(cudaMalloc(&dcnt, 3 * sizeof(unsigned long long)), "cudaMalloc");
@@ -1233,7 +1306,9 @@ int clv_render_batch(clv_device_scene* const* ds, const clv_render_opts* opts, d
     B.n = n;
     B.total = total;
     clv_device_scene* d0 = ds[0];  // path state, counters and the error word come from the first scene
-    uint64_t q = opts[0].path_slots ? opts[0].path_slots : (uint64_t)sm_count() * 2048 * 4;
+    uint64_t q = opts[0].path_slots ? opts[0].path_slots
+                 : d0->tuned_slots    ? d0->tuned_slots
+                                      : (uint64_t)sm_count() * 2048 * 4;
     q = std::min<uint64_t>(q, total);
     q = (q + 127) / 128 * 128;
     WfState W = d0->wavefront_state((uint32_t)q);
@@ -1242,7 +1317,7 @@ int clv_render_batch(clv_device_scene* const* ds, const clv_render_opts* opts, d
     WfCounters* C = d0->wf_counters;
     const int block = 128;
     const uint32_t grid = (uint32_t)((q + block - 1) / block);
-    const uint32_t qgrid = std::min<uint32_t>(grid, (uint32_t)sm_count() * 16);
+    const uint32_t qgrid = std::min<uint32_t>(grid, (uint32_t)sm_count() * (d0->tuned_shade ? d0->tuned_shade : 16));
     const ClvDeviceScene& S0 = d0->view;
     const WfParams P0 = params[0];
     wf_init<true><<<grid, block, 0, st>>>(S0, P0, W, B);

@@ -159,6 +159,22 @@ int clv_resolve_device(const double* film_dev, uint32_t width, uint32_t height, 
 /* Host variant of the resolve for XYZ(E) means already on the host. */
 int clv_resolve_srgb(const float* xyz, uint32_t width, uint32_t height, uint8_t* rgb_out);
 
+/* Wavefront shape tuning (no counterpart in the reference; north star
+ * pattern (2)).  Renders `opts` -- pass a short render, a few samples per
+ * pixel of the workload to tune for -- twice for each candidate shape: paths
+ * in flight (path_slots) SMs x {1, 2, 4, 8, 16} x 1024 and shading grids of
+ * {8, 16, 32} blocks per SM, and keeps the fastest in the scene: later
+ * wavefront renders of this scene with opts->path_slots = 0 use it.  results
+ * (optional) receives up to max_results timings, n_results their count (15).
+ * Allocates a film and the largest path state it tries. */
+typedef struct clv_tune_result {
+  uint32_t path_slots;
+  uint32_t shade_blocks_per_sm;
+  float ms;
+} clv_tune_result;
+int clv_autotune(clv_device_scene* dscene, const clv_render_opts* opts, clv_tune_result* results,
+                 uint32_t max_results, uint32_t* n_results, void* stream);
+
 /* ---- ray casts --------------------------------------------------------- */
 
 /* Closest hit of each ray with BVHNode::hit's exact decision order

@@ -96,3 +96,17 @@ def test_render_rejects_mismatched_size(box_scene_path):
     d = cg.Scene.from_json(box_scene_path, 16, 16).upload()
     with pytest.raises(cg.ClvError):
         cg.draw(cg.GlobalOptions(), cg.RenderOptions(width=32, height=16, samples=1), d)
+
+
+def test_autotune_keeps_the_image(box_scene_path):
+    d = cg.Scene.from_json(box_scene_path, 128, 128).upload()
+    opts = cg.RenderOptions(width=128, height=128, samples=8, max_depth=8, seed=3)
+    before = cg.draw(cg.GlobalOptions(quiet=True), opts, d)
+    res = d.autotune(cg.RenderOptions(width=128, height=128, samples=4, max_depth=8, seed=1))
+    assert len(res) == 15 and all(ms > 0 for _, _, ms in res)
+    best = min(res, key=lambda r: r[2])
+    print("autotune: best %s of %d candidates" % (best, len(res)))
+    after = cg.draw(cg.GlobalOptions(quiet=True), opts, d)
+    # the same random streams give the same paths; only the f64 deposit order may move the last bits
+    assert np.allclose(before, after, rtol=1e-5, atol=1e-9)
+    assert d.status() == 0
