@@ -500,6 +500,7 @@ def main():
     import torch
     import clovers_gb300 as cg
     from clovers_gb300 import _lib, scenes
+    from clovers_gb300.distributed import reduce_film
 
     torch.cuda.set_device(local)
     L = _lib.lib()
@@ -529,7 +530,7 @@ def main():
         tune = None
         if args.autotune:  # one-time shape search on a short render of the same scene, before the timed region
             t0 = time.perf_counter()
-            res = dscene.autotune(cg.RenderOptions(width=W_IMG, height=H_IMG, samples=max(1, SPP // 16),
+            res = dscene.autotune(cg.RenderOptions(width=W_IMG, height=H_IMG, samples=max(1, SPP // 4),
                                                    max_depth=DEPTH, seed=SEED + 7), stream=sp)
             best = min(res, key=lambda r: r[2])
             tune = {"path_slots": best[0], "shade_blocks_per_sm": best[1], "candidates": len(res),
@@ -550,6 +551,8 @@ def main():
                 e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
                 e0.record(stream)
                 _lib.check(L.clv_render_device(dscene.handle, ctypes.byref(opts_for(k)), film.data_ptr(), sp))
+                if world > 1:  # one image of all ranks' samples: the film sum (clovers_gb300.distributed)
+                    reduce_film(film)
                 e1.record(stream)
                 e1.synchronize()
                 step_ms.append(e0.elapsed_time(e1))
@@ -616,7 +619,8 @@ def main():
             "data": "synthetic (seeded enclosed-box scene in the reference's scene format)",
             "config": {"workload": "enclosed box %dx%d, %d spp, depth %d (wavefront engine)" % (W_IMG, H_IMG, SPP, DEPTH),
                        "samples_per_step": samples_step, "l2": "flushed between steps (256 MiB write)",
-                       "parallelism": "replicas" if world > 1 else "single GPU", "wall_s_timed_loop": round(wall, 3),
+                       "parallelism": "sample ranges per GPU + film sum" if world > 1 else "single GPU",
+                       "wall_s_timed_loop": round(wall, 3),
                        "autotune": tune},
             "e2e": {"value": round(e2e_value, 3), "unit": "Msamples/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(npix * 3 * 4)},

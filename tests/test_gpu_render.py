@@ -110,3 +110,12 @@ def test_autotune_keeps_the_image(box_scene_path):
     # the same random streams give the same paths; only the f64 deposit order may move the last bits
     assert np.allclose(before, after, rtol=1e-5, atol=1e-9)
     assert d.status() == 0
+
+
+def test_draw_distributed_single_rank_equals_draw(box_scene_path):
+    from clovers_gb300.distributed import draw_distributed
+    d = cg.Scene.from_json(box_scene_path, 64, 64).upload()
+    opts = cg.RenderOptions(width=64, height=64, samples=16, max_depth=8, seed=5)
+    a = cg.draw(cg.GlobalOptions(quiet=True), opts, d)
+    b = draw_distributed(cg.GlobalOptions(quiet=True), opts, d)
+    assert np.allclose(a, b, rtol=1e-5, atol=1e-9)
