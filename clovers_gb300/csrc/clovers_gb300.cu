@@ -30,10 +30,6 @@ using namespace clvd;
 
 // ------------------------------------------------------------------ kernels --
 
-#ifndef CLV_WF_PERSIST
-#define CLV_WF_PERSIST 0  // 1: the persistent wavefront intersect (wf_intersect_persist)
-#endif
-
 // ---- ray order -----------------------------------------------------------
 // Ray casts traverse their rays in the order of a Morton code of the origin
 // (6 bits per axis of the scene box): warps then start from nearby points and
@@ -1154,9 +1150,6 @@ static int render_wavefront(clv_device_scene* d, const clv_render_opts* o, doubl
     WfCounters* C = d->wf_counters;
     // shading kernels walk their queues with a grid-stride loop over a fixed grid
     const uint32_t qgrid = std::min<uint32_t>(grid, (uint32_t)sm_count() * (d->tuned_shade ? d->tuned_shade : 16));
-    // the persistent intersect: every resident block of its launch bound
-    const uint32_t pgrid = std::min<uint32_t>(grid, (uint32_t)sm_count() * CLV_MINB);
-    (void)pgrid;
     if (prof) {
       std::memset(prof, 0, sizeof *prof);
       ck(cudaMalloc(&dcnt, 3 * sizeof(unsigned long long)), "cudaMalloc");
@@ -1176,15 +1169,10 @@ static int render_wavefront(clv_device_scene* d, const clv_render_opts* o, doubl
     }
     // one bounce: counters, closest hits, the shading passes, path ends
     auto bounce = [&](cudaStream_t s, int k) {
-      cudaMemsetAsync(&d->wf_counters->live, 0, 6 * sizeof(unsigned int), s);  // live, 4 queue lengths, isect_next
+      cudaMemsetAsync(&d->wf_counters->live, 0, 5 * sizeof(unsigned int), s);  // live + 4 queue lengths
       if (prof) cudaEventRecord(evs[4 * k], s);
-#if CLV_WF_PERSIST
-#define CLV_ISECT(L, N, T) \
-  wf_intersect_persist<L, N, T><<<pgrid, block, 0, s>>>(d->view, W, C, d->err, N ? dcnt : nullptr)
-#else
 #define CLV_ISECT(L, N, T) \
   wf_intersect<L, N, false, T><<<grid, block, 0, s>>>(d->view, W, C, d->err, N ? dcnt : nullptr, WfBatch{})
-#endif
       switch ((level * 2 + (prof ? 1 : 0)) * 2 + (d->view.watertight ? 1 : 0)) {
         case 0: CLV_ISECT(0, false, CLV_WT_OFF); break;
         case 1: CLV_ISECT(0, false, CLV_WT_ON); break;

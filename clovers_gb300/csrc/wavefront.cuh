@@ -46,7 +46,6 @@ struct WfCounters {
   unsigned long long next_work;  // next unassigned work item
   unsigned int live;             // live paths after the last shading pass
   unsigned int queue[4];         // per-class queue lengths of this bounce
-  unsigned int isect_next;       // next slot of the persistent intersect
 };
 
 struct WfParams {
@@ -172,10 +171,6 @@ __device__ __forceinline__ int material_class(const ClvDeviceScene& S, uint32_t 
   return WF_Q_SPEC;
 }
 
-template <int CPLX>
-__device__ __forceinline__ void intersect_finish(const ClvDeviceScene& S, const WfState& W, WfCounters* C, uint32_t i,
-                                                 const uint4& m, bool any, const Hit& h, const Rec& full,
-                                                 const Rng& rng);
 template <int CPLX, bool COUNT, int WT>
 __device__ __forceinline__ void intersect_slot(const ClvDeviceScene& S, const WfState& W, WfCounters* C, uint32_t* err,
                                                uint32_t i, const uint4& m, Counters& c) {
@@ -191,15 +186,6 @@ __device__ __forceinline__ void intersect_slot(const ClvDeviceScene& S, const Wf
   }
   const bool any = closest_hit<CPLX, WT>(S, r, CLV_EPS_ACNE, CLV_FLT_MAX, CPLX == 2 ? &rng : nullptr, h,
                                      CPLX ? &full : nullptr, COUNT ? &c : nullptr, err);
-  intersect_finish<CPLX>(S, W, C, i, m, any, h, full, rng);
-}
-
-// After the closest hit of slot i: media randomness, material class, the
-// compound record, the hit, and the slot's place in its class queue.
-template <int CPLX>
-__device__ __forceinline__ void intersect_finish(const ClvDeviceScene& S, const WfState& W, WfCounters* C, uint32_t i,
-                                                 const uint4& m, bool any, const Hit& h, const Rec& full,
-                                                 const Rng& rng) {
   if (CPLX == 2 && rng.counter != m.z) W.meta[i].z = rng.counter;
   int cls = WF_Q_FINISH;
   if (any) {
@@ -218,62 +204,6 @@ __device__ __forceinline__ void intersect_finish(const ClvDeviceScene& S, const 
   }
   W.hit[i] = make_float4(any ? h.t : 0.0f, __uint_as_float(any ? h.ref : CLV_REF_EMPTY), h.a, h.b);
   wf_enqueue(W, C, cls, i);
-}
-
-// Persistent form of wf_intersect for one scene: each lane takes the next
-// path slot (one atomic per warp step with idle lanes, on C->isect_next),
-// skips dead slots at the fetch and starts its next query as soon as its
-// traversal ends, so lanes do not wait for the slowest query of the warp.
-// Same queries, same results as wf_intersect.
-template <int CPLX, bool COUNT, int WT>
-__global__ void __launch_bounds__(128, CLV_MINB) wf_intersect_persist(ClvDeviceScene S, WfState W, WfCounters* C,
-                                                                      uint32_t* err, unsigned long long* cnt) {
-  const int lane = threadIdx.x & 31;
-  Counters c{0u, 0u};
-  uint32_t live = 0;
-  Trav T;
-  float4 stack[CLV_STACK];
-  Hit h;
-  Rec full;
-  Rng rng;
-  Ray r{};
-  uint4 m = make_uint4(0u, 0u, 0u, 0u);
-  uint32_t i = 0;
-  bool have = false;
-  while (true) {
-    const unsigned act = __activemask();
-    const unsigned idle = __ballot_sync(act, !have);
-    if (idle) {
-      const int leader = __ffs(idle) - 1;
-      unsigned base = 0;
-      if (lane == leader) base = atomicAdd(&C->isect_next, (unsigned)__popc(idle));
-      base = __shfl_sync(act, base, leader);
-      if (!have) {
-        const unsigned k = base + __popc(idle & ((1u << lane) - 1u));
-        if (k >= W.Q) break;  // every slot taken
-        m = W.meta[k];
-        if (m.w & 1u) {
-          i = k;
-          const float4 a = W.o_time[i], b = W.d_lambda[i];
-          r = Ray{mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, __float_as_int(b.w)};
-          if (CPLX == 2) {  // media draw randomness inside the traversal
-            const uint2 kk = W.key[i];
-            rng.key = (uint64_t)kk.x | ((uint64_t)kk.y << 32);
-            rng.counter = m.z;
-          }
-          trav_begin<WT>(S, r, CLV_EPS_ACNE, CLV_FLT_MAX, T, h);
-          have = true;
-          ++live;
-        }
-      }
-    }
-    if (have && !trav_step<CPLX, WT>(S, r, T, stack, CPLX == 2 ? &rng : nullptr, h, CPLX ? &full : nullptr,
-                                     COUNT ? &c : nullptr, err)) {
-      intersect_finish<CPLX>(S, W, C, i, m, T.found, h, full, rng);
-      have = false;
-    }
-  }
-  if (COUNT) warp_add_counts(cnt, live, c.nodes, c.prims);
 }
 
 // WT: CLV_WT_OFF / CLV_WT_ON for one scene, CLV_WT_SCENE for batches
