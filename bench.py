@@ -472,7 +472,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline legs")
     ap.add_argument("--guided", action="store_true", help="with --config: also the guided time to relMSE 1e-3")
     ap.add_argument("--no-guided", action="store_true", help="skip the guided-vs-plain section of the default run")
-    ap.add_argument("--autotune", action="store_true", help="tune the wavefront shape before the timed render")
+    ap.add_argument("--no-autotune", action="store_true", help="skip the wavefront shape search before the timed render")
     ap.add_argument("--guided-only", action="store_true",
                     help="with --config --guided: only the guided passes (short case for profiling)")
     ap.add_argument("--guide-alpha", type=float, default=0.5)
@@ -528,7 +528,7 @@ def main():
             return o
 
         tune = None
-        if args.autotune:  # one-time shape search on a short render of the same scene, before the timed region
+        if not args.no_autotune:  # one-time shape search on a shorter render of the same scene, before the timed region
             t0 = time.perf_counter()
             res = dscene.autotune(cg.RenderOptions(width=W_IMG, height=H_IMG, samples=max(1, SPP // 4),
                                                    max_depth=DEPTH, seed=SEED + 7), stream=sp)
@@ -567,6 +567,8 @@ def main():
         # e2e: through the host-buffer C ABI (scene upload + render + image download), every step
         xyz = np.empty((npix, 3), np.float32)
         host_opts = opts_for(0)
+        if tune:  # a fresh upload each step: carry the tuned pool size over
+            host_opts.path_slots = tune["path_slots"]
         e2e_times = []
         st = _lib.StatsC()
         h2d = 0
