@@ -105,6 +105,9 @@ __global__ void ray_scatter(const uint32_t* __restrict__ key, uint64_t n, uint32
 // which lanes are idle), so lanes do not sit out the longest ray of their
 // warp (persistent threads with dynamic fetch, Aila & Laine 2009).  Every ray
 // runs closest_hit's exact traversal.  COUNT: per-ray visit counts wanted.
+#ifndef CLV_SHSTACK
+#define CLV_SHSTACK 0  // ray casts: stack entries kept in shared memory (0: all in local memory)
+#endif
 #ifndef CLV_MINB_RAY
 #define CLV_MINB_RAY 9  // 56 registers, no spills: 36 warps per SM (measured best of 6..16)
 #endif
@@ -115,7 +118,14 @@ __global__ void __launch_bounds__(128, CLV_MINB_RAY) raycast_persist_kernel(
     unsigned long long* next, const uint32_t* __restrict__ perm) {
   const int lane = threadIdx.x & 31;
   Trav T;
-  float4 stack[CLV_STACK];
+#if CLV_SHSTACK
+  __shared__ float4 sh_stack[CLV_SHSTACK * 128];
+  float4 loc_stack[CLV_STACK - CLV_SHSTACK];
+  HybridStack<CLV_SHSTACK> stack{sh_stack + threadIdx.x, loc_stack};
+#else
+  float4 stack_mem[CLV_STACK];
+  float4* stack = stack_mem;
+#endif
   Hit h;
   Counters c{0u, 0u};
   Ray r{};

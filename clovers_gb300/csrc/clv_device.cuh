@@ -763,6 +763,26 @@ __device__ __forceinline__ bool leaf_test(const ClvDeviceScene& S, uint32_t ref,
 // stack belongs to an ancestor whose near subtree is being traversed, so when
 // a hit is accepted all current entries are marked, which keeps the marked
 // entries a prefix [0, marked) of the stack.
+// Traversal stacks.  A plain per-thread array (local memory, L1-cached), or a
+// hybrid whose first SH entries sit in shared memory (one column per thread
+// of a 128-thread block) and whose deeper entries spill to local memory.
+__device__ __forceinline__ void st_put(float4* s, int i, float4 v) { s[i] = v; }
+__device__ __forceinline__ float4 st_get(float4* s, int i) { return s[i]; }
+template <int SH>
+struct HybridStack {
+  float4* sh;   // this thread's column: entry k at sh[k * 128]
+  float4* loc;  // entries SH.. in local memory
+};
+template <int SH>
+__device__ __forceinline__ void st_put(HybridStack<SH>& s, int i, float4 v) {
+  if (i < SH) s.sh[i * 128] = v;
+  else s.loc[i - SH] = v;
+}
+template <int SH>
+__device__ __forceinline__ float4 st_get(HybridStack<SH>& s, int i) {
+  return i < SH ? s.sh[i * 128] : s.loc[i - SH];
+}
+
 // The scalar state (kept in registers); the stack array lives apart from it
 // because an indexed array forces its enclosing object into local memory.
 struct Trav {
@@ -795,8 +815,8 @@ __device__ __forceinline__ void trav_begin(const ClvDeviceScene& S, const Ray& r
 // One node visit or leaf test, then the next reference (descend, or pop the
 // next deferred far child whose visit the reference would make).  Returns
 // false when the traversal is over (result in hit / T.found).
-template <int CPLX, int WT>
-__device__ __forceinline__ bool trav_step(const ClvDeviceScene& S, const Ray& r, Trav& T, float4* stack, Rng* rng,
+template <int CPLX, int WT, class STK>
+__device__ __forceinline__ bool trav_step(const ClvDeviceScene& S, const Ray& r, Trav& T, STK& stack, Rng* rng,
                                           Hit& hit, Rec* full, Counters* cnt, uint32_t* err) {
   const RayPre& R = T.R;
   uint32_t ref = T.ref;
@@ -828,7 +848,7 @@ __device__ __forceinline__ bool trav_step(const ClvDeviceScene& S, const Ray& r,
             else slab(fb, r.o, R.inv, fN, fF);
           }
           if (T.sp < CLV_STACK) {
-            stack[T.sp++] = make_float4(__uint_as_float(far), fmaxf(ld, rd), fN, fF);
+            st_put(stack, T.sp++, make_float4(__uint_as_float(far), fmaxf(ld, rd), fN, fF));
           } else if (err) {
             atomicOr(err, CLV_ERR_STACK);
           }
@@ -866,7 +886,7 @@ __device__ __forceinline__ bool trav_step(const ClvDeviceScene& S, const Ray& r,
   // pop the next deferred far child whose visit the reference would make
   while (T.sp > 0) {
     --T.sp;
-    const float4 e = stack[T.sp];
+    const float4 e = st_get(stack, T.sp);
     const bool near_hit = T.sp < T.marked;
     if (T.marked > T.sp) T.marked = T.sp;
     if (near_hit && hit.t < e.y) continue;  // near subtree's hit is closer than the far box
@@ -881,7 +901,8 @@ template <int CPLX, int WT = CLV_WT_SCENE>
 __device__ bool closest_hit(const ClvDeviceScene& S, const Ray& r, float tmin, float tmax, Rng* rng, Hit& hit,
                             Rec* full, Counters* cnt, uint32_t* err) {
   Trav T;
-  float4 stack[CLV_STACK];
+  float4 stack_mem[CLV_STACK];
+  float4* stack = stack_mem;
   trav_begin<WT>(S, r, tmin, tmax, T, hit);
   while (trav_step<CPLX, WT>(S, r, T, stack, rng, hit, full, cnt, err)) {
   }
