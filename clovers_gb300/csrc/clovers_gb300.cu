@@ -106,7 +106,9 @@ __global__ void ray_scatter(const uint32_t* __restrict__ key, uint64_t n, uint32
 // warp (persistent threads with dynamic fetch, Aila & Laine 2009).  Every ray
 // runs closest_hit's exact traversal.  COUNT: per-ray visit counts wanted.
 #ifndef CLV_SHSTACK
-#define CLV_SHSTACK 0  // ray casts: stack entries kept in shared memory (0: all in local memory)
+// ray casts: the first 12 stack entries of each thread in shared memory (24 KB
+// per block, the most that keeps 9 blocks per SM; measured best of 0..24)
+#define CLV_SHSTACK 12
 #endif
 #ifndef CLV_MINB_RAY
 #define CLV_MINB_RAY 9  // 56 registers, no spills: 36 warps per SM (measured best of 6..16)

@@ -897,16 +897,22 @@ __device__ __forceinline__ bool trav_step(const ClvDeviceScene& S, const Ray& r,
   }
   return false;
 }
-template <int CPLX, int WT = CLV_WT_SCENE>
-__device__ bool closest_hit(const ClvDeviceScene& S, const Ray& r, float tmin, float tmax, Rng* rng, Hit& hit,
-                            Rec* full, Counters* cnt, uint32_t* err) {
+// closest_hit with a caller-provided stack (a local array or a HybridStack)
+template <int CPLX, int WT, class STK>
+__device__ __forceinline__ bool closest_hit_stk(const ClvDeviceScene& S, const Ray& r, float tmin, float tmax, Rng* rng,
+                                                Hit& hit, Rec* full, Counters* cnt, uint32_t* err, STK& stack) {
   Trav T;
-  float4 stack_mem[CLV_STACK];
-  float4* stack = stack_mem;
   trav_begin<WT>(S, r, tmin, tmax, T, hit);
   while (trav_step<CPLX, WT>(S, r, T, stack, rng, hit, full, cnt, err)) {
   }
   return T.found;
+}
+template <int CPLX, int WT = CLV_WT_SCENE>
+__device__ bool closest_hit(const ClvDeviceScene& S, const Ray& r, float tmin, float tmax, Rng* rng, Hit& hit,
+                            Rec* full, Counters* cnt, uint32_t* err) {
+  float4 stack_mem[CLV_STACK];
+  float4* stack = stack_mem;
+  return closest_hit_stk<CPLX, WT>(S, r, tmin, tmax, rng, hit, full, cnt, err, stack);
 }
 
 // Full record of the closest hit (deterministic rebuild for primitives).
