@@ -17,10 +17,6 @@
 #include "clv_device.cuh"
 #include "guide.cuh"
 
-#ifndef CLV_SHSTACK_WF
-#define CLV_SHSTACK_WF 0  // wavefront intersect: stack entries kept in shared memory (0: all in local memory)
-#endif
-
 namespace clvd {
 
 struct WfState {
@@ -188,16 +184,8 @@ __device__ __forceinline__ void intersect_slot(const ClvDeviceScene& S, const Wf
     rng.key = (uint64_t)k.x | ((uint64_t)k.y << 32);
     rng.counter = m.z;
   }
-#if CLV_SHSTACK_WF
-  __shared__ float4 sh_stack[CLV_SHSTACK_WF * 128];
-  float4 loc_stack[CLV_STACK - CLV_SHSTACK_WF];
-  HybridStack<CLV_SHSTACK_WF> stack{sh_stack + threadIdx.x, loc_stack};
-#else
-  float4 stack_mem[CLV_STACK];
-  float4* stack = stack_mem;
-#endif
-  const bool any = closest_hit_stk<CPLX, WT>(S, r, CLV_EPS_ACNE, CLV_FLT_MAX, CPLX == 2 ? &rng : nullptr, h,
-                                             CPLX ? &full : nullptr, COUNT ? &c : nullptr, err, stack);
+  const bool any = closest_hit<CPLX, WT>(S, r, CLV_EPS_ACNE, CLV_FLT_MAX, CPLX == 2 ? &rng : nullptr, h,
+                                     CPLX ? &full : nullptr, COUNT ? &c : nullptr, err);
   if (CPLX == 2 && rng.counter != m.z) W.meta[i].z = rng.counter;
   int cls = WF_Q_FINISH;
   if (any) {
