@@ -428,6 +428,11 @@ __device__ __noinline__ bool ObjEval<LEVEL>::hit(const ClvDeviceScene& S, uint32
 // which keeps the loop's state small).  Returns 0 miss, 1 hit, 2 not handled
 // here (media, lists, deeper chains).
 #define CLV_CHAIN 4
+#define CLV_PRAGMA_S(x) _Pragma(#x)
+#define CLV_PRAGMA(x) CLV_PRAGMA_S(x)
+#ifndef CLV_BOXY_UNROLL
+#define CLV_BOXY_UNROLL 1  // unroll factor of a Boxy leaf's loop over its quads
+#endif
 __device__ __forceinline__ V chain_dir(const ClvDeviceScene& S, uint32_t ref, V d, int upto) {
   // direction of the ray as seen below level `upto` (inclusive)
   for (int j = 0; j <= upto; ++j) {
@@ -479,6 +484,7 @@ __device__ __forceinline__ int chain_hit(const ClvDeviceScene& S, uint32_t top, 
     const ClvObj& o = S.objs[idx];
     if (o.kind == CLV_OBJ_BOXY) {  // closest of its 6 quads (boxy.rs:76-94)
       float closest = tmax;
+      CLV_PRAGMA(unroll CLV_BOXY_UNROLL)
       for (int k = 0; k < 6; ++k) {
         if (cnt) cnt->prims++;
         float f[16], t, a, b;
@@ -913,6 +919,50 @@ __device__ bool closest_hit(const ClvDeviceScene& S, const Ray& r, float tmin, f
   float4 stack_mem[CLV_STACK];
   float4* stack = stack_mem;
   return closest_hit_stk<CPLX, WT>(S, r, tmin, tmax, rng, hit, full, cnt, err, stack);
+}
+
+#ifndef CLV_WARP_SCHED
+#define CLV_WARP_SCHED 1  // 0: off; 1: chain leaves wait for the warp; 2: one step class per turn; 3: leaves wait for nodes
+#endif
+// closest_hit for the 32 lanes of a warp together (every lane calls it; `go`
+// is false for lanes without a ray).  Each turn, the warp chooses which of its
+// traversing lanes take their next step; the others wait.  A wrapper-chain
+// leaf (CPLX 1 and 2) costs several primitive tests and transforms, so under
+// scheme 1 a lane whose next step is one waits until every traversing lane of
+// the warp is at one, and the leaf then runs once for all of them.  Every lane
+// still makes exactly closest_hit's sequence of node visits and leaf tests,
+// only later in time, so hits and counts are unchanged.
+template <int CPLX, int WT>
+__device__ __forceinline__ bool closest_hit_warp(const ClvDeviceScene& S, const Ray& r, bool go, float tmin, float tmax,
+                                                 Rng* rng, Hit& hit, Rec* full, Counters* cnt, uint32_t* err) {
+  float4 stack_mem[CLV_STACK];
+  float4* stack = stack_mem;
+  Trav T;
+  T.found = false;
+  T.ref = CLV_REF_EMPTY;
+  bool active = go;
+  if (go) trav_begin<WT>(S, r, tmin, tmax, T, hit);
+  for (;;) {
+    const unsigned act = __ballot_sync(0xFFFFFFFFu, active);
+    if (act == 0u) break;
+    const uint32_t kind = CLV_REF_KIND(T.ref);
+    bool run;
+    if (CLV_WARP_SCHED == 2) {
+      const unsigned nodes = __ballot_sync(0xFFFFFFFFu, active && kind == CLV_REF_NODE);
+      const unsigned chains = __ballot_sync(0xFFFFFFFFu, active && kind == CLV_REF_OBJ);
+      const unsigned prims = act & ~nodes & ~chains;
+      const unsigned turn = nodes ? nodes : (prims ? prims : chains);
+      run = (turn >> (threadIdx.x & 31)) & 1u;
+    } else if (CLV_WARP_SCHED == 3) {
+      const unsigned nodes = __ballot_sync(0xFFFFFFFFu, active && kind == CLV_REF_NODE);
+      run = active && (kind == CLV_REF_NODE || nodes == 0u);
+    } else {
+      const unsigned chains = __ballot_sync(0xFFFFFFFFu, active && kind == CLV_REF_OBJ);
+      run = active && (kind != CLV_REF_OBJ || chains == act);
+    }
+    if (run) active = trav_step<CPLX, WT>(S, r, T, stack, rng, hit, full, cnt, err);
+  }
+  return go && T.found;
 }
 
 // Full record of the closest hit (deterministic rebuild for primitives).

@@ -171,21 +171,34 @@ __device__ __forceinline__ int material_class(const ClvDeviceScene& S, uint32_t 
   return WF_Q_SPEC;
 }
 
+// Every lane of the warp calls this (go: the slot holds a live path).
 template <int CPLX, bool COUNT, int WT>
 __device__ __forceinline__ void intersect_slot(const ClvDeviceScene& S, const WfState& W, WfCounters* C, uint32_t* err,
-                                               uint32_t i, const uint4& m, Counters& c) {
-  const float4 a = W.o_time[i], b = W.d_lambda[i];
-  const Ray r{mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, __float_as_int(b.w)};
+                                               uint32_t i, const uint4& m, bool go, Counters& c) {
+  constexpr bool WARP = CLV_WARP_SCHED > 0 && CPLX > 0;
+  if (!WARP && !go) return;
+  Ray r{mk(0.0f, 0.0f, 0.0f), mk(0.0f, 0.0f, 1.0f), 0.0f, 0};
+  if (go) {
+    const float4 a = W.o_time[i], b = W.d_lambda[i];
+    r = Ray{mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, __float_as_int(b.w)};
+  }
   Hit h;
   Rec full;
   Rng rng;
-  if (CPLX == 2) {  // media draw randomness inside the traversal
+  if (CPLX == 2 && go) {  // media draw randomness inside the traversal
     const uint2 k = W.key[i];
     rng.key = (uint64_t)k.x | ((uint64_t)k.y << 32);
     rng.counter = m.z;
   }
-  const bool any = closest_hit<CPLX, WT>(S, r, CLV_EPS_ACNE, CLV_FLT_MAX, CPLX == 2 ? &rng : nullptr, h,
-                                     CPLX ? &full : nullptr, COUNT ? &c : nullptr, err);
+  bool any;
+  if constexpr (WARP) {
+    any = closest_hit_warp<CPLX, WT>(S, r, go, CLV_EPS_ACNE, CLV_FLT_MAX, CPLX == 2 ? &rng : nullptr, h, &full,
+                                     COUNT ? &c : nullptr, err);
+    if (!go) return;
+  } else {
+    any = closest_hit<CPLX, WT>(S, r, CLV_EPS_ACNE, CLV_FLT_MAX, CPLX == 2 ? &rng : nullptr, h,
+                                CPLX ? &full : nullptr, COUNT ? &c : nullptr, err);
+  }
   if (CPLX == 2 && rng.counter != m.z) W.meta[i].z = rng.counter;
   int cls = WF_Q_FINISH;
   if (any) {
@@ -213,14 +226,11 @@ __global__ void __launch_bounds__(128, CLV_MINB) wf_intersect(ClvDeviceScene S, 
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   Counters c{0u, 0u};
   uint32_t live = 0;
-  if (i < W.Q) {
-    const uint4 m = W.meta[i];
-    if (m.w & 1u) {
-      live = 1;
-      if constexpr (BATCH) intersect_slot<CPLX, COUNT, WT>(B.scenes[m.w >> 8], W, C, err, i, m, c);
-      else intersect_slot<CPLX, COUNT, WT>(S, W, C, err, i, m, c);
-    }
-  }
+  const uint4 m = i < W.Q ? W.meta[i] : make_uint4(0u, 0u, 0u, 0u);
+  const bool go = (m.w & 1u) != 0u;
+  live = go ? 1u : 0u;
+  if constexpr (BATCH) intersect_slot<CPLX, COUNT, WT>(B.scenes[go ? m.w >> 8 : 0u], W, C, err, i, m, go, c);
+  else intersect_slot<CPLX, COUNT, WT>(S, W, C, err, i, m, go, c);
   if (COUNT) warp_add_counts(cnt, live, c.nodes, c.prims);
 }
 
