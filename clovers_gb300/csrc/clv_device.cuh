@@ -789,6 +789,52 @@ __device__ __forceinline__ float4 st_get(HybridStack<SH>& s, int i) {
   return i < SH ? s.sh[i * 128] : s.loc[i - SH];
 }
 
+#ifndef CLV_NODE_FUSED
+#define CLV_NODE_FUSED 2  // 0: separate child box tests; 1: fused; 2: fused, one RayPre::fast branch per node
+#endif
+// Both tests the traversal makes of one child box, from one set of
+// differences d = bound - origin (the same f32 values that AABB::distance and
+// AABB::hit each compute): the slab interval (N, F) of the child's own
+// AABB::hit, made when the child is visited, and its entry distance
+// (AABB::distance, the quotients d / direction).
+// FAST: 0 divides where RayPre::fast does not hold, 1 uses div_fast, 2 tests RayPre::fast per division.
+template <int FAST>
+__device__ __forceinline__ bool child_tests(const float* b, const RayPre& R, float& dist, float& N, float& F) {
+  float d[6];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    d[2 * a] = b[2 * a] - comp(R.o, a);
+    d[2 * a + 1] = b[2 * a + 1] - comp(R.o, a);
+  }
+  float n = -CLV_FLT_MAX * 2.0f, f = CLV_FLT_MAX * 2.0f;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const float t0 = d[2 * a] * comp(R.inv, a), t1 = d[2 * a + 1] * comp(R.inv, a);
+    float nn, ff;
+    if (t0 < t1) { nn = t0; ff = t1; } else { nn = t1; ff = t0; }
+    n = fmaxf(n, nn);
+    f = fminf(f, ff);
+  }
+  N = n;
+  F = f;
+  float q[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    const int a = k >> 1;
+    q[k] = FAST == 2 ? divc(R, d[k], a) : (FAST ? div_fast(d[k], comp(R.d, a), comp(R.inv, a)) : d[k] / comp(R.d, a));
+  }
+  const float tx1 = q[0], tx2 = q[1];
+  float tmin = fminf(tx1, tx2), tmax = fmaxf(tx1, tx2);
+  const float ty1 = q[2], ty2 = q[3];
+  tmin = fmaxf(tmin, fminf(ty1, ty2));
+  tmax = fminf(tmax, fmaxf(ty1, ty2));
+  const float tz1 = q[4], tz2 = q[5];
+  tmin = fmaxf(tmin, fminf(tz1, tz2));
+  tmax = fminf(tmax, fmaxf(tz1, tz2));
+  dist = tmin;
+  return tmax >= tmin && tmax > 0.0f;
+}
+
 // The scalar state (kept in registers); the stack array lives apart from it
 // because an indexed array forces its enclosing object into local memory.
 struct Trav {
@@ -836,7 +882,44 @@ __device__ __forceinline__ bool trav_step(const ClvDeviceScene& S, const Ray& r,
       const uint32_t L = __float_as_uint(q3.x), Rr = __float_as_uint(q3.y);
       uint32_t next = CLV_REF_EMPTY;
       bool left_next = true;
-      if (L != CLV_REF_EMPTY && Rr != CLV_REF_EMPTY) {
+      if (CLV_NODE_FUSED && !wt_on<WT>(S)) {
+        float ld, rd, NL, FL, NR, FR;
+        bool lh, rh;
+        if (CLV_NODE_FUSED == 2) {
+          if (R.fast) {
+            lh = child_tests<1>(lb, R, ld, NL, FL);
+            rh = child_tests<1>(rb, R, rd, NR, FR);
+          } else {
+            lh = child_tests<0>(lb, R, ld, NL, FL);
+            rh = child_tests<0>(rb, R, rd, NR, FR);
+          }
+        } else {
+          lh = child_tests<2>(lb, R, ld, NL, FL);
+          rh = child_tests<2>(rb, R, rd, NR, FR);
+        }
+        const bool both = L != CLV_REF_EMPTY && Rr != CLV_REF_EMPTY;
+        if (both && lh && rh) {
+          left_next = ld < rd;
+          next = left_next ? L : Rr;
+          if (T.sp < CLV_STACK) {
+            st_put(stack, T.sp++, make_float4(__uint_as_float(left_next ? Rr : L), fmaxf(ld, rd), left_next ? NR : NL,
+                                              left_next ? FR : FL));
+          } else if (err) {
+            atomicOr(err, CLV_ERR_STACK);
+          }
+        } else if (both ? lh : L != CLV_REF_EMPTY) {
+          next = L;
+        } else if (both ? rh : Rr != CLV_REF_EMPTY) {
+          next = Rr;
+          left_next = false;
+        }
+        if (next != CLV_REF_EMPTY) {
+          T.N = left_next ? NL : NR;
+          T.F = left_next ? FL : FR;
+          T.ref = next;
+          return true;
+        }
+      } else if (L != CLV_REF_EMPTY && Rr != CLV_REF_EMPTY) {
         float ld, rd;
         const bool wide = wt_on<WT>(S);
         const bool lh = wide ? box_distance_wide(lb, R, ld) : box_distance_pre(lb, R, ld);
