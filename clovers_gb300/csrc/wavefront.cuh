@@ -163,6 +163,66 @@ __device__ __forceinline__ void wf_enqueue(const WfState& W, WfCounters* C, int 
   W.queue[(size_t)cls * W.Q + base + __popc(peers & ((1u << lane) - 1u))] = i;
 }
 
+#ifndef CLV_MINB_SHADE
+#define CLV_MINB_SHADE 8  // resident blocks per SM asked of the shading kernels (64 registers)
+#endif
+#ifndef CLV_BLOCK_ATOMICS
+#define CLV_BLOCK_ATOMICS 1  // queue, work and live counters reserved once per block (1) or per warp (0)
+#endif
+// Appends each thread's slot i to queue `cls` (cls < 0: nothing) with one
+// atomic per class for the whole block; every thread of the 128-thread block
+// calls it.
+__device__ __forceinline__ void wf_enqueue_block(const WfState& W, WfCounters* C, int cls, uint32_t i) {
+  __shared__ uint32_t cnt[4][4];  // [class][warp]
+  __shared__ uint32_t base[4];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned mine = 0u;
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    const unsigned m = __ballot_sync(0xFFFFFFFFu, cls == c);
+    if (lane == 0) cnt[c][warp] = (uint32_t)__popc(m);
+    if (cls == c) mine = m;
+  }
+  __syncthreads();
+  if (threadIdx.x < 4) {
+    const int c = threadIdx.x;
+    const uint32_t tot = cnt[c][0] + cnt[c][1] + cnt[c][2] + cnt[c][3];
+    base[c] = tot ? atomicAdd(&C->queue[c], tot) : 0u;
+  }
+  __syncthreads();
+  if (cls >= 0) {
+    uint32_t pos = base[cls] + (uint32_t)__popc(mine & ((1u << lane) - 1u));
+    for (int w = 0; w < warp; ++w) pos += cnt[cls][w];
+    W.queue[(size_t)cls * W.Q + pos] = i;
+  }
+}
+// Appends the slots of the threads with `want` to queue `cls`, one atomic for
+// the block; every thread of the 128-thread block calls it, in every round.
+__device__ __forceinline__ void wf_enqueue_block_one(const WfState& W, WfCounters* C, int cls, bool want, uint32_t i) {
+  __shared__ uint32_t cnt1[4];
+  __shared__ uint32_t base1;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned m = __ballot_sync(0xFFFFFFFFu, want);
+  if (lane == 0) cnt1[warp] = (uint32_t)__popc(m);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const uint32_t tot = cnt1[0] + cnt1[1] + cnt1[2] + cnt1[3];
+    base1 = tot ? atomicAdd(&C->queue[cls], tot) : 0u;
+  }
+  __syncthreads();
+  if (want) {
+    uint32_t pos = base1 + (uint32_t)__popc(m & ((1u << lane) - 1u));
+    for (int w = 0; w < warp; ++w) pos += cnt1[w];
+    W.queue[(size_t)cls * W.Q + pos] = i;
+  }
+  __syncthreads();  // cnt1 and base1 are rewritten next round
+}
+// The live-path count of a shading kernel: one atomic per warp for all its rounds.
+__device__ __forceinline__ void wf_add_live(WfCounters* C, uint32_t n) {
+  n = __reduce_add_sync(0xFFFFFFFFu, n);
+  if ((threadIdx.x & 31) == 0 && n) atomicAdd(&C->live, n);
+}
+
 __device__ __forceinline__ int material_class(const ClvDeviceScene& S, uint32_t mat, bool guided) {
   const uint32_t k = S.materials[mat].kind;
   if (k == CLV_MAT_LAMBERTIAN) return guided ? WF_Q_GUIDE : WF_Q_DIFF;
@@ -171,12 +231,13 @@ __device__ __forceinline__ int material_class(const ClvDeviceScene& S, uint32_t 
   return WF_Q_SPEC;
 }
 
-// Every lane of the warp calls this (go: the slot holds a live path).
+// Every lane of the warp calls this (go: the slot holds a live path); returns
+// the queue class of the slot's next step, -1 without a path.
 template <int CPLX, bool COUNT, int WT>
-__device__ __forceinline__ void intersect_slot(const ClvDeviceScene& S, const WfState& W, WfCounters* C, uint32_t* err,
-                                               uint32_t i, const uint4& m, bool go, Counters& c) {
+__device__ __forceinline__ int intersect_slot(const ClvDeviceScene& S, const WfState& W, uint32_t* err, uint32_t i,
+                                              const uint4& m, bool go, Counters& c) {
   constexpr bool WARP = CLV_WARP_SCHED > 0 && CPLX > 0;
-  if (!WARP && !go) return;
+  if (!WARP && !go) return -1;
   Ray r{mk(0.0f, 0.0f, 0.0f), mk(0.0f, 0.0f, 1.0f), 0.0f, 0};
   if (go) {
     const float4 a = W.o_time[i], b = W.d_lambda[i];
@@ -194,7 +255,7 @@ __device__ __forceinline__ void intersect_slot(const ClvDeviceScene& S, const Wf
   if constexpr (WARP) {
     any = closest_hit_warp<CPLX, WT>(S, r, go, CLV_EPS_ACNE, CLV_FLT_MAX, CPLX == 2 ? &rng : nullptr, h, &full,
                                      COUNT ? &c : nullptr, err);
-    if (!go) return;
+    if (!go) return -1;
   } else {
     any = closest_hit<CPLX, WT>(S, r, CLV_EPS_ACNE, CLV_FLT_MAX, CPLX == 2 ? &rng : nullptr, h,
                                 CPLX ? &full : nullptr, COUNT ? &c : nullptr, err);
@@ -216,7 +277,7 @@ __device__ __forceinline__ void intersect_slot(const ClvDeviceScene& S, const Wf
     }
   }
   W.hit[i] = make_float4(any ? h.t : 0.0f, __uint_as_float(any ? h.ref : CLV_REF_EMPTY), h.a, h.b);
-  wf_enqueue(W, C, cls, i);
+  return cls;
 }
 
 // WT: CLV_WT_OFF / CLV_WT_ON for one scene, CLV_WT_SCENE for batches
@@ -229,8 +290,11 @@ __global__ void __launch_bounds__(128, CLV_MINB) wf_intersect(ClvDeviceScene S, 
   const uint4 m = i < W.Q ? W.meta[i] : make_uint4(0u, 0u, 0u, 0u);
   const bool go = (m.w & 1u) != 0u;
   live = go ? 1u : 0u;
-  if constexpr (BATCH) intersect_slot<CPLX, COUNT, WT>(B.scenes[go ? m.w >> 8 : 0u], W, C, err, i, m, go, c);
-  else intersect_slot<CPLX, COUNT, WT>(S, W, C, err, i, m, go, c);
+  int cls;
+  if constexpr (BATCH) cls = intersect_slot<CPLX, COUNT, WT>(B.scenes[go ? m.w >> 8 : 0u], W, err, i, m, go, c);
+  else cls = intersect_slot<CPLX, COUNT, WT>(S, W, err, i, m, go, c);
+  if (CLV_BLOCK_ATOMICS) wf_enqueue_block(W, C, cls, i);
+  else if (cls >= 0) wf_enqueue(W, C, cls, i);
   if (COUNT) warp_add_counts(cnt, live, c.nodes, c.prims);
 }
 
@@ -295,7 +359,7 @@ __device__ __forceinline__ bool wf_advance(const WfParams& P, const WfState& W, 
   const uint32_t depth = p.meta.y + 1;
   if (depth > P.max_depth) {  // trace at depth > max_depth returns 0
     W.meta[i].z = p.rng.counter;
-    wf_enqueue(W, C, WF_Q_FINISH, i);
+    if (!CLV_BLOCK_ATOMICS) wf_enqueue(W, C, WF_Q_FINISH, i);
     return false;
   }
   W.o_time[i] = make_float4(origin.x, origin.y, origin.z, p.ray.time);
@@ -341,17 +405,19 @@ __device__ __forceinline__ bool specular_slot(const ClvDeviceScene& S, const WfP
 }
 
 template <bool BATCH>
-__global__ void __launch_bounds__(128) wf_shade_specular(ClvDeviceScene S, WfParams P, WfState W, WfCounters* C,
+__global__ void __launch_bounds__(128, CLV_MINB_SHADE) wf_shade_specular(ClvDeviceScene S, WfParams P, WfState W, WfCounters* C,
                                                          uint32_t* err, WfBatch B) {
   const uint32_t n = C->queue[WF_Q_SPEC];
   const uint32_t stride = gridDim.x * blockDim.x;
   const uint32_t first = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t rounds = (n + stride - 1) / stride;
+  uint32_t nlive = 0;
   for (uint32_t r = 0; r < rounds; ++r) {
     const uint32_t q = first + r * stride;
     bool live = false;
+    uint32_t i = 0;
     if (q < n) {
-      const uint32_t i = W.queue[(size_t)WF_Q_SPEC * W.Q + q];
+      i = W.queue[(size_t)WF_Q_SPEC * W.Q + q];
       if constexpr (BATCH) {
         const uint32_t sid = W.meta[i].w >> 8;
         live = specular_slot(B.scenes[sid], B.params[sid], W, C, i);
@@ -359,8 +425,11 @@ __global__ void __launch_bounds__(128) wf_shade_specular(ClvDeviceScene S, WfPar
         live = specular_slot(S, P, W, C, i);
       }
     }
-    wf_count_live(C, live);
+    if (CLV_BLOCK_ATOMICS) wf_enqueue_block_one(W, C, WF_Q_FINISH, q < n && !live, i);
+    if (CLV_BLOCK_ATOMICS) nlive += live ? 1u : 0u;
+    else wf_count_live(C, live);
   }
+  if (CLV_BLOCK_ATOMICS) wf_add_live(C, nlive);
 }
 
 // Diffuse bounce: MixturePDF(HitablePDF(priority tree), Cosine/SpherePDF), pdf.rs:122-140, trace.rs:80-119
@@ -407,7 +476,7 @@ __device__ __forceinline__ bool diffuse_slot(const ClvDeviceScene& S, const WfPa
   }
   if (!scatter) {
     W.meta[i].z = p.rng.counter;
-    wf_enqueue(W, C, WF_Q_FINISH, i);
+    if (!CLV_BLOCK_ATOMICS) wf_enqueue(W, C, WF_Q_FINISH, i);
     return false;
   }
   float atten[4];
@@ -418,17 +487,19 @@ __device__ __forceinline__ bool diffuse_slot(const ClvDeviceScene& S, const WfPa
 }
 
 template <bool BATCH>
-__global__ void __launch_bounds__(128) wf_shade_diffuse(ClvDeviceScene S, WfParams P, WfState W, WfCounters* C,
+__global__ void __launch_bounds__(128, CLV_MINB_SHADE) wf_shade_diffuse(ClvDeviceScene S, WfParams P, WfState W, WfCounters* C,
                                                         uint32_t* err, WfBatch B) {
   const uint32_t n = C->queue[WF_Q_DIFF];
   const uint32_t stride = gridDim.x * blockDim.x;
   const uint32_t first = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t rounds = (n + stride - 1) / stride;
+  uint32_t nlive = 0;
   for (uint32_t r = 0; r < rounds; ++r) {
     const uint32_t q = first + r * stride;
     bool live = false;
+    uint32_t i = 0;
     if (q < n) {
-      const uint32_t i = W.queue[(size_t)WF_Q_DIFF * W.Q + q];
+      i = W.queue[(size_t)WF_Q_DIFF * W.Q + q];
       if constexpr (BATCH) {
         const uint32_t sid = W.meta[i].w >> 8;
         live = diffuse_slot(B.scenes[sid], B.params[sid], W, C, err, i);
@@ -436,8 +507,11 @@ __global__ void __launch_bounds__(128) wf_shade_diffuse(ClvDeviceScene S, WfPara
         live = diffuse_slot(S, P, W, C, err, i);
       }
     }
-    wf_count_live(C, live);
+    if (CLV_BLOCK_ATOMICS) wf_enqueue_block_one(W, C, WF_Q_FINISH, q < n && !live, i);
+    if (CLV_BLOCK_ATOMICS) nlive += live ? 1u : 0u;
+    else wf_count_live(C, live);
   }
+  if (CLV_BLOCK_ATOMICS) wf_add_live(C, nlive);
 }
 
 // ---- guided Lambertian bounces: pre -> guide network (guide.cu) -> post ----
@@ -546,7 +620,7 @@ __device__ __forceinline__ bool guide_post_slot(const ClvDeviceScene& S, const W
     }
   }
   if (cs < 0.0f) {  // Lambertian::scattering_pdf is None below the surface
-    wf_enqueue(W, C, WF_Q_FINISH, i);
+    if (!CLV_BLOCK_ATOMICS) wf_enqueue(W, C, WF_Q_FINISH, i);
     return false;
   }
   const float spdf = cs / CLV_PI;
@@ -564,12 +638,17 @@ __global__ void __launch_bounds__(128) wf_guide_post(ClvDeviceScene S, WfParams 
   const uint32_t stride = gridDim.x * blockDim.x;
   const uint32_t first = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t rounds = (n + stride - 1) / stride;
+  uint32_t nlive = 0;
   for (uint32_t r = 0; r < rounds; ++r) {
     const uint32_t q = first + r * stride;
     bool live = false;
-    if (q < n) live = guide_post_slot(S, P, W, C, err, G, W.queue[(size_t)WF_Q_GUIDE * W.Q + q]);
-    wf_count_live(C, live);
+    const uint32_t i = q < n ? W.queue[(size_t)WF_Q_GUIDE * W.Q + q] : 0u;
+    if (q < n) live = guide_post_slot(S, P, W, C, err, G, i);
+    if (CLV_BLOCK_ATOMICS) wf_enqueue_block_one(W, C, WF_Q_FINISH, q < n && !live, i);
+    if (CLV_BLOCK_ATOMICS) nlive += live ? 1u : 0u;
+    else wf_count_live(C, live);
   }
+  if (CLV_BLOCK_ATOMICS) wf_add_live(C, nlive);
 }
 
 // film rule of draw_cpu.rs:131-142, deposited as f64 sums
@@ -639,12 +718,13 @@ __device__ __forceinline__ void finish_slot(const ClvDeviceScene& S, const WfSta
 
 // Ends paths, then each slot takes the next work item (one atomic per warp).
 template <bool BATCH>
-__global__ void __launch_bounds__(128) wf_finish(ClvDeviceScene S, WfParams P, WfState W, WfCounters* C,
+__global__ void __launch_bounds__(128, CLV_MINB_SHADE) wf_finish(ClvDeviceScene S, WfParams P, WfState W, WfCounters* C,
                                                  double* __restrict__ film, WfBatch B) {
   const uint32_t n = C->queue[WF_Q_FINISH];
   const uint32_t stride = gridDim.x * blockDim.x;
   const uint32_t first = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t rounds = (n + stride - 1) / stride;
+  uint32_t nlive = 0;
   for (uint32_t r = 0; r < rounds; ++r) {
     const uint32_t q = first + r * stride;
     bool need = false;
@@ -661,12 +741,30 @@ __global__ void __launch_bounds__(128) wf_finish(ClvDeviceScene S, WfParams P, W
     }
     const unsigned mask = __ballot_sync(0xFFFFFFFFu, need);
     bool live = false;
-    if (mask) {
-      const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31;
+    unsigned long long base = 0;
+    if (CLV_BLOCK_ATOMICS) {  // one reservation of work items for the block
+      __shared__ uint32_t wcnt[4];
+      __shared__ unsigned long long wbase;
+      const int warp = threadIdx.x >> 5;
+      if (lane == 0) wcnt[warp] = (uint32_t)__popc(mask);
+      __syncthreads();
+      uint32_t before = 0, total = 0;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        before += k < warp ? wcnt[k] : 0u;
+        total += wcnt[k];
+      }
+      if (threadIdx.x == 0 && total) wbase = atomicAdd(&C->next_work, (unsigned long long)total);
+      __syncthreads();
+      if (total) base = wbase + before;
+      __syncthreads();  // wcnt and wbase are rewritten next round
+    } else if (mask) {
       const int leader = __ffs(mask) - 1;
-      unsigned long long base = 0;
       if (lane == leader) base = atomicAdd(&C->next_work, (unsigned long long)__popc(mask));
       base = __shfl_sync(0xFFFFFFFFu, base, leader);
+    }
+    if (mask) {
       if (need) {
         const uint64_t w = base + __popc(mask & ((1u << lane) - 1u));
         if constexpr (BATCH) {
@@ -687,8 +785,10 @@ __global__ void __launch_bounds__(128) wf_finish(ClvDeviceScene S, WfParams P, W
         }
       }
     }
-    wf_count_live(C, live);
+    if (CLV_BLOCK_ATOMICS) nlive += live ? 1u : 0u;
+    else wf_count_live(C, live);
   }
+  if (CLV_BLOCK_ATOMICS) wf_add_live(C, nlive);
 }
 
 }  // namespace clvd
