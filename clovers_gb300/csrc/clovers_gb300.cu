@@ -544,11 +544,32 @@ static bool boxes_div_safe(const clv::HostScene& h) {
 }
 
 // Which traversal variant the scene needs: 0 primitives only, 1 wrapper
-// chains handled inline (chain_hit), 2 media or lists (interpreter).
+// chains handled inline (chain_hit), 2 media or lists (interpreter).  Only the
+// objects the BVH's leaves reach count: a list or mesh given at the top level
+// is flattened into the tree, and its own record is never visited.
 static uint32_t compound_level(const clv::HostScene& h) {
   if (h.objs.empty()) return 0;
-  for (size_t i = 0; i < h.objs.size(); ++i) {
+  std::vector<char> seen(h.objs.size(), 0);
+  std::vector<uint32_t> todo;
+  auto reach = [&](uint32_t r) {
+    if (r == CLV_REF_EMPTY || CLV_REF_KIND(r) != CLV_REF_OBJ) return;
+    const uint32_t i = CLV_REF_INDEX(r);
+    if (i < h.objs.size() && !seen[i]) {
+      seen[i] = 1;
+      todo.push_back(i);
+    }
+  };
+  reach(h.root);
+  for (const ClvNode& n : h.nodes) {
+    reach(n.left);
+    reach(n.right);
+  }
+  uint32_t level = 0;
+  while (!todo.empty()) {
+    const uint32_t i = todo.back();
+    todo.pop_back();
     const ClvObj& o = h.objs[i];
+    level = std::max(level, 1u);
     if (o.kind == CLV_OBJ_MEDIUM || o.kind == CLV_OBJ_LIST) return 2;
     if (o.kind == CLV_OBJ_TRANSLATE || o.kind == CLV_OBJ_ROTATEY) {
       int depth = 0;
@@ -560,9 +581,10 @@ static uint32_t compound_level(const clv::HostScene& h) {
         r = w.a;
       }
       if (depth > CLV_CHAIN) return 2;
+      reach(o.a);
     }
   }
-  return 1;
+  return level;
 }
 
 struct clv_device_scene {
