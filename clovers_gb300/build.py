@@ -74,6 +74,7 @@ def build(force=False, verbose=False, ptxas_info=False):
         guide_cmd[1:1] = ["-Xptxas", "-v"]
     extra = os.environ.get("CLV_NVCC_FLAGS", "").split()  # e.g. -DCLV_MINB=8 for occupancy experiments
     cu_cmd[1:1] = extra
+    guide_cmd[1:1] = extra
     cxx = os.environ.get("CXX", "g++")
     cpp_cmd = [cxx, "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-I", INCLUDE, "-c",
                os.path.join(CSRC, "scene.cpp"), "-o", cpp_obj]

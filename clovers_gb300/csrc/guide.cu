@@ -682,12 +682,21 @@ __global__ void __launch_bounds__(128, 1) guide_train_kernel(const unsigned char
 
 // Gathers the records that carry light (f > 0); the others add nothing to the
 // gradient.  Warp-aggregated append, order not preserved.
+// Keeps the records with a positive finite weight.  Record k of the input is
+// read at (k * GD_SHUFFLE) mod n, a permutation of [0, n) since the prime
+// GD_SHUFFLE exceeds n: the records come out of the renderer roughly in pixel
+// order, and the training steps take consecutive batches of the output, which
+// this spreads over the whole image.
+#ifndef GD_SHUFFLE
+#define GD_SHUFFLE 2654435761ull  // prime above the largest record capacity (2^26)
+#endif
 __global__ void guide_compact_kernel(const float4* __restrict__ rec, uint32_t n, float4* __restrict__ out,
                                      unsigned int* __restrict__ count) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t i = k < n ? (uint32_t)(((uint64_t)k * GD_SHUFFLE) % n) : 0u;
   bool keep = false;
   float4 c = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-  if (i < n) {
+  if (k < n) {
     c = rec[GD_REC_F4 * (size_t)i + 2];
     keep = c.w > 0.0f && c.w < 3.0e38f;
   }
