@@ -1206,7 +1206,7 @@ static int render_wavefront(clv_device_scene* d, const clv_render_opts* o, doubl
       cudaMemsetAsync(&d->wf_counters->live, 0, 5 * sizeof(unsigned int), s);  // live + 4 queue lengths
       if (prof) cudaEventRecord(evs[4 * k], s);
 #define CLV_ISECT(L, N, T) \
-  wf_intersect<L, N, false, T><<<grid, block, 0, s>>>(d->view, W, C, d->err, N ? dcnt : nullptr, WfBatch{})
+  wf_intersect<L, N, false, T><<<grid, block, 0, s>>>(d->view, W, C, d->err, N ? dcnt : nullptr, WfBatch{}, -1)
       switch ((level * 2 + (prof ? 1 : 0)) * 2 + (d->view.watertight ? 1 : 0)) {
         case 0: CLV_ISECT(0, false, CLV_WT_OFF); break;
         case 1: CLV_ISECT(0, false, CLV_WT_ON); break;
@@ -1302,7 +1302,7 @@ int clv_render_batch(clv_device_scene* const* ds, const clv_render_opts* opts, d
     std::vector<WfParams> params(n);
     std::vector<unsigned long long> prefix(n + 1, 0ull);
     std::vector<double*> fl(films, films + n);
-    uint32_t level = 0;
+    uint32_t levels = 0;  // bit L: some scene needs traversal level L
     for (uint32_t k = 0; k < n; ++k) {
       views[k] = ds[k]->view;
       const clv_render_opts& o = opts[k];
@@ -1315,8 +1315,9 @@ int clv_render_batch(clv_device_scene* const* ds, const clv_render_opts* opts, d
       P.total = P.npix * o.samples;
       P.seed = o.seed;
       prefix[k + 1] = prefix[k] + P.total;
-      level = std::max(level, ds[k]->view.compound_level);
+      levels |= 1u << ds[k]->view.compound_level;
     }
+    const int nlevels = __builtin_popcount(levels);
     const unsigned long long total = prefix[n];
     // one staging allocation for the batch tables
     const size_t b_views = n * sizeof(ClvDeviceScene), b_params = n * sizeof(WfParams);
@@ -1362,11 +1363,16 @@ int clv_render_batch(clv_device_scene* const* ds, const clv_render_opts* opts, d
     auto bounces = [&](cudaStream_t s) {
       for (int k = 0; k < batch; ++k) {
         cudaMemsetAsync(&C->live, 0, 5 * sizeof(unsigned int), s);
-        switch (level) {
-          case 0: wf_intersect<0, false, true, CLV_WT_SCENE><<<grid, block, 0, s>>>(S0, W, C, d0->err, nullptr, B); break;
-          case 1: wf_intersect<1, false, true, CLV_WT_SCENE><<<grid, block, 0, s>>>(S0, W, C, d0->err, nullptr, B); break;
-          default: wf_intersect<2, false, true, CLV_WT_SCENE><<<grid, block, 0, s>>>(S0, W, C, d0->err, nullptr, B); break;
-        }
+        // one intersect launch per traversal level present, each over its own scenes' slots
+        const int only = nlevels > 1 ? 0 : -1;
+        if (levels & 1u)
+          wf_intersect<0, false, true, CLV_WT_SCENE><<<grid, block, 0, s>>>(S0, W, C, d0->err, nullptr, B, only);
+        if (levels & 2u)
+          wf_intersect<1, false, true, CLV_WT_SCENE><<<grid, block, 0, s>>>(S0, W, C, d0->err, nullptr, B,
+                                                                            only < 0 ? -1 : 1);
+        if (levels & 4u)
+          wf_intersect<2, false, true, CLV_WT_SCENE><<<grid, block, 0, s>>>(S0, W, C, d0->err, nullptr, B,
+                                                                            only < 0 ? -1 : 2);
         wf_shade_specular<true><<<qgrid, block, 0, s>>>(S0, P0, W, C, d0->err, B);
         wf_shade_diffuse<true><<<qgrid, block, 0, s>>>(S0, P0, W, C, d0->err, B);
         wf_finish<true><<<qgrid, block, 0, s>>>(S0, P0, W, C, nullptr, B);
@@ -1376,7 +1382,7 @@ int clv_render_batch(clv_device_scene* const* ds, const clv_render_opts* opts, d
     for (uint64_t it = 0;; it += batch) {
       if (graph.exec) ck(cudaGraphLaunch(graph.exec, st), "cudaGraphLaunch");
       else bounces(st);
-      g_launches += 4 * batch;
+      g_launches += (3 + nlevels) * batch;
       ck(cudaGetLastError(), "wavefront launch");
       ck(cudaMemcpyAsync(d0->wf_live_host, &C->live, sizeof(unsigned int), cudaMemcpyDeviceToHost, st),
          "cudaMemcpyAsync");
@@ -1638,12 +1644,12 @@ extern "C" int clv_render_device_noalloc(clv_device_scene* d, const clv_render_o
     for (int k = 0; k < batch; ++k) {
       cudaMemsetAsync(&C->live, 0, 5 * sizeof(unsigned int), st);
       switch (level * 2 + (d->view.watertight ? 1 : 0)) {
-        case 0: wf_intersect<0, false, false, CLV_WT_OFF><<<grid, block, 0, st>>>(d->view, W, C, d->err, nullptr, WfBatch{}); break;
-        case 1: wf_intersect<0, false, false, CLV_WT_ON><<<grid, block, 0, st>>>(d->view, W, C, d->err, nullptr, WfBatch{}); break;
-        case 2: wf_intersect<1, false, false, CLV_WT_OFF><<<grid, block, 0, st>>>(d->view, W, C, d->err, nullptr, WfBatch{}); break;
-        case 3: wf_intersect<1, false, false, CLV_WT_ON><<<grid, block, 0, st>>>(d->view, W, C, d->err, nullptr, WfBatch{}); break;
-        case 4: wf_intersect<2, false, false, CLV_WT_OFF><<<grid, block, 0, st>>>(d->view, W, C, d->err, nullptr, WfBatch{}); break;
-        default: wf_intersect<2, false, false, CLV_WT_ON><<<grid, block, 0, st>>>(d->view, W, C, d->err, nullptr, WfBatch{}); break;
+        case 0: wf_intersect<0, false, false, CLV_WT_OFF><<<grid, block, 0, st>>>(d->view, W, C, d->err, nullptr, WfBatch{}, -1); break;
+        case 1: wf_intersect<0, false, false, CLV_WT_ON><<<grid, block, 0, st>>>(d->view, W, C, d->err, nullptr, WfBatch{}, -1); break;
+        case 2: wf_intersect<1, false, false, CLV_WT_OFF><<<grid, block, 0, st>>>(d->view, W, C, d->err, nullptr, WfBatch{}, -1); break;
+        case 3: wf_intersect<1, false, false, CLV_WT_ON><<<grid, block, 0, st>>>(d->view, W, C, d->err, nullptr, WfBatch{}, -1); break;
+        case 4: wf_intersect<2, false, false, CLV_WT_OFF><<<grid, block, 0, st>>>(d->view, W, C, d->err, nullptr, WfBatch{}, -1); break;
+        default: wf_intersect<2, false, false, CLV_WT_ON><<<grid, block, 0, st>>>(d->view, W, C, d->err, nullptr, WfBatch{}, -1); break;
       }
       wf_shade_specular<false><<<qgrid, block, 0, st>>>(d->view, P, W, C, d->err, WfBatch{});
       wf_shade_diffuse<false><<<qgrid, block, 0, st>>>(d->view, P, W, C, d->err, WfBatch{});

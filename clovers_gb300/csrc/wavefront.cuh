@@ -280,15 +280,18 @@ __device__ __forceinline__ int intersect_slot(const ClvDeviceScene& S, const WfS
   return cls;
 }
 
-// WT: CLV_WT_OFF / CLV_WT_ON for one scene, CLV_WT_SCENE for batches
+// WT: CLV_WT_OFF / CLV_WT_ON for one scene, CLV_WT_SCENE for batches.
+// only_level >= 0 (batches): only the slots of scenes at that traversal level,
+// so that a batch runs each scene with the variant its objects need.
 template <int CPLX, bool COUNT, bool BATCH, int WT>
 __global__ void __launch_bounds__(128, CLV_MINB) wf_intersect(ClvDeviceScene S, WfState W, WfCounters* C, uint32_t* err,
-                                                              unsigned long long* cnt, WfBatch B) {
+                                                              unsigned long long* cnt, WfBatch B, int only_level) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   Counters c{0u, 0u};
   uint32_t live = 0;
   const uint4 m = i < W.Q ? W.meta[i] : make_uint4(0u, 0u, 0u, 0u);
-  const bool go = (m.w & 1u) != 0u;
+  bool go = (m.w & 1u) != 0u;
+  if (BATCH && go && only_level >= 0) go = B.scenes[m.w >> 8].compound_level == (uint32_t)only_level;
   live = go ? 1u : 0u;
   int cls;
   if constexpr (BATCH) cls = intersect_slot<CPLX, COUNT, WT>(B.scenes[go ? m.w >> 8 : 0u], W, err, i, m, go, c);
