@@ -36,7 +36,7 @@ namespace clvd {
 #define CLV_MIS_STACK 32   // MIS tree evaluation stack
 #define CLV_NEST 6         // wrapper nesting depth handled by the object interpreter
 #ifndef CLV_MINB
-#define CLV_MINB 8         // resident blocks per SM asked of the traversal kernels (64 registers)
+#define CLV_MINB 7         // resident blocks per SM asked of the traversal kernels (72 registers; 6 and 8 slower)
 #endif
 
 // Device error flags (bitwise OR into a status word the host reads).
