@@ -53,6 +53,29 @@ __device__ __forceinline__ V add(V a, V b) { return mk(a.x + b.x, a.y + b.y, a.z
 __device__ __forceinline__ V sub(V a, V b) { return mk(a.x - b.x, a.y - b.y, a.z - b.z); }
 __device__ __forceinline__ V neg(V a) { return mk(-a.x, -a.y, -a.z); }
 __device__ __forceinline__ V scl(float s, V a) { return mk(s * a.x, s * a.y, s * a.z); }
+// a / d for the slab divisions of AABB::distance, given inv = RN(1/d).
+// q0 = RN(a*inv); the residual a - q0*d is exact with an FMA and one
+// correction step q0 + residual*inv rounds to the correctly rounded quotient
+// (Markstein's theorem; Muller et al., Handbook of Floating-Point Arithmetic,
+// ch. 8) provided nothing overflows or underflows.  The traversal uses the
+// unguarded form only when that is guaranteed for every box of the scene and
+// the ray (see RayPre::fast); otherwise it divides.
+__device__ __forceinline__ float div_fast(float a, float d, float inv) {
+  const float q0 = a * inv;
+  const float r = __fmaf_rn(-q0, d, a);
+  return __fmaf_rn(r, inv, q0);
+}
+// the guarded form, valid for any operands (used by the self-test)
+__device__ __forceinline__ float div_rn(float a, float d, float inv) {
+  const float q0 = a * inv;
+  const float aq = fabsf(q0);
+  if (aq >= 8.67361738e-19f && aq <= 1.15292150e18f) {  // 2^-60 .. 2^60
+    const float r = __fmaf_rn(-q0, d, a);
+    return __fmaf_rn(r, inv, q0);
+  }
+  return a / d;
+}
+
 __device__ __forceinline__ V dvs(V a, float s) { return mk(a.x / s, a.y / s, a.z / s); }
 __device__ __forceinline__ float dot(V a, V b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 __device__ __forceinline__ V cross(V a, V b) {
@@ -614,29 +637,6 @@ struct Hit {
   uint32_t ref;  // leaf ref that produced the hit, CLV_REF_EMPTY if none
   float a, b;    // plane coordinates (triangle / quad)
 };
-
-// a / d for the slab divisions of AABB::distance, given inv = RN(1/d).
-// q0 = RN(a*inv); the residual a - q0*d is exact with an FMA and one
-// correction step q0 + residual*inv rounds to the correctly rounded quotient
-// (Markstein's theorem; Muller et al., Handbook of Floating-Point Arithmetic,
-// ch. 8) provided nothing overflows or underflows.  The traversal uses the
-// unguarded form only when that is guaranteed for every box of the scene and
-// the ray (see RayPre::fast); otherwise it divides.
-__device__ __forceinline__ float div_fast(float a, float d, float inv) {
-  const float q0 = a * inv;
-  const float r = __fmaf_rn(-q0, d, a);
-  return __fmaf_rn(r, inv, q0);
-}
-// the guarded form, valid for any operands (used by the self-test)
-__device__ __forceinline__ float div_rn(float a, float d, float inv) {
-  const float q0 = a * inv;
-  const float aq = fabsf(q0);
-  if (aq >= 8.67361738e-19f && aq <= 1.15292150e18f) {  // 2^-60 .. 2^60
-    const float r = __fmaf_rn(-q0, d, a);
-    return __fmaf_rn(r, inv, q0);
-  }
-  return a / d;
-}
 
 // Per-ray constants of the traversal.  `fast` holds when the scene's box
 // coordinates and the ray origin are each 0 or of magnitude in [2^-70, 2^59]
