@@ -797,6 +797,19 @@ __device__ __forceinline__ float4 st_get(HybridStack<SH>& s, int i) {
 // AABB::hit each compute): the slab interval (N, F) of the child's own
 // AABB::hit, made when the child is visited, and its entry distance
 // (AABB::distance, the quotients d / direction).
+#ifndef CLV_MINMAX3
+#define CLV_MINMAX3 1  // fast rays: slab and distance reductions as three-input min / max
+#endif
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+  float d;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
+}
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+  float d;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
+}
 // FAST: 0 divides where RayPre::fast does not hold, 1 uses div_fast, 2 tests RayPre::fast per division.
 template <int FAST>
 __device__ __forceinline__ bool child_tests(const float* b, const RayPre& R, float& dist, float& N, float& F) {
@@ -805,6 +818,26 @@ __device__ __forceinline__ bool child_tests(const float* b, const RayPre& R, flo
   for (int a = 0; a < 3; ++a) {
     d[2 * a] = b[2 * a] - comp(R.o, a);
     d[2 * a + 1] = b[2 * a + 1] - comp(R.o, a);
+  }
+  if (FAST == 1 && CLV_MINMAX3) {
+    // Under RayPre::fast every difference is finite and every reciprocal finite
+    // and non-zero, so no slab value or quotient is NaN: the reference's
+    // compare-and-swap ordering and its chained fmin/fmax reduce to plain
+    // min / max (equal up to the sign of a zero, and the results feed only
+    // comparisons).
+    float t[6], q[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      const int a = k >> 1;
+      t[k] = d[k] * comp(R.inv, a);
+      q[k] = div_fast(d[k], comp(R.d, a), comp(R.inv, a));
+    }
+    N = max3f(fminf(t[0], t[1]), fminf(t[2], t[3]), fminf(t[4], t[5]));
+    F = min3f(fmaxf(t[0], t[1]), fmaxf(t[2], t[3]), fmaxf(t[4], t[5]));
+    const float tmin = max3f(fminf(q[0], q[1]), fminf(q[2], q[3]), fminf(q[4], q[5]));
+    const float tmax = min3f(fmaxf(q[0], q[1]), fmaxf(q[2], q[3]), fmaxf(q[4], q[5]));
+    dist = tmin;
+    return tmax >= tmin && tmax > 0.0f;
   }
   float n = -CLV_FLT_MAX * 2.0f, f = CLV_FLT_MAX * 2.0f;
 #pragma unroll
