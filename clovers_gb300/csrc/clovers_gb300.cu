@@ -110,6 +110,9 @@ __global__ void ray_scatter(const uint32_t* __restrict__ key, uint64_t n, uint32
 // per block, the most that keeps 9 blocks per SM; measured best of 0..24)
 #define CLV_SHSTACK 12
 #endif
+#ifndef CLV_LEAF_BATCH
+#define CLV_LEAF_BATCH 8  // ray casts: a lane at a leaf waits until this many lanes are at one (0: never; 4..16 measured)
+#endif
 #ifndef CLV_MINB_RAY
 #define CLV_MINB_RAY 9  // 56 registers, no spills: 36 warps per SM (measured best of 6..16)
 #endif
@@ -154,7 +157,16 @@ __global__ void __launch_bounds__(128, CLV_MINB_RAY) raycast_persist_kernel(
         have = true;
       }
     }
-    if (have && !trav_step<CPLX, WT>(S, r, T, stack, &rng, h, nullptr, COUNT ? &c : nullptr, err)) {
+    bool step = have;
+    if (CLV_LEAF_BATCH > 0) {
+      // Leaf tests in groups: a lane whose next step is a leaf waits while
+      // fewer than CLV_LEAF_BATCH lanes are at one and some lane is at a node.
+      // Each ray's own sequence of steps is unchanged.
+      const bool at_leaf = have && CLV_REF_KIND(T.ref) != CLV_REF_NODE;
+      const unsigned lm = __ballot_sync(act, at_leaf), hm = __ballot_sync(act, have);
+      if (at_leaf && __popc(lm) < CLV_LEAF_BATCH && lm != hm) step = false;
+    }
+    if (step && !trav_step<CPLX, WT>(S, r, T, stack, &rng, h, nullptr, COUNT ? &c : nullptr, err)) {
       __stcs(prim + i, T.found ? hit_gid(S, h.ref) : 0xFFFFFFFFu);
       __stcs(tout + i, T.found ? h.t : 0.0f);
       if (COUNT) {

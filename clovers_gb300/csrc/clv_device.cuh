@@ -1040,6 +1040,7 @@ __device__ bool closest_hit(const ClvDeviceScene& S, const Ray& r, float tmin, f
 #ifndef CLV_WARP_SCHED
 #define CLV_WARP_SCHED 1  // 0: off; 1: chain leaves wait for the warp; 2: one step class per turn; 3: leaves wait for nodes
 #endif
+
 // closest_hit for the 32 lanes of a warp together (every lane calls it; `go`
 // is false for lanes without a ray).  Each turn, the warp chooses which of its
 // traversing lanes take their next step; the others wait.  A wrapper-chain
