@@ -166,6 +166,9 @@ __device__ __forceinline__ void wf_enqueue(const WfState& W, WfCounters* C, int 
 #ifndef CLV_MINB_SHADE
 #define CLV_MINB_SHADE 8  // resident blocks per SM asked of the shading kernels (64 registers)
 #endif
+#ifndef CLV_MINB_GUIDE
+#define CLV_MINB_GUIDE CLV_MINB_SHADE  // the same for the guided bounce kernels
+#endif
 #ifndef CLV_BLOCK_ATOMICS
 #define CLV_BLOCK_ATOMICS 1  // queue, work and live counters reserved once per block (1) or per warp (0)
 #endif
@@ -553,7 +556,7 @@ __device__ __forceinline__ void guide_pre_slot(const ClvDeviceScene& S, const Wf
   W.meta[i].z = p.rng.counter;
 }
 
-__global__ void __launch_bounds__(128) wf_guide_pre(ClvDeviceScene S, WfState W, WfCounters* C, float alpha) {
+__global__ void __launch_bounds__(128, CLV_MINB_GUIDE) wf_guide_pre(ClvDeviceScene S, WfState W, WfCounters* C, float alpha) {
   const uint32_t n = C->queue[WF_Q_GUIDE];
   const uint32_t stride = gridDim.x * blockDim.x;
   for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += stride)
@@ -635,7 +638,7 @@ __device__ __forceinline__ bool guide_post_slot(const ClvDeviceScene& S, const W
   return wf_advance(P, W, C, i, p, rec.p, nd);
 }
 
-__global__ void __launch_bounds__(128) wf_guide_post(ClvDeviceScene S, WfParams P, WfState W, WfCounters* C,
+__global__ void __launch_bounds__(128, CLV_MINB_GUIDE) wf_guide_post(ClvDeviceScene S, WfParams P, WfState W, WfCounters* C,
                                                      uint32_t* err, GuideDev G) {
   const uint32_t n = C->queue[WF_Q_GUIDE];
   const uint32_t stride = gridDim.x * blockDim.x;
