@@ -29,7 +29,7 @@ class RenderOptsC(ctypes.Structure):
 class SceneInfoC(ctypes.Structure):
     _fields_ = [("objects", c_u64), ("nodes", c_u32), ("triangles", c_u32), ("quads", c_u32),
                 ("spheres", c_u32), ("compound", c_u32), ("materials", c_u32), ("tree_depth", c_u32),
-                ("mis_nodes", c_u32), ("width", c_u32), ("height", c_u32)]
+                ("mis_nodes", c_u32), ("width", c_u32), ("height", c_u32), ("traversal_level", c_u32)]
 
 
 class StatsC(ctypes.Structure):

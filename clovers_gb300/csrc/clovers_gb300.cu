@@ -962,6 +962,7 @@ int clv_scene_info_get(const clv_scene* s, clv_scene_info* out) {
   out->mis_nodes = (uint32_t)h.mis_nodes.size();
   out->width = h.width;
   out->height = h.height;
+  out->traversal_level = compound_level(h);
   return CLV_OK;
 }
 

@@ -65,6 +65,9 @@ typedef struct clv_scene_info {
   uint32_t tree_depth;  /* BVH depth (root = 1) */
   uint32_t mis_nodes;
   uint32_t width, height;
+  uint32_t traversal_level; /* intersect variant the scene needs: 0 primitives only, 1 wrapper
+                               chains (Translate/RotateY over Boxy, spheres, quads, triangles),
+                               2 media or nested lists; only objects the BVH reaches count */
 } clv_scene_info;
 
 typedef struct clv_stats {
