@@ -617,10 +617,15 @@ def main():
                    "wf_shade": (prof.ms_shade, shade_bytes, prof.shade_launches)}
         dom = max(kernels, key=lambda k: kernels[k][0])
         d_ms, d_bytes, d_launches = kernels[dom]
+        # captured per-launch DRAM bytes, scaled to this render's path-slot count (one slot per query)
+        dom_traffic = traffic.get(dom + ".bytes_per_launch")
+        if dom_traffic is not None and traffic.get(dom + ".slots"):
+            slots = tune["path_slots"] if tune else torch.cuda.get_device_properties(0).multi_processor_count * 8192
+            dom_traffic = round(dom_traffic * slots / traffic[dom + ".slots"])
         achieved = d_bytes / (d_ms / 1e3) / 1e9
         roofline = {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",
                     "frac": round(achieved / hbm_peak, 4), "peak_kind": peak_kind,
-                    "traffic": traffic.get(dom + ".bytes_per_launch"),
+                    "traffic": dom_traffic,
                     "algorithmic_bytes_per_launch": round(d_bytes / max(1, d_launches)),
                     "kernel_ms_per_step": {k: round(v[0], 3) for k, v in kernels.items()},
                     "path_segments": segs, "node_visits": prof.node_visits, "prim_tests": prof.prim_tests}
