@@ -789,17 +789,11 @@ __device__ __forceinline__ float4 st_get(HybridStack<SH>& s, int i) {
   return i < SH ? s.sh[i * 128] : s.loc[i - SH];
 }
 
-#ifndef CLV_NODE_FUSED
-#define CLV_NODE_FUSED 2  // 0: separate child box tests; 1: fused; 2: fused, one RayPre::fast branch per node
-#endif
 // Both tests the traversal makes of one child box, from one set of
 // differences d = bound - origin (the same f32 values that AABB::distance and
 // AABB::hit each compute): the slab interval (N, F) of the child's own
 // AABB::hit, made when the child is visited, and its entry distance
 // (AABB::distance, the quotients d / direction).
-#ifndef CLV_MINMAX3
-#define CLV_MINMAX3 1  // fast rays: slab and distance reductions as three-input min / max
-#endif
 __device__ __forceinline__ float max3f(float a, float b, float c) {
   float d;
   asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
@@ -810,8 +804,8 @@ __device__ __forceinline__ float min3f(float a, float b, float c) {
   asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
   return d;
 }
-// FAST: 0 divides where RayPre::fast does not hold, 1 uses div_fast, 2 tests RayPre::fast per division.
-template <int FAST>
+// FAST: RayPre::fast holds (quotients by div_fast), else IEEE division.
+template <bool FAST>
 __device__ __forceinline__ bool child_tests(const float* b, const RayPre& R, float& dist, float& N, float& F) {
   float d[6];
 #pragma unroll
@@ -819,7 +813,7 @@ __device__ __forceinline__ bool child_tests(const float* b, const RayPre& R, flo
     d[2 * a] = b[2 * a] - comp(R.o, a);
     d[2 * a + 1] = b[2 * a + 1] - comp(R.o, a);
   }
-  if (FAST == 1 && CLV_MINMAX3) {
+  if (FAST) {
     // Under RayPre::fast every difference is finite and every reciprocal finite
     // and non-zero, so no slab value or quotient is NaN: the reference's
     // compare-and-swap ordering and its chained fmin/fmax reduce to plain
@@ -854,7 +848,7 @@ __device__ __forceinline__ bool child_tests(const float* b, const RayPre& R, flo
 #pragma unroll
   for (int k = 0; k < 6; ++k) {
     const int a = k >> 1;
-    q[k] = FAST == 2 ? divc(R, d[k], a) : (FAST ? div_fast(d[k], comp(R.d, a), comp(R.inv, a)) : d[k] / comp(R.d, a));
+    q[k] = d[k] / comp(R.d, a);
   }
   const float tx1 = q[0], tx2 = q[1];
   float tmin = fminf(tx1, tx2), tmax = fmaxf(tx1, tx2);
@@ -915,20 +909,15 @@ __device__ __forceinline__ bool trav_step(const ClvDeviceScene& S, const Ray& r,
       const uint32_t L = __float_as_uint(q3.x), Rr = __float_as_uint(q3.y);
       uint32_t next = CLV_REF_EMPTY;
       bool left_next = true;
-      if (CLV_NODE_FUSED && !wt_on<WT>(S)) {
+      if (!wt_on<WT>(S)) {
         float ld, rd, NL, FL, NR, FR;
         bool lh, rh;
-        if (CLV_NODE_FUSED == 2) {
-          if (R.fast) {
-            lh = child_tests<1>(lb, R, ld, NL, FL);
-            rh = child_tests<1>(rb, R, rd, NR, FR);
-          } else {
-            lh = child_tests<0>(lb, R, ld, NL, FL);
-            rh = child_tests<0>(rb, R, rd, NR, FR);
-          }
+        if (R.fast) {  // one branch per node on the division form
+          lh = child_tests<true>(lb, R, ld, NL, FL);
+          rh = child_tests<true>(rb, R, rd, NR, FR);
         } else {
-          lh = child_tests<2>(lb, R, ld, NL, FL);
-          rh = child_tests<2>(rb, R, rd, NR, FR);
+          lh = child_tests<false>(lb, R, ld, NL, FL);
+          rh = child_tests<false>(rb, R, rd, NR, FR);
         }
         const bool both = L != CLV_REF_EMPTY && Rr != CLV_REF_EMPTY;
         if (both && lh && rh) {
@@ -1037,16 +1026,12 @@ __device__ bool closest_hit(const ClvDeviceScene& S, const Ray& r, float tmin, f
   return closest_hit_stk<CPLX, WT>(S, r, tmin, tmax, rng, hit, full, cnt, err, stack);
 }
 
-#ifndef CLV_WARP_SCHED
-#define CLV_WARP_SCHED 1  // 0: off; 1: chain leaves wait for the warp; 2: one step class per turn; 3: leaves wait for nodes
-#endif
-
 // closest_hit for the 32 lanes of a warp together (every lane calls it; `go`
 // is false for lanes without a ray).  Each turn, the warp chooses which of its
 // traversing lanes take their next step; the others wait.  A wrapper-chain
-// leaf (CPLX 1 and 2) costs several primitive tests and transforms, so under
-// scheme 1 a lane whose next step is one waits until every traversing lane of
-// the warp is at one, and the leaf then runs once for all of them.  Every lane
+// leaf (CPLX 1 and 2) costs several primitive tests and transforms, so a lane
+// whose next step is one waits until every traversing lane of the warp is at
+// one, and the leaf then runs once for all of them.  Every lane
 // still makes exactly closest_hit's sequence of node visits and leaf tests,
 // only later in time, so hits and counts are unchanged.
 template <int CPLX, int WT>
@@ -1062,22 +1047,9 @@ __device__ __forceinline__ bool closest_hit_warp(const ClvDeviceScene& S, const 
   for (;;) {
     const unsigned act = __ballot_sync(0xFFFFFFFFu, active);
     if (act == 0u) break;
-    const uint32_t kind = CLV_REF_KIND(T.ref);
-    bool run;
-    if (CLV_WARP_SCHED == 2) {
-      const unsigned nodes = __ballot_sync(0xFFFFFFFFu, active && kind == CLV_REF_NODE);
-      const unsigned chains = __ballot_sync(0xFFFFFFFFu, active && kind == CLV_REF_OBJ);
-      const unsigned prims = act & ~nodes & ~chains;
-      const unsigned turn = nodes ? nodes : (prims ? prims : chains);
-      run = (turn >> (threadIdx.x & 31)) & 1u;
-    } else if (CLV_WARP_SCHED == 3) {
-      const unsigned nodes = __ballot_sync(0xFFFFFFFFu, active && kind == CLV_REF_NODE);
-      run = active && (kind == CLV_REF_NODE || nodes == 0u);
-    } else {
-      const unsigned chains = __ballot_sync(0xFFFFFFFFu, active && kind == CLV_REF_OBJ);
-      run = active && (kind != CLV_REF_OBJ || chains == act);
-    }
-    if (run) active = trav_step<CPLX, WT>(S, r, T, stack, rng, hit, full, cnt, err);
+    const bool at_chain = active && CLV_REF_KIND(T.ref) == CLV_REF_OBJ;
+    const unsigned chains = __ballot_sync(0xFFFFFFFFu, at_chain);
+    if (active && (!at_chain || chains == act)) active = trav_step<CPLX, WT>(S, r, T, stack, rng, hit, full, cnt, err);
   }
   return go && T.found;
 }

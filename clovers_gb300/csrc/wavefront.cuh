@@ -150,27 +150,11 @@ __device__ __forceinline__ void warp_add_counts(unsigned long long* cnt, uint32_
   }
 }
 
-// Appends slot i to queue `cls`: lanes with the same class are grouped with
-// __match_any_sync and each group reserves its slots with one atomic.
-__device__ __forceinline__ void wf_enqueue(const WfState& W, WfCounters* C, int cls, uint32_t i) {
-  const unsigned active = __activemask();
-  const unsigned peers = __match_any_sync(active, cls);
-  const int lane = threadIdx.x & 31;
-  const int leader = __ffs(peers) - 1;
-  unsigned base = 0;
-  if (lane == leader) base = atomicAdd(&C->queue[cls], (unsigned)__popc(peers));
-  base = __shfl_sync(peers, base, leader);
-  W.queue[(size_t)cls * W.Q + base + __popc(peers & ((1u << lane) - 1u))] = i;
-}
-
 #ifndef CLV_MINB_SHADE
 #define CLV_MINB_SHADE 8  // resident blocks per SM asked of the shading kernels (64 registers)
 #endif
 #ifndef CLV_MINB_GUIDE
 #define CLV_MINB_GUIDE CLV_MINB_SHADE  // the same for the guided bounce kernels
-#endif
-#ifndef CLV_BLOCK_ATOMICS
-#define CLV_BLOCK_ATOMICS 1  // queue, work and live counters reserved once per block (1) or per warp (0)
 #endif
 // Appends each thread's slot i to queue `cls` (cls < 0: nothing) with one
 // atomic per class for the whole block; every thread of the 128-thread block
@@ -239,7 +223,7 @@ __device__ __forceinline__ int material_class(const ClvDeviceScene& S, uint32_t 
 template <int CPLX, bool COUNT, int WT>
 __device__ __forceinline__ int intersect_slot(const ClvDeviceScene& S, const WfState& W, uint32_t* err, uint32_t i,
                                               const uint4& m, bool go, Counters& c) {
-  constexpr bool WARP = CLV_WARP_SCHED > 0 && CPLX > 0;
+  constexpr bool WARP = CPLX > 0;
   if (!WARP && !go) return -1;
   Ray r{mk(0.0f, 0.0f, 0.0f), mk(0.0f, 0.0f, 1.0f), 0.0f, 0};
   if (go) {
@@ -299,8 +283,7 @@ __global__ void __launch_bounds__(128, CLV_MINB) wf_intersect(ClvDeviceScene S, 
   int cls;
   if constexpr (BATCH) cls = intersect_slot<CPLX, COUNT, WT>(B.scenes[go ? m.w >> 8 : 0u], W, err, i, m, go, c);
   else cls = intersect_slot<CPLX, COUNT, WT>(S, W, err, i, m, go, c);
-  if (CLV_BLOCK_ATOMICS) wf_enqueue_block(W, C, cls, i);
-  else if (cls >= 0) wf_enqueue(W, C, cls, i);
+  wf_enqueue_block(W, C, cls, i);
   if (COUNT) warp_add_counts(cnt, live, c.nodes, c.prims);
 }
 
@@ -365,7 +348,6 @@ __device__ __forceinline__ bool wf_advance(const WfParams& P, const WfState& W, 
   const uint32_t depth = p.meta.y + 1;
   if (depth > P.max_depth) {  // trace at depth > max_depth returns 0
     W.meta[i].z = p.rng.counter;
-    if (!CLV_BLOCK_ATOMICS) wf_enqueue(W, C, WF_Q_FINISH, i);
     return false;
   }
   W.o_time[i] = make_float4(origin.x, origin.y, origin.z, p.ray.time);
@@ -373,10 +355,6 @@ __device__ __forceinline__ bool wf_advance(const WfParams& P, const WfState& W, 
   W.beta[i] = make_float4(p.beta[0], p.beta[1], p.beta[2], p.beta[3]);
   W.meta[i] = make_uint4(p.meta.x, depth, p.rng.counter, (p.meta.w & ~0xFFu) | 1u);
   return true;
-}
-__device__ __forceinline__ void wf_count_live(WfCounters* C, bool live) {
-  const unsigned lm = __ballot_sync(0xFFFFFFFFu, live);
-  if ((threadIdx.x & 31) == 0 && lm) atomicAdd(&C->live, (unsigned)__popc(lm));
 }
 
 // Specular bounce: Metal (metal.rs:27-51), Dielectric / Dispersive (dielectric.rs:37-81, dispersive.rs:58-123)
@@ -431,11 +409,10 @@ __global__ void __launch_bounds__(128, CLV_MINB_SHADE) wf_shade_specular(ClvDevi
         live = specular_slot(S, P, W, C, i);
       }
     }
-    if (CLV_BLOCK_ATOMICS) wf_enqueue_block_one(W, C, WF_Q_FINISH, q < n && !live, i);
-    if (CLV_BLOCK_ATOMICS) nlive += live ? 1u : 0u;
-    else wf_count_live(C, live);
+    wf_enqueue_block_one(W, C, WF_Q_FINISH, q < n && !live, i);
+    nlive += live ? 1u : 0u;
   }
-  if (CLV_BLOCK_ATOMICS) wf_add_live(C, nlive);
+  wf_add_live(C, nlive);
 }
 
 // Diffuse bounce: MixturePDF(HitablePDF(priority tree), Cosine/SpherePDF), pdf.rs:122-140, trace.rs:80-119
@@ -482,7 +459,6 @@ __device__ __forceinline__ bool diffuse_slot(const ClvDeviceScene& S, const WfPa
   }
   if (!scatter) {
     W.meta[i].z = p.rng.counter;
-    if (!CLV_BLOCK_ATOMICS) wf_enqueue(W, C, WF_Q_FINISH, i);
     return false;
   }
   float atten[4];
@@ -513,11 +489,10 @@ __global__ void __launch_bounds__(128, CLV_MINB_SHADE) wf_shade_diffuse(ClvDevic
         live = diffuse_slot(S, P, W, C, err, i);
       }
     }
-    if (CLV_BLOCK_ATOMICS) wf_enqueue_block_one(W, C, WF_Q_FINISH, q < n && !live, i);
-    if (CLV_BLOCK_ATOMICS) nlive += live ? 1u : 0u;
-    else wf_count_live(C, live);
+    wf_enqueue_block_one(W, C, WF_Q_FINISH, q < n && !live, i);
+    nlive += live ? 1u : 0u;
   }
-  if (CLV_BLOCK_ATOMICS) wf_add_live(C, nlive);
+  wf_add_live(C, nlive);
 }
 
 // ---- guided Lambertian bounces: pre -> guide network (guide.cu) -> post ----
@@ -626,7 +601,6 @@ __device__ __forceinline__ bool guide_post_slot(const ClvDeviceScene& S, const W
     }
   }
   if (cs < 0.0f) {  // Lambertian::scattering_pdf is None below the surface
-    if (!CLV_BLOCK_ATOMICS) wf_enqueue(W, C, WF_Q_FINISH, i);
     return false;
   }
   const float spdf = cs / CLV_PI;
@@ -650,11 +624,10 @@ __global__ void __launch_bounds__(128, CLV_MINB_GUIDE) wf_guide_post(ClvDeviceSc
     bool live = false;
     const uint32_t i = q < n ? W.queue[(size_t)WF_Q_GUIDE * W.Q + q] : 0u;
     if (q < n) live = guide_post_slot(S, P, W, C, err, G, i);
-    if (CLV_BLOCK_ATOMICS) wf_enqueue_block_one(W, C, WF_Q_FINISH, q < n && !live, i);
-    if (CLV_BLOCK_ATOMICS) nlive += live ? 1u : 0u;
-    else wf_count_live(C, live);
+    wf_enqueue_block_one(W, C, WF_Q_FINISH, q < n && !live, i);
+    nlive += live ? 1u : 0u;
   }
-  if (CLV_BLOCK_ATOMICS) wf_add_live(C, nlive);
+  wf_add_live(C, nlive);
 }
 
 // film rule of draw_cpu.rs:131-142, deposited as f64 sums
@@ -749,7 +722,7 @@ __global__ void __launch_bounds__(128, CLV_MINB_SHADE) wf_finish(ClvDeviceScene 
     bool live = false;
     const int lane = threadIdx.x & 31;
     unsigned long long base = 0;
-    if (CLV_BLOCK_ATOMICS) {  // one reservation of work items for the block
+    {  // one reservation of work items for the block
       __shared__ uint32_t wcnt[4];
       __shared__ unsigned long long wbase;
       const int warp = threadIdx.x >> 5;
@@ -765,10 +738,6 @@ __global__ void __launch_bounds__(128, CLV_MINB_SHADE) wf_finish(ClvDeviceScene 
       __syncthreads();
       if (total) base = wbase + before;
       __syncthreads();  // wcnt and wbase are rewritten next round
-    } else if (mask) {
-      const int leader = __ffs(mask) - 1;
-      if (lane == leader) base = atomicAdd(&C->next_work, (unsigned long long)__popc(mask));
-      base = __shfl_sync(0xFFFFFFFFu, base, leader);
     }
     if (mask) {
       if (need) {
@@ -791,10 +760,9 @@ __global__ void __launch_bounds__(128, CLV_MINB_SHADE) wf_finish(ClvDeviceScene 
         }
       }
     }
-    if (CLV_BLOCK_ATOMICS) nlive += live ? 1u : 0u;
-    else wf_count_live(C, live);
+    nlive += live ? 1u : 0u;
   }
-  if (CLV_BLOCK_ATOMICS) wf_add_live(C, nlive);
+  wf_add_live(C, nlive);
 }
 
 }  // namespace clvd
