@@ -471,19 +471,23 @@ __device__ __forceinline__ V chain_dir(const ClvDeviceScene& S, uint32_t ref, V 
   }
   return d;
 }
-template <int WT = CLV_WT_SCENE>
-__device__ __forceinline__ int chain_hit(const ClvDeviceScene& S, uint32_t top, const Ray& r0, float tmin, float tmax,
-                                         Rec& rec, Counters* cnt) {
-  int n = 0;
-  Ray r = r0;
-  uint32_t ref = top;
+// The ray below a chain's wrappers: Translate moves the origin, RotateY
+// rotates origin and direction and renormalises the direction (rotate.rs:104-
+// 126).  Returns false for chains the inline form does not take (too deep, or
+// ending in a list or a medium); otherwise r, the terminal ref and the number
+// of wrappers n.
+__device__ __forceinline__ bool chain_walk(const ClvDeviceScene& S, uint32_t top, const Ray& r0, Ray& r,
+                                           uint32_t& ref, int& n) {
+  n = 0;
+  r = r0;
+  ref = top;
   while (CLV_REF_KIND(ref) == CLV_REF_OBJ) {
     const ClvObj& o = S.objs[CLV_REF_INDEX(ref)];
     if (o.kind == CLV_OBJ_TRANSLATE) {
-      if (n == CLV_CHAIN) return 2;
+      if (n == CLV_CHAIN) return false;
       r.o = sub(r.o, mk(o.p[0], o.p[1], o.p[2]));
     } else if (o.kind == CLV_OBJ_ROTATEY) {
-      if (n == CLV_CHAIN) return 2;
+      if (n == CLV_CHAIN) return false;
       const float sn = o.p[0], cs = o.p[1];
       V ro = r.o, rd = r.d;
       ro.x = cs * r.o.x - sn * r.o.z;
@@ -495,11 +499,24 @@ __device__ __forceinline__ int chain_hit(const ClvDeviceScene& S, uint32_t top, 
     } else if (o.kind == CLV_OBJ_BOXY || o.kind == CLV_OBJ_MOVING) {
       break;
     } else {
-      return 2;
+      return false;
     }
     ++n;
     ref = o.a;
   }
+  return true;
+}
+// The record of a hit below n wrappers brought back to the frame of `top`:
+// the wrappers' inverse transforms from the innermost out, each setting the
+// face against the ray direction as seen at its level.
+__device__ __forceinline__ void chain_unwind(const ClvDeviceScene& S, uint32_t top, const Ray& r0, int n, Rec& rec);
+template <int WT = CLV_WT_SCENE>
+__device__ __forceinline__ int chain_hit(const ClvDeviceScene& S, uint32_t top, const Ray& r0, float tmin, float tmax,
+                                         Rec& rec, Counters* cnt) {
+  int n;
+  Ray r;
+  uint32_t ref;
+  if (!chain_walk(S, top, r0, r, ref, n)) return 2;
   // terminal
   const uint32_t kind = CLV_REF_KIND(ref), idx = CLV_REF_INDEX(ref);
   bool any = false;
@@ -551,6 +568,10 @@ __device__ __forceinline__ int chain_hit(const ClvDeviceScene& S, uint32_t top, 
     return 2;
   }
   if (!any) return 0;
+  chain_unwind(S, top, r0, n, rec);
+  return 1;
+}
+__device__ __forceinline__ void chain_unwind(const ClvDeviceScene& S, uint32_t top, const Ray& r0, int n, Rec& rec) {
   for (int l = n - 1; l >= 0; --l) {
     uint32_t wr = top;
     for (int j = 0; j < l; ++j) wr = S.objs[CLV_REF_INDEX(wr)].a;
@@ -575,7 +596,6 @@ __device__ __forceinline__ int chain_hit(const ClvDeviceScene& S, uint32_t top, 
       rec.n = rec.front ? un : neg(un);
     }
   }
-  return 1;
 }
 
 // A compound BVH leaf, out of line so the traversal loop stays small.
@@ -891,6 +911,33 @@ __device__ __forceinline__ void trav_begin(const ClvDeviceScene& S, const Ray& r
   else slab(S.root_box, r.o, T.R.inv, T.N, T.F);
   T.found = false;
 }
+// Pops the next deferred far child whose visit the reference would make;
+// false when the traversal is over.
+template <class STK>
+__device__ __forceinline__ bool trav_pop(Trav& T, STK& stack, const Hit& hit) {
+  while (T.sp > 0) {
+    --T.sp;
+    const float4 e = st_get(stack, T.sp);
+    const bool near_hit = T.sp < T.marked;
+    if (T.marked > T.sp) T.marked = T.sp;
+    if (near_hit && hit.t < e.y) continue;  // near subtree's hit is closer than the far box
+    T.ref = __float_as_uint(e.x);
+    T.N = e.z;
+    T.F = e.w;
+    return true;
+  }
+  return false;
+}
+// After a leaf test (found: the leaf produced the new closest hit in `hit`).
+template <class STK>
+__device__ __forceinline__ bool trav_leaf_done(Trav& T, STK& stack, const Hit& hit, bool found) {
+  if (found) {
+    T.tmax = hit.t;
+    T.found = true;
+    T.marked = T.sp;
+  }
+  return trav_pop(T, stack, hit);
+}
 // One node visit or leaf test, then the next reference (descend, or pop the
 // next deferred far child whose visit the reference would make).  Returns
 // false when the traversal is over (result in hit / T.found).
@@ -987,26 +1034,9 @@ __device__ __forceinline__ bool trav_step(const ClvDeviceScene& S, const Ray& r,
         return true;
       }
     }
-  } else {
-    if (leaf_test<CPLX, WT>(S, ref, r, T.tmin, T.tmax, rng, hit, full, cnt, err)) {
-      T.tmax = hit.t;
-      T.found = true;
-      T.marked = T.sp;
-    }
+    return trav_pop(T, stack, hit);
   }
-  // pop the next deferred far child whose visit the reference would make
-  while (T.sp > 0) {
-    --T.sp;
-    const float4 e = st_get(stack, T.sp);
-    const bool near_hit = T.sp < T.marked;
-    if (T.marked > T.sp) T.marked = T.sp;
-    if (near_hit && hit.t < e.y) continue;  // near subtree's hit is closer than the far box
-    T.ref = __float_as_uint(e.x);
-    T.N = e.z;
-    T.F = e.w;
-    return true;
-  }
-  return false;
+  return trav_leaf_done(T, stack, hit, leaf_test<CPLX, WT>(S, ref, r, T.tmin, T.tmax, rng, hit, full, cnt, err));
 }
 // closest_hit with a caller-provided stack (a local array or a HybridStack)
 template <int CPLX, int WT, class STK>
