@@ -95,7 +95,7 @@ int clv_scene_from_mesh(const float* verts, uint32_t nverts, const uint32_t* ind
                         clv_scene** out);
 
 /* Scene options, set before clv_scene_upload.  No counterpart in the
- * reference (the benchmark spec's precision item).
+ * reference (an opt-in precision mode).
  * CLV_OPT_WATERTIGHT 1: triangles use the watertight test of Woop, Benthin
  * and Wald 2013 (shear-frame edge functions, double-precision fallback on a
  * zero edge function) on their vertices as given, so rays through shared
@@ -162,8 +162,8 @@ int clv_resolve_device(const double* film_dev, uint32_t width, uint32_t height, 
 /* Host variant of the resolve for XYZ(E) means already on the host. */
 int clv_resolve_srgb(const float* xyz, uint32_t width, uint32_t height, uint8_t* rgb_out);
 
-/* Wavefront shape tuning (no counterpart in the reference; north star
- * pattern (2)).  Renders `opts` -- pass a short render, a few samples per
+/* Wavefront shape tuning (no counterpart in the reference; part of the
+ * batching and autotuning layer).  Renders `opts` -- pass a short render, a few samples per
  * pixel of the workload to tune for -- twice for each candidate shape: paths
  * in flight (path_slots) SMs x {1, 2, 4, 8, 16} x 1024 and shading grids of
  * {8, 16, 32} blocks per SM, and keeps the fastest in the scene: later

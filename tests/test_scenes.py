@@ -18,7 +18,7 @@ import clovers_gb300 as cg
 import oracle
 from clovers_gb300 import scenes
 
-REFERENCE = "/root/reference"
+REFERENCE = os.environ.get("CLOVERS_REFERENCE", "/root/reference")  # where the reference's files are read
 
 
 @pytest.fixture(scope="module")
