@@ -802,7 +802,8 @@ int clv_memset(void* dst, int value, uint64_t bytes) {
 }
 
 static int render_wavefront(clv_device_scene* d, const clv_render_opts* o, double* film, cudaStream_t st,
-                            clv_render_profile* prof, clv_guide* guide = nullptr, float alpha = 0.0f);
+                            clv_render_profile* prof, clv_guide* guide = nullptr, float alpha = 0.0f,
+                            bool count = true);
 
 int clv_render_profile_run(clv_device_scene* d, const clv_render_opts* o, double* film_dev, void* stream,
                            clv_render_profile* out) {
@@ -811,7 +812,28 @@ int clv_render_profile_run(clv_device_scene* d, const clv_render_opts* o, double
   if (!film_dev || !out) return fail(CLV_E_INVALID, "null argument");
   if (o->mode != CLV_MODE_PATH_TRACING || o->engine != 0)
     return fail(CLV_E_INVALID, "profiling covers the wavefront path tracer only");
-  return render_wavefront(d, o, film_dev, (cudaStream_t)stream, out);
+  // device times of the production kernels ...
+  rc = render_wavefront(d, o, film_dev, (cudaStream_t)stream, out, nullptr, 0.0f, false);
+  if (rc) return rc;
+  // ... and the traversal counts from the same render with the counting kernels, into a scratch film
+  double* scratch = nullptr;
+  try {
+    ck(cudaMalloc(&scratch, (size_t)o->width * o->height * 3 * sizeof(double)), "cudaMalloc");
+    ck(cudaMemsetAsync(scratch, 0, (size_t)o->width * o->height * 3 * sizeof(double), (cudaStream_t)stream),
+       "cudaMemsetAsync");
+  } catch (std::exception& e) {
+    if (scratch) cudaFree(scratch);
+    return fail(CLV_E_CUDA, e.what());
+  }
+  clv_render_profile counted{};
+  rc = render_wavefront(d, o, scratch, (cudaStream_t)stream, &counted, nullptr, 0.0f, true);
+  cudaStreamSynchronize((cudaStream_t)stream);
+  cudaFree(scratch);
+  if (rc) return rc;
+  out->path_segments = counted.path_segments;
+  out->node_visits = counted.node_visits;
+  out->prim_tests = counted.prim_tests;
+  return CLV_OK;
 }
 
 // Times the wavefront render `o` (a short one: a few samples per pixel) for
@@ -1150,11 +1172,14 @@ int clv_raycast(clv_device_scene* d, const float* rays, uint64_t n, uint32_t* pr
 }
 
 // Wavefront render loop.  With `prof` set, each intersect and shade launch is
+// bracketed by events, and with `count` as well the intersect launches are the
+// counting variants that also fill prof's traversal counts.  (The counting
+// variants are slower, so device times come from a render without them.)
 // bracketed by events and the traversal work is counted (diagnostic runs).
 // With `guide` set, Lambertian bounces go through the guided kernels (a share
 // alpha drawn from the guide network) and leave training records.
 static int render_wavefront(clv_device_scene* d, const clv_render_opts* o, double* film, cudaStream_t st,
-                            clv_render_profile* prof, clv_guide* guide, float alpha) {
+                            clv_render_profile* prof, clv_guide* guide, float alpha, bool count) {
   std::vector<cudaEvent_t> evs;
   unsigned long long* dcnt = nullptr;
   auto cleanup = [&]() {
@@ -1220,7 +1245,7 @@ static int render_wavefront(clv_device_scene* d, const clv_render_opts* o, doubl
       if (prof) cudaEventRecord(evs[4 * k], s);
 #define CLV_ISECT(L, N, T) \
   wf_intersect<L, N, false, T><<<grid, block, 0, s>>>(d->view, W, C, d->err, N ? dcnt : nullptr, WfBatch{}, -1)
-      switch ((level * 2 + (prof ? 1 : 0)) * 2 + (d->view.watertight ? 1 : 0)) {
+      switch ((level * 2 + (prof && count ? 1 : 0)) * 2 + (d->view.watertight ? 1 : 0)) {
         case 0: CLV_ISECT(0, false, CLV_WT_OFF); break;
         case 1: CLV_ISECT(0, false, CLV_WT_ON); break;
         case 2: CLV_ISECT(0, true, CLV_WT_OFF); break;
@@ -1284,9 +1309,11 @@ static int render_wavefront(clv_device_scene* d, const clv_render_opts* o, doubl
     if (prof) {
       unsigned long long h[3];
       ck(cudaMemcpy(h, dcnt, sizeof h, cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
-      prof->path_segments = h[0];
-      prof->node_visits = h[1];
-      prof->prim_tests = h[2];
+      if (count) {
+        prof->path_segments = h[0];
+        prof->node_visits = h[1];
+        prof->prim_tests = h[2];
+      }
       prof->paths = P.total;
       prof->path_slots = q;
     }

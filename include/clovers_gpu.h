@@ -274,7 +274,10 @@ uint64_t clv_kernel_launches(void);
 
 /* ---- diagnostics (no counterpart in the reference) ----------------------- */
 
-/* One wavefront render with per-kernel device times and traversal counts. */
+/* One wavefront render with per-kernel device times and traversal counts.
+ * The times are those of the production kernels; the counts come from a
+ * second render of the same samples with the counting kernels (into scratch
+ * memory, so film_dev holds one render). */
 typedef struct clv_render_profile {
   double ms_init, ms_intersect, ms_shade;  /* summed device time per kernel type */
   uint64_t intersect_launches, shade_launches;

@@ -119,3 +119,31 @@ def test_draw_distributed_single_rank_equals_draw(box_scene_path):
     a = cg.draw(cg.GlobalOptions(quiet=True), opts, d)
     b = draw_distributed(cg.GlobalOptions(quiet=True), opts, d)
     assert np.allclose(a, b, rtol=1e-5, atol=1e-9)
+
+
+def test_profile_run_times_and_counts(box_scene_path):
+    """clv_render_profile_run: the film holds one render (the plain render's
+    film), the device times are the production kernels', and the traversal
+    counts (from a second, counting render of the same samples) are the same
+    on every call."""
+    import ctypes
+    from clovers_gb300 import _lib
+    w = h = 64
+    d = cg.Scene.from_json(box_scene_path, w, h).upload()
+    o = cg.RenderOptions(width=w, height=h, samples=16, max_depth=8, seed=11)
+    plain = cg.DeviceBuffer(w * h * 3 * 8).zero()
+    _lib.check(_lib.lib().clv_render_device(d.handle, ctypes.byref(cg.render_opts(o)), plain.ptr, None))
+    runs = []
+    for _ in range(2):
+        film = cg.DeviceBuffer(w * h * 3 * 8).zero()
+        prof = _lib.RenderProfileC()
+        _lib.check(_lib.lib().clv_render_profile_run(d.handle, ctypes.byref(cg.render_opts(o)), film.ptr, None,
+                                                     ctypes.byref(prof)))
+        img = film.to_numpy(np.float64, (w * h, 3))
+        assert np.allclose(img, plain.to_numpy(np.float64, (w * h, 3)), rtol=1e-9, atol=1e-12)
+        runs.append((prof.path_segments, prof.node_visits, prof.prim_tests))
+        assert prof.paths == w * h * 16 and prof.path_segments >= prof.paths
+        assert prof.node_visits > prof.path_segments and prof.prim_tests > 0
+        assert prof.ms_intersect > 0 and prof.ms_shade > 0 and prof.intersect_launches > 0
+    assert runs[0] == runs[1]
+    assert d.status() == 0
