@@ -911,33 +911,6 @@ __device__ __forceinline__ void trav_begin(const ClvDeviceScene& S, const Ray& r
   else slab(S.root_box, r.o, T.R.inv, T.N, T.F);
   T.found = false;
 }
-// Pops the next deferred far child whose visit the reference would make;
-// false when the traversal is over.
-template <class STK>
-__device__ __forceinline__ bool trav_pop(Trav& T, STK& stack, const Hit& hit) {
-  while (T.sp > 0) {
-    --T.sp;
-    const float4 e = st_get(stack, T.sp);
-    const bool near_hit = T.sp < T.marked;
-    if (T.marked > T.sp) T.marked = T.sp;
-    if (near_hit && hit.t < e.y) continue;  // near subtree's hit is closer than the far box
-    T.ref = __float_as_uint(e.x);
-    T.N = e.z;
-    T.F = e.w;
-    return true;
-  }
-  return false;
-}
-// After a leaf test (found: the leaf produced the new closest hit in `hit`).
-template <class STK>
-__device__ __forceinline__ bool trav_leaf_done(Trav& T, STK& stack, const Hit& hit, bool found) {
-  if (found) {
-    T.tmax = hit.t;
-    T.found = true;
-    T.marked = T.sp;
-  }
-  return trav_pop(T, stack, hit);
-}
 // One node visit or leaf test, then the next reference (descend, or pop the
 // next deferred far child whose visit the reference would make).  Returns
 // false when the traversal is over (result in hit / T.found).
@@ -1034,9 +1007,26 @@ __device__ __forceinline__ bool trav_step(const ClvDeviceScene& S, const Ray& r,
         return true;
       }
     }
-    return trav_pop(T, stack, hit);
+  } else {
+    if (leaf_test<CPLX, WT>(S, ref, r, T.tmin, T.tmax, rng, hit, full, cnt, err)) {
+      T.tmax = hit.t;
+      T.found = true;
+      T.marked = T.sp;
+    }
   }
-  return trav_leaf_done(T, stack, hit, leaf_test<CPLX, WT>(S, ref, r, T.tmin, T.tmax, rng, hit, full, cnt, err));
+  // pop the next deferred far child whose visit the reference would make
+  while (T.sp > 0) {
+    --T.sp;
+    const float4 e = st_get(stack, T.sp);
+    const bool near_hit = T.sp < T.marked;
+    if (T.marked > T.sp) T.marked = T.sp;
+    if (near_hit && hit.t < e.y) continue;  // near subtree's hit is closer than the far box
+    T.ref = __float_as_uint(e.x);
+    T.N = e.z;
+    T.F = e.w;
+    return true;
+  }
+  return false;
 }
 // closest_hit with a caller-provided stack (a local array or a HybridStack)
 template <int CPLX, int WT, class STK>
