@@ -809,11 +809,7 @@ __device__ __forceinline__ float4 st_get(HybridStack<SH>& s, int i) {
   return i < SH ? s.sh[i * 128] : s.loc[i - SH];
 }
 
-// Both tests the traversal makes of one child box, from one set of
-// differences d = bound - origin (the same f32 values that AABB::distance and
-// AABB::hit each compute): the slab interval (N, F) of the child's own
-// AABB::hit, made when the child is visited, and its entry distance
-// (AABB::distance, the quotients d / direction).
+// Three-input f32 max / min (NaN inputs ignored, as fmaxf / fminf do).
 __device__ __forceinline__ float max3f(float a, float b, float c) {
   float d;
   asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
@@ -824,7 +820,12 @@ __device__ __forceinline__ float min3f(float a, float b, float c) {
   asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
   return d;
 }
-// FAST: RayPre::fast holds (quotients by div_fast), else IEEE division.
+// Both tests the traversal makes of one child box, from one set of
+// differences d = bound - origin (the same f32 values that AABB::distance and
+// AABB::hit each compute): the slab interval (N, F) of the child's own
+// AABB::hit, made when the child is visited, and its entry distance
+// (AABB::distance, the quotients d / direction).  FAST: RayPre::fast holds
+// (quotients by div_fast), else IEEE division.
 template <bool FAST>
 __device__ __forceinline__ bool child_tests(const float* b, const RayPre& R, float& dist, float& N, float& F) {
   float d[6];
