@@ -327,12 +327,19 @@ def draw_guided(global_options: GlobalOptions, render_options: RenderOptions, sc
     return (film.to_numpy(np.float64, (w * h, 3)) / spp).astype(np.float32)
 
 
-def raycast(scene: DeviceScene, rays, with_counts=False):
-    """Closest hits of rays (n, 8) = {ox,oy,oz,tmin,dx,dy,dz,tmax}: (prim_id u32, t f32[, nodes, tests])."""
+def raycast(scene: DeviceScene, rays, with_counts=False, out=None):
+    """Closest hits of rays (n, 8) = {ox,oy,oz,tmin,dx,dy,dz,tmax}: (prim_id u32, t f32[, nodes, tests]).
+    `out` = (prim, t): arrays of n u32 / f32 to fill instead of new ones (repeated casts reuse them)."""
     r = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 8)
     n = r.shape[0]
-    prim = np.empty(n, np.uint32)
-    t = np.empty(n, np.float32)
+    if out is not None:
+        prim, t = out
+        if prim.dtype != np.uint32 or t.dtype != np.float32 or prim.size != n or t.size != n or \
+                not (prim.flags.c_contiguous and t.flags.c_contiguous):
+            raise ValueError("out must be contiguous u32 and f32 arrays of one entry per ray")
+    else:
+        prim = np.empty(n, np.uint32)
+        t = np.empty(n, np.float32)
     nodes = np.empty(n, np.uint32) if with_counts else None
     tests = np.empty(n, np.uint32) if with_counts else None
     check(lib().clv_raycast(scene.handle, r.ctypes.data, n, prim.ctypes.data, t.ctypes.data,

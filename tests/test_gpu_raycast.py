@@ -147,3 +147,21 @@ def test_watertight_mode_parity_and_no_leaks(rotate):
     rays2[:, :3] = rays2[:, :3] * 3.0 - 1.5
     _compare(dscene, oracle.Scene.from_mesh(v, f).set_watertight(), rays2)
     _compare(cg.Scene.from_mesh(v, f).upload(), oracle.Scene.from_mesh(v, f), rays2)
+
+
+def test_raycast_into_caller_arrays():
+    """Repeated host-buffer casts can reuse their output arrays: the same ids
+    and distances as fresh arrays; arrays of the wrong type or size are refused."""
+    v, idx = scenes.triangle_soup(4096, seed=7)
+    d = cg.Scene.from_mesh(v, idx).upload()
+    rays = scenes.random_rays(20000, seed=8)
+    prim, t = cg.raycast(d, rays)
+    out = (np.full(len(rays), 7, np.uint32), np.full(len(rays), -1.0, np.float32))
+    for _ in range(2):
+        p2, t2 = cg.raycast(d, rays, out=out)
+        assert p2 is out[0] and t2 is out[1]
+        assert np.array_equal(p2, prim) and np.array_equal(t2, t)
+    with pytest.raises(ValueError):
+        cg.raycast(d, rays, out=(np.empty(len(rays), np.int64), np.empty(len(rays), np.float32)))
+    with pytest.raises(ValueError):
+        cg.raycast(d, rays, out=(np.empty(len(rays) - 1, np.uint32), np.empty(len(rays), np.float32)))
