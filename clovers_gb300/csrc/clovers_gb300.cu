@@ -509,15 +509,42 @@ void ck(cudaError_t e, const char* what) {
   if (e != cudaSuccess) throw CudaError(std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-template <class T>
-T* upload(const std::vector<T>& v, std::vector<void*>& owned) {
-  if (v.empty()) return nullptr;
-  void* p = nullptr;
-  ck(cudaMalloc(&p, v.size() * sizeof(T)), "cudaMalloc");
-  owned.push_back(p);
-  ck(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice), "cudaMemcpy H2D");
-  return static_cast<T*>(p);
-}
+// A scene's device arrays in one allocation: `add` records each array at a
+// 256-byte aligned offset, `commit` allocates once and copies every array
+// straight from its host vector, with one synchronisation at the end.
+struct UploadPack {
+  struct Item {
+    const void* src;
+    size_t bytes, offset;
+    const void** dst;
+  };
+  std::vector<Item> items;
+  size_t total = 0;
+  template <class T>
+  void add(const std::vector<T>& v, const T** dst) {
+    *dst = nullptr;
+    if (v.empty()) return;
+    items.push_back(Item{v.data(), v.size() * sizeof(T), total, reinterpret_cast<const void**>(dst)});
+    total += (v.size() * sizeof(T) + 255) / 256 * 256;
+  }
+  size_t reserve(size_t bytes) {  // device-only space (no host data)
+    const size_t off = total;
+    total += (bytes + 255) / 256 * 256;
+    return off;
+  }
+  char* commit(std::vector<void*>& owned) {
+    void* base = nullptr;
+    ck(cudaMalloc(&base, std::max<size_t>(total, 256)), "cudaMalloc scene");
+    owned.push_back(base);
+    char* b = static_cast<char*>(base);
+    for (const Item& it : items) {
+      ck(cudaMemcpyAsync(b + it.offset, it.src, it.bytes, cudaMemcpyHostToDevice, 0), "cudaMemcpyAsync H2D");
+      *it.dst = b + it.offset;
+    }
+    ck(cudaStreamSynchronize(0), "cudaStreamSynchronize");
+    return b;
+  }
+};
 
 int sm_count() {
   static int n = 0;
@@ -639,10 +666,8 @@ struct clv_device_scene {
   }
   ~clv_device_scene() {
     if (cap_stream) cudaStreamDestroy(cap_stream);
-    if (ray_next) cudaFree(ray_next);
     if (ray_sort) cudaFree(ray_sort);
-    for (void* p : owned) cudaFree(p);
-    if (err) cudaFree(err);
+    for (void* p : owned) cudaFree(p);  // scene arrays, error word and ray counter
     if (scratch) cudaFree(scratch);
     if (wf_mem) cudaFree(wf_mem);
     if (wf_counters) cudaFree(wf_counters);
@@ -1006,31 +1031,37 @@ int clv_scene_upload(const clv_scene* s, clv_device_scene** out) {
     const clv::HostScene& h = s->host;
     std::unique_ptr<clv_device_scene> d(new clv_device_scene());
     ClvDeviceScene& v = d->view;
-    auto& o = d->owned;
-    v.nodes = upload(h.nodes, o);
-    v.tris = upload(h.tris, o);
-    v.quads = upload(h.quads, o);
-    v.spheres = upload(h.spheres, o);
-    v.objs = upload(h.objs, o);
-    v.obj_children = upload(h.obj_children, o);
-    v.tri_gid = upload(h.tri_gid, o);
-    v.quad_gid = upload(h.quad_gid, o);
-    v.sphere_gid = upload(h.sphere_gid, o);
-    v.obj_gid = upload(h.obj_gid, o);
-    v.tri_mat = upload(h.tri_mat, o);
-    v.quad_mat = upload(h.quad_mat, o);
-    v.sphere_mat = upload(h.sphere_mat, o);
-    v.tri_area = upload(h.tri_area, o);
-    v.quad_area = upload(h.quad_area, o);
-    v.materials = upload(h.materials, o);
-    v.spd = upload(h.spd, o);
+    UploadPack pk;
+    pk.add(h.nodes, &v.nodes);
+    pk.add(h.tris, &v.tris);
+    pk.add(h.quads, &v.quads);
+    pk.add(h.spheres, &v.spheres);
+    pk.add(h.objs, &v.objs);
+    pk.add(h.obj_children, &v.obj_children);
+    pk.add(h.tri_gid, &v.tri_gid);
+    pk.add(h.quad_gid, &v.quad_gid);
+    pk.add(h.sphere_gid, &v.sphere_gid);
+    pk.add(h.obj_gid, &v.obj_gid);
+    pk.add(h.tri_mat, &v.tri_mat);
+    pk.add(h.quad_mat, &v.quad_mat);
+    pk.add(h.sphere_mat, &v.sphere_mat);
+    pk.add(h.tri_area, &v.tri_area);
+    pk.add(h.quad_area, &v.quad_area);
+    pk.add(h.materials, &v.materials);
+    pk.add(h.spd, &v.spd);
     std::vector<float> ill((size_t)clv_tables::kNumIlluminants * 400);
     std::memcpy(ill.data(), clv_tables::kIlluminants, ill.size() * sizeof(float));
-    v.illuminant = upload(ill, o);
+    pk.add(ill, &v.illuminant);
     std::vector<float> cmf(400 * 3);
     for (int i = 0; i < 400; ++i) clv::wavelength_to_xyz(380 + i, &cmf[3 * i]);
-    v.cmf = upload(cmf, o);
-    v.mis_nodes = upload(h.mis_nodes, o);
+    pk.add(cmf, &v.cmf);
+    pk.add(h.mis_nodes, &v.mis_nodes);
+    v.tri_verts = nullptr;
+    if (s->watertight && !h.tri_verts.empty()) pk.add(h.tri_verts, &v.tri_verts);
+    const size_t off_err = pk.reserve(sizeof(uint32_t)), off_next = pk.reserve(sizeof(unsigned long long));
+    char* base = pk.commit(d->owned);
+    d->err = reinterpret_cast<uint32_t*>(base + off_err);
+    d->ray_next = reinterpret_cast<unsigned long long*>(base + off_next);
     v.root = h.root;
     v.mis_root = h.mis_root;
     std::memcpy(v.root_box, h.root_box, sizeof v.root_box);
@@ -1047,11 +1078,6 @@ int clv_scene_upload(const clv_scene* s, clv_device_scene** out) {
     v.mis_depth = h.mis_depth;
     v.camera = h.camera;
     v.watertight = s->watertight;
-    v.tri_verts = nullptr;
-    if (s->watertight && !h.tri_verts.empty())
-      v.tri_verts = upload(h.tri_verts, o);
-    ck(cudaMalloc(&d->err, sizeof(uint32_t)), "cudaMalloc");
-    ck(cudaMalloc(&d->ray_next, sizeof(unsigned long long)), "cudaMalloc");
     ck(cudaMemset(d->err, 0, sizeof(uint32_t)), "cudaMemset");
     d->width = h.width;
     d->height = h.height;
