@@ -105,6 +105,9 @@ __global__ void ray_scatter(const uint32_t* __restrict__ key, uint64_t n, uint32
 // which lanes are idle), so lanes do not sit out the longest ray of their
 // warp (persistent threads with dynamic fetch, Aila & Laine 2009).  Every ray
 // runs closest_hit's exact traversal.  COUNT: per-ray visit counts wanted.
+#ifndef CLV_SHADE_BLOCKS
+#define CLV_SHADE_BLOCKS 8  // shading-kernel blocks per SM when no tuned shape is set (one wave at 8 resident)
+#endif
 #ifndef CLV_SHSTACK
 // ray casts: the first 12 stack entries of each thread in shared memory (24 KB
 // per block, the most that keeps 9 blocks per SM; measured best of 0..24)
@@ -1247,7 +1250,8 @@ static int render_wavefront(clv_device_scene* d, const clv_render_opts* o, doubl
     const int batch = 8;  // bounces between polls of the live-path counter
     WfCounters* C = d->wf_counters;
     // shading kernels walk their queues with a grid-stride loop over a fixed grid
-    const uint32_t qgrid = std::min<uint32_t>(grid, (uint32_t)sm_count() * (d->tuned_shade ? d->tuned_shade : 16));
+    const uint32_t qgrid =
+        std::min<uint32_t>(grid, (uint32_t)sm_count() * (d->tuned_shade ? d->tuned_shade : CLV_SHADE_BLOCKS));
     if (prof) {
       std::memset(prof, 0, sizeof *prof);
       ck(cudaMalloc(&dcnt, 3 * sizeof(unsigned long long)), "cudaMalloc");
@@ -1418,7 +1422,8 @@ int clv_render_batch(clv_device_scene* const* ds, const clv_render_opts* opts, d
     WfCounters* C = d0->wf_counters;
     const int block = 128;
     const uint32_t grid = (uint32_t)((q + block - 1) / block);
-    const uint32_t qgrid = std::min<uint32_t>(grid, (uint32_t)sm_count() * (d0->tuned_shade ? d0->tuned_shade : 16));
+    const uint32_t qgrid =
+        std::min<uint32_t>(grid, (uint32_t)sm_count() * (d0->tuned_shade ? d0->tuned_shade : CLV_SHADE_BLOCKS));
     const ClvDeviceScene& S0 = d0->view;
     const WfParams P0 = params[0];
     wf_init<true><<<grid, block, 0, st>>>(S0, P0, W, B);
@@ -1698,7 +1703,7 @@ extern "C" int clv_render_device_noalloc(clv_device_scene* d, const clv_render_o
   W.grec_cap = 0;
   const int block = 128;
   const uint32_t grid = (uint32_t)((q + block - 1) / block);
-  const uint32_t qgrid = std::min<uint32_t>(grid, (uint32_t)sm_count() * 16);
+  const uint32_t qgrid = std::min<uint32_t>(grid, (uint32_t)sm_count() * CLV_SHADE_BLOCKS);
   // the array keeps the previous call's contents: counters are reset here and
   // wf_init rewrites every path slot
   noalloc_counters_init<<<1, 1, 0, st>>>(C, std::min<uint64_t>(q, P.total));
