@@ -36,7 +36,10 @@ namespace clvd {
 #define CLV_MIS_STACK 32   // MIS tree evaluation stack
 #define CLV_NEST 6         // wrapper nesting depth handled by the object interpreter
 #ifndef CLV_MINB
-#define CLV_MINB 7         // resident blocks per SM asked of the traversal kernels (72 registers; 6 and 8 slower)
+#define CLV_MINB 8         // resident blocks per SM asked of the wavefront intersect (64 registers)
+#endif
+#ifndef CLV_MINB_CHAIN
+#define CLV_MINB_CHAIN 7   // the same for its wrapper-chain variant (72 registers; 6 and 8 slower on the box)
 #endif
 
 // Device error flags (bitwise OR into a status word the host reads).

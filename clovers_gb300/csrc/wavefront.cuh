@@ -271,7 +271,7 @@ __device__ __forceinline__ int intersect_slot(const ClvDeviceScene& S, const WfS
 // only_level >= 0 (batches): only the slots of scenes at that traversal level,
 // so that a batch runs each scene with the variant its objects need.
 template <int CPLX, bool COUNT, bool BATCH, int WT>
-__global__ void __launch_bounds__(128, CLV_MINB) wf_intersect(ClvDeviceScene S, WfState W, WfCounters* C, uint32_t* err,
+__global__ void __launch_bounds__(128, CPLX == 1 ? CLV_MINB_CHAIN : CLV_MINB) wf_intersect(ClvDeviceScene S, WfState W, WfCounters* C, uint32_t* err,
                                                               unsigned long long* cnt, WfBatch B, int only_level) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   Counters c{0u, 0u};
