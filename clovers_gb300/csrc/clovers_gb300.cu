@@ -379,12 +379,11 @@ __global__ void debug_kernel(ClvDeviceScene S, RenderParams P, double* __restric
   Rng rng;
   rng.init(P.seed, (uint32_t)pix, P.sample_offset);
   const int lambda = random_wavelength(rng);
-  const float time = rng.f32();
-  (void)time;
+  const float time = rng.f32();  // the ray's time: moving spheres are where they are at it
   const ClvCamera& C = S.camera;
   const float pu = (float)x / (float)P.width, pv = (float)y / (float)P.height;
   const V dir = sub(add(add(ld3(C.llc), scl(pu, ld3(C.horizontal))), scl(pv, ld3(C.vertical))), ld3(C.origin));
-  Ray r{ld3(C.origin), unit(dir), 0.0f, lambda};
+  Ray r{ld3(C.origin), unit(dir), time, lambda};
   float rgb[3] = {0.0f, 0.0f, 0.0f};  // linear sRGB
   Hit h;
   Rec full;

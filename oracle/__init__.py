@@ -61,6 +61,7 @@ def lib():
                 "orc_scene_background_xyz": (None, [vp, vp]),
                 "orc_raycast": (i32, [vp, vp, u64, vp, vp, vp, vp, i32]),
                 "orc_render": (i32, [vp, u32, u32, u32, u32, u64, u32, u32, u32, u32, u32, vp, i32]),
+                "orc_render_debug": (i32, [vp, u32, u32, u32, u64, u32, vp, i32]),
                 "orc_trace_sample": (i32, [vp, u32, u32, u32, u32, u32, u32, u64, vp, vp, vp]),
                 "orc_guide_forward": (None, [vp, vp, u64, i32, vp]),
                 "orc_guide_gradient": (ctypes.c_double, [vp, vp, u64, i32, vp]),
@@ -219,6 +220,15 @@ class Scene:
         out = np.zeros(((r1 - r0) * (x1 - x0), 3), np.float64)
         rc = lib().orc_render(self.h, width, height, spp, max_depth, seed, x0, r0, x1, r1, sample_offset, _buf(out),
                               threads or os.cpu_count() or 1)
+        if rc != 0:
+            raise RuntimeError(_err())
+        return out
+
+    def render_debug(self, width, height, mode, seed, sample_offset=0, threads=None):
+        """Debug render modes (1 normal map, 2 BVH test count, 3 primitive test count): (h*w, 3) linear sRGB."""
+        out = np.zeros((width * height, 3), np.float32)
+        rc = lib().orc_render_debug(self.h, width, height, mode, seed, sample_offset, _buf(out),
+                                    threads or os.cpu_count() or 1)
         if rc != 0:
             raise RuntimeError(_err())
         return out

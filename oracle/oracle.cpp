@@ -2096,6 +2096,60 @@ int orc_render(void* s, uint32_t width, uint32_t height, uint32_t spp, uint32_t 
   }
 }
 
+// Debug render modes (clovers-cli/src/draw_cpu.rs:148-207): one ray per pixel
+// through its corner (x / width, y / height), no lens offset, with a drawn
+// wavelength and time.  Mode 1 colours the hit normal (normals.rs:11-37),
+// modes 2 and 3 the BVH node and primitive test counts through the ramp of
+// debug_visualizations.rs:18-35.  Writes linear sRGB per buffer pixel (row 0
+// at the top of the image, like the path tracer's film).
+int orc_render_debug(void* s, uint32_t width, uint32_t height, uint32_t mode, uint64_t seed, uint32_t sample_offset,
+                     float* rgb_out, int threads) {
+  try {
+    Scene* sc = static_cast<Scene*>(s);
+    if (mode < 1 || mode > 3) throw std::runtime_error("debug mode must be 1, 2 or 3");
+    parallel_for(height, threads, [&](uint64_t row) {
+      for (uint32_t x = 0; x < width; ++x) {
+        const uint64_t pix = row * width + x;
+        const uint32_t y = height - 1 - (uint32_t)row;
+        Rng rng(seed, (uint32_t)pix, sample_offset);
+        const int lambda = random_wavelength(rng);
+        const Float time = rng.next_f32();
+        const Ray ray = sc->camera.get_ray((Float)x / (Float)width, (Float)y / (Float)height, 0.0f, 0.0f, time, lambda);
+        HitRecord rec;
+        Counters c;
+        const bool any = sc->bvh_root->hit(ray, EPSILON_SHADOW_ACNE, 3.40282347e+38f, &rng, rec, &c);
+        float* o = rgb_out + 3 * pix;
+        o[0] = o[1] = o[2] = 0.0f;
+        if (mode == 1) {
+          if (any) {
+            const Vec3 n{-rec.normal.x, rec.normal.y, -rec.normal.z};
+            o[0] = 0.5f + 0.5f * n.x;
+            o[1] = 0.5f + 0.5f * n.y;
+            o[2] = n.z < 0.0f ? 0.0f : n.z;
+          }
+        } else {
+          const uint64_t d = mode == 2 ? c.nodes : c.prims;
+          if (d <= 255) {
+            o[0] = o[1] = o[2] = (Float)d / 255.0f;
+          } else if (d <= 511) {
+            o[0] = 1.0f;
+            o[1] = 1.0f;
+          } else if (d <= 1023) {
+            o[0] = 1.0f;
+            o[1] = 0.5f;
+          } else {
+            o[0] = 1.0f;
+          }
+        }
+      }
+    });
+    return 0;
+  } catch (std::exception& e) {
+    g_err = e.what();
+    return -1;
+  }
+}
+
 // One path's spectral powers (trace.rs return value) for buffer pixel (x, r), sample index.
 int orc_trace_sample(void* s, uint32_t width, uint32_t height, uint32_t x, uint32_t r, uint32_t sample,
                      uint32_t max_depth, uint64_t seed, float p_out[4], int waves_out[4], float ray_out[6]) {
