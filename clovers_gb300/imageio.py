@@ -32,6 +32,31 @@ def png_bytes(rgb, width, height, texts=()):
     return b"".join(out)
 
 
+def format_duration(seconds):
+    """The render duration as the reference prints it (render.rs:150-151 formats
+    it with the humantime crate, 2.x, which is not vendored): the non-zero
+    components among days, hours, minutes, seconds, milliseconds, microseconds
+    and nanoseconds, largest first, separated by spaces, with the suffixes
+    "day"/"days", "h", "m", "s", "ms", "us", "ns"; "0s" for no time at all.
+    Longer units (months, years) do not occur for a render."""
+    ns = max(0, int(round(float(seconds) * 1e9)))
+    if ns == 0:
+        return "0s"
+    secs, frac = divmod(ns, 1_000_000_000)
+    days, rem = divmod(secs, 86400)
+    parts = []
+    if days:
+        parts.append("%d%s" % (days, "day" if days == 1 else "days"))
+    h, rem = divmod(rem, 3600)
+    m, s = divmod(rem, 60)
+    ms, rest = divmod(frac, 1_000_000)
+    us, n = divmod(rest, 1000)
+    for value, unit in ((h, "h"), (m, "m"), (s, "s"), (ms, "ms"), (us, "us"), (n, "ns")):
+        if value:
+            parts.append("%d%s" % (value, unit))
+    return " ".join(parts)
+
+
 def write_png(path, rgb, width, height, render_options=None, duration_s=None):
     texts = []
     if render_options is not None:
@@ -41,7 +66,8 @@ def write_png(path, rgb, width, height, render_options=None, duration_s=None):
         details = (", %d samples per pixel, %d max ray bounce depth." % (render_options.samples,
                                                                          render_options.max_depth)
                    if render_options.mode == "path-tracing" else ".")
-        stats = "Rendering finished in %.3fs, using %d threads." % (duration_s or 0.0, os.cpu_count() or 1)
+        stats = "Rendering finished in %s, using %d threads." % (format_duration(duration_s or 0.0),
+                                                                  os.cpu_count() or 1)
         texts = [("Comment", common + details + " " + stats), ("Software", "clovers")]
     with open(path, "wb") as f:
         f.write(png_bytes(rgb, width, height, texts))

@@ -136,3 +136,32 @@ def test_png_and_exr_encoders(tmp_path):
     # last scanline holds B, G, R planes of the last image row
     last = np.frombuffer(ex[-4 * 12:], "<f4").reshape(3, 4)
     assert np.array_equal(last[2], xyz.reshape(3, 4, 3)[2, :, 0])
+
+
+def test_png_metadata_as_the_reference_writes_it(tmp_path):
+    """write.rs:54-73: a Comment tEXt chunk (scene, mode in its Rust name,
+    resolution, samples and depth for path tracing, the duration in humantime's
+    format, the thread count) followed by Software = clovers."""
+    import struct
+    import clovers_gb300 as cg
+    from clovers_gb300 import imageio
+    assert imageio.format_duration(0) == "0s"
+    assert imageio.format_duration(1.23456789) == "1s 234ms 567us 890ns"
+    assert imageio.format_duration(9420.001) == "2h 37m 1ms"
+    assert imageio.format_duration(90061) == "1day 1h 1m 1s"
+    assert imageio.format_duration(2 * 86400 + 0.5) == "2days 500ms"
+    opts = cg.RenderOptions(input="scenes/cornell.json", width=4, height=3, samples=16, max_depth=8)
+    path = str(tmp_path / "x.png")
+    imageio.write_png(path, np.zeros((12, 3), np.uint8), 4, 3, opts, duration_s=1.5)
+    data = open(path, "rb").read()
+    texts, pos = [], 8
+    while pos < len(data):
+        n = struct.unpack(">I", data[pos:pos + 4])[0]
+        if data[pos + 4:pos + 8] == b"tEXt":
+            texts.append(data[pos + 8:pos + 8 + n].decode("latin-1"))
+        pos += 12 + n
+    import os
+    assert texts == ["Comment\0Rendered with the clovers path tracing engine. Scene file scenes/cornell.json rendered "
+                     "using the PathTracing rendering mode at 4x3 resolution, 16 samples per pixel, 8 max ray bounce "
+                     "depth. Rendering finished in 1s 500ms, using %d threads." % (os.cpu_count() or 1),
+                     "Software\0clovers"]
