@@ -955,10 +955,10 @@ int clv_selftest_division(uint64_t n, uint64_t seed, uint64_t* mismatches) {
 int clv_scene_load_json_text(const char* json, const char* base_dir, uint32_t width, uint32_t height, int bvh_alg,
                              clv_scene** out) {
   if (!json || !out) return fail(CLV_E_INVALID, "null argument");
-  if (bvh_alg != CLV_BVH_SAH) return fail(CLV_E_INVALID, "only the SAH BVH builder is supported");
+  if (bvh_alg != CLV_BVH_SAH && bvh_alg != CLV_BVH_LAM) return fail(CLV_E_INVALID, "unknown BVH algorithm");
   try {
     std::unique_ptr<clv_scene> s(new clv_scene());
-    s->host = clv::load_scene_text(json, width, height, base_dir ? base_dir : ".");
+    s->host = clv::load_scene_text(json, width, height, base_dir ? base_dir : ".", bvh_alg == CLV_BVH_LAM);
     if (s->host.tree_depth > CLV_STACK) return fail(CLV_E_SCENE, "BVH deeper than the traversal stack");
     if (s->host.mis_depth > CLV_MIS_STACK) return fail(CLV_E_SCENE, "MIS tree deeper than its evaluation stack");
     *out = s.release();
@@ -970,10 +970,10 @@ int clv_scene_load_json_text(const char* json, const char* base_dir, uint32_t wi
 
 int clv_scene_load_json(const char* path, uint32_t width, uint32_t height, int bvh_alg, clv_scene** out) {
   if (!path || !out) return fail(CLV_E_INVALID, "null argument");
-  if (bvh_alg != CLV_BVH_SAH) return fail(CLV_E_INVALID, "only the SAH BVH builder is supported");
+  if (bvh_alg != CLV_BVH_SAH && bvh_alg != CLV_BVH_LAM) return fail(CLV_E_INVALID, "unknown BVH algorithm");
   try {
     std::unique_ptr<clv_scene> s(new clv_scene());
-    s->host = clv::load_scene_json(path, width, height);
+    s->host = clv::load_scene_json(path, width, height, bvh_alg == CLV_BVH_LAM);
     if (s->host.tree_depth > CLV_STACK) return fail(CLV_E_SCENE, "BVH deeper than the traversal stack");
     if (s->host.mis_depth > CLV_MIS_STACK) return fail(CLV_E_SCENE, "MIS tree deeper than its evaluation stack");
     *out = s.release();

@@ -79,7 +79,7 @@ inline void box_pad(Box& a) {  // aabb.rs:99-119
   }
 }
 
-// ---- SAH build over items with a box and a centroid.
+// ---- BVH builds over items with a box and a centroid.
 struct Item {
   Box box;
   V3 c;
@@ -923,17 +923,87 @@ void set_gid(HostScene& S, uint32_t ref, uint32_t gid) {
   else if (k == CLV_REF_OBJ) S.obj_gid[i] = gid;
 }
 
+// longest_axis_midpoint.rs:12-93: the list sorted by box minimum along the
+// axis of largest span, split at its middle (one object and a node of two at
+// three objects).  The reference's comparator (bvh/build/utils.rs:7-21)
+// answers Less only for a strictly smaller minimum: a stable sort keeps ties
+// in list order, and the two-object case, which compares the pair directly,
+// puts the second object first on a tie.  Nodes in preorder, like sah_build.
+BuildResult lam_build(const std::vector<Item>& items) {
+  BuildResult out;
+  const size_t n = items.size();
+  if (n == 0) throw std::runtime_error("BVH build over an empty list (the reference's builder panics)");
+  std::vector<uint32_t> ids(n);
+  for (size_t i = 0; i < n; ++i) ids[i] = (uint32_t)i;
+  struct Task {
+    size_t b, e;
+    int64_t parent;
+    int side;
+    uint32_t depth;
+  };
+  std::vector<Task> stack;
+  stack.push_back({0, n, -1, 0, 1});
+  auto item_code = [](uint32_t i) { return -(int64_t)i - 2; };
+  while (!stack.empty()) {
+    const Task t = stack.back();
+    stack.pop_back();
+    const int64_t me = (int64_t)out.nodes.size();
+    out.nodes.emplace_back();
+    out.depth = std::max(out.depth, t.depth);
+    if (t.parent >= 0) (t.side == 0 ? out.nodes[t.parent].left : out.nodes[t.parent].right) = me;
+    Box bb = items[ids[t.b]].box;
+    for (size_t i = t.b + 1; i < t.e; ++i) box_grow(bb, items[ids[i]].box);
+    out.nodes[me].box = bb;
+    const float sx = bb.b[1] - bb.b[0], sy = bb.b[3] - bb.b[2], sz = bb.b[5] - bb.b[4];
+    const float largest = std::fmax(std::fmax(sx, sy), sz);
+    const int axis = sx == largest ? 0 : (sy == largest ? 1 : (sz == largest ? 2 : -1));
+    if (axis < 0) throw std::runtime_error("no axis of largest span (NaN box)");
+    auto key = [&](uint32_t i) { return items[i].box.b[2 * axis]; };
+    const size_t count = t.e - t.b;
+    if (count == 1) {
+      out.nodes[me].left = item_code(ids[t.b]);
+      continue;
+    }
+    if (count == 2) {
+      const uint32_t a = ids[t.b], c = ids[t.b + 1];
+      const bool keep = key(a) < key(c);
+      out.nodes[me].left = item_code(keep ? a : c);
+      out.nodes[me].right = item_code(keep ? c : a);
+      continue;
+    }
+    std::stable_sort(ids.begin() + (std::ptrdiff_t)t.b, ids.begin() + (std::ptrdiff_t)t.e,
+                     [&](uint32_t a, uint32_t c) { return key(a) < key(c); });
+    if (count == 3) {
+      out.nodes[me].left = item_code(ids[t.b]);
+      const int64_t r = (int64_t)out.nodes.size();
+      out.nodes.emplace_back();
+      out.nodes[me].right = r;
+      Box rb = items[ids[t.b + 1]].box;
+      box_grow(rb, items[ids[t.b + 2]].box);
+      out.nodes[r].box = rb;
+      out.nodes[r].left = item_code(ids[t.b + 1]);
+      out.nodes[r].right = item_code(ids[t.b + 2]);
+      out.depth = std::max(out.depth, t.depth + 1);
+      continue;
+    }
+    const size_t mid = t.b + count / 2;
+    stack.push_back({mid, t.e, me, 1, t.depth + 1});  // popped after the left subtree: preorder
+    stack.push_back({t.b, mid, me, 0, t.depth + 1});
+  }
+  return out;
+}
+
 void store_box(float dst[6], const Box& b) { std::memcpy(dst, b.b, sizeof b.b); }
 
 // Main BVH: nodes carry both children's boxes.
-void flatten_main(HostScene& S, const std::vector<Emitted>& tops) {
+void flatten_main(HostScene& S, const std::vector<Emitted>& tops, bool lam = false) {
   std::vector<Item> items(tops.size());
   for (size_t i = 0; i < tops.size(); ++i) {
     if (!tops[i].has_box) throw std::runtime_error("an unbounded object cannot be placed in the BVH");
     items[i].box = tops[i].box;
     items[i].c = tops[i].c;
   }
-  BuildResult br = sah_build(items);
+  BuildResult br = lam ? lam_build(items) : sah_build(items);
   S.nodes.resize(br.nodes.size());
   auto child = [&](int64_t code, float box[6]) -> uint32_t {
     if (code == kEmpty) { std::memset(box, 0, 6 * sizeof(float)); return CLV_REF_EMPTY; }
@@ -953,7 +1023,7 @@ void flatten_main(HostScene& S, const std::vector<Emitted>& tops) {
   S.tree_depth = br.depth;
 }
 
-void flatten_mis(HostScene& S, const std::vector<Emitted>& prio) {
+void flatten_mis(HostScene& S, const std::vector<Emitted>& prio, bool lam = false) {
   std::vector<Item> items(prio.size());
   for (size_t i = 0; i < prio.size(); ++i) {
     if (!prio[i].has_box) throw std::runtime_error("an unbounded priority object cannot be placed in the MIS BVH");
@@ -964,7 +1034,7 @@ void flatten_mis(HostScene& S, const std::vector<Emitted>& prio) {
     items[i].box = prio[i].box;
     items[i].c = prio[i].c;
   }
-  BuildResult br = sah_build(items);
+  BuildResult br = lam ? lam_build(items) : sah_build(items);
   S.mis_nodes.resize(br.nodes.size());
   auto child = [&](int64_t code) -> uint32_t {
     if (code == kEmpty) return CLV_REF_EMPTY;
@@ -1004,7 +1074,8 @@ void camera_init(ClvCamera& cam, V3 look_from, V3 look_at, V3 up, float vfov, fl
 
 }  // namespace
 
-HostScene load_scene_text(const std::string& text, uint32_t width, uint32_t height, const std::string& base_dir) {
+HostScene load_scene_text(const std::string& text, uint32_t width, uint32_t height, const std::string& base_dir,
+                          bool lam) {
   if (width == 0 || height == 0) throw std::runtime_error("width and height must be positive");
   const Value root = clv_json::parse(text);
   HostScene S;
@@ -1055,18 +1126,19 @@ HostScene load_scene_text(const std::string& text, uint32_t width, uint32_t heig
     throw std::runtime_error("the scene has no priority objects (the reference's MIS BVH build panics)");
   for (size_t i = 0; i < tops.size(); ++i) set_gid(S, tops[i].ref, (uint32_t)i);
   S.object_count = tops.size();
-  flatten_main(S, tops);
-  flatten_mis(S, prio);
+  flatten_main(S, tops, lam);  // scenefile.rs:106-108: both trees with the same algorithm
+  flatten_mis(S, prio, lam);
   return S;
 }
 
-HostScene load_scene_json(const std::string& path, uint32_t width, uint32_t height) {
+HostScene load_scene_json(const std::string& path, uint32_t width, uint32_t height, bool lam) {
   std::ifstream f(path);
   if (!f) throw std::runtime_error("cannot open scene file `" + path + "`");
   std::stringstream ss;
   ss << f.rdbuf();
   const size_t slash = path.find_last_of('/');
-  return load_scene_text(ss.str(), width, height, slash == std::string::npos ? std::string(".") : path.substr(0, slash));
+  return load_scene_text(ss.str(), width, height, slash == std::string::npos ? std::string(".") : path.substr(0, slash),
+                         lam);
 }
 
 HostScene mesh_scene(const float* verts, uint32_t nverts, const uint32_t* idx, uint32_t ntris) {

@@ -36,8 +36,10 @@ struct HostScene {
 
 // Loads a clovers scene file (JSON).  width/height set the camera aspect ratio
 // (clovers-cli/src/scenefile.rs:47-57).  Throws std::runtime_error.
-HostScene load_scene_json(const std::string& path, uint32_t width, uint32_t height);
-HostScene load_scene_text(const std::string& text, uint32_t width, uint32_t height, const std::string& base_dir);
+// lam: the longest-axis-midpoint builder (BvhAlgorithm::Lam) for both trees instead of the SAH builder.
+HostScene load_scene_json(const std::string& path, uint32_t width, uint32_t height, bool lam = false);
+HostScene load_scene_text(const std::string& text, uint32_t width, uint32_t height, const std::string& base_dir,
+                          bool lam = false);
 
 // A scene made only of triangles given as a vertex buffer and u32 index
 // triples (Triangle::from_coordinates, clovers/src/objects/triangle.rs:106-117),

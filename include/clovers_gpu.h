@@ -29,7 +29,7 @@ extern "C" {
 #define CLV_E_CUDA -3      /* CUDA runtime error (message has the details)  */
 #define CLV_E_DEVICE -4    /* a kernel reported an error flag (stack, nesting) */
 
-#define CLV_BVH_LAM 0 /* BvhAlgorithm::Lam -- not supported (returns CLV_E_INVALID) */
+#define CLV_BVH_LAM 0 /* BvhAlgorithm::Lam (bvh/build/longest_axis_midpoint.rs) */
 #define CLV_BVH_SAH 1 /* BvhAlgorithm::Sah (the clovers-cli default, render.rs:43-44) */
 
 /* RenderMode, clovers-cli/src/render.rs:51-61 */

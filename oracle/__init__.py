@@ -52,6 +52,7 @@ def lib():
                 "orc_interval": (None, [f32, f32, vp]),
                 "orc_prim_hit": (i32, [i32, vp, vp, vp, vp, vp, vp]),
                 "orc_scene_load_json": (vp, [ctypes.c_char_p, u32, u32]),
+                "orc_scene_load_json_bvh": (vp, [ctypes.c_char_p, u32, u32, i32]),
                 "orc_scene_from_mesh": (vp, [vp, u32, vp, u32]),
                 "orc_scene_free": (None, [vp]),
                 "orc_scene_set_watertight": (None, [vp, i32]),
@@ -164,8 +165,10 @@ class Scene:
         self.h = ctypes.c_void_p(handle)
 
     @classmethod
-    def from_json(cls, path, width, height):
-        return cls(lib().orc_scene_load_json(os.fsencode(path), width, height))
+    def from_json(cls, path, width, height, bvh="sah"):
+        if bvh not in ("sah", "lam"):
+            raise ValueError("unknown BVH algorithm %r" % bvh)
+        return cls(lib().orc_scene_load_json_bvh(os.fsencode(path), width, height, 0 if bvh == "lam" else 1))
 
     @classmethod
     def from_mesh(cls, verts, idx):

@@ -1275,6 +1275,59 @@ static std::unique_ptr<BVHNode> build_sah(std::vector<HPtr> hs) {
   node->right = build_sah(std::move(R));
   return node;
 }
+// longest_axis_midpoint.rs:12-93: split at the middle of the list sorted by
+// box minimum along the axis of largest span.  The comparator
+// (bvh/build/utils.rs:7-21) answers Less only for a strictly smaller minimum,
+// so a stable sort keeps ties in list order, while the two-object case, which
+// compares the pair directly, puts the second object first on a tie.
+static std::unique_ptr<BVHNode> build_lam(std::vector<HPtr> hs) {
+  std::unique_ptr<BVHNode> node(new BVHNode());
+  if (!vec_bounding_box(hs, node->box)) throw std::runtime_error("No bounding box for objects");
+  const Float sx = node->box.x.size(), sy = node->box.y.size(), sz = node->box.z.size();
+  const Float largest = rmax(rmax(sx, sy), sz);
+  int axis;
+  if (sx == largest) axis = 0;
+  else if (sy == largest) axis = 1;
+  else if (sz == largest) axis = 2;
+  else throw std::runtime_error("no axis of largest span (NaN box)");
+  auto key = [axis](const HPtr& h) { return h->aabb()->axis(axis).min; };
+  const size_t n = hs.size();
+  if (n == 1) {
+    node->left = std::move(hs[0]);
+    node->right.reset(new Empty());
+    return node;
+  }
+  if (n == 2) {
+    if (key(hs[0]) < key(hs[1])) {
+      node->left = std::move(hs[0]);
+      node->right = std::move(hs[1]);
+    } else {
+      node->left = std::move(hs[1]);
+      node->right = std::move(hs[0]);
+    }
+    return node;
+  }
+  std::stable_sort(hs.begin(), hs.end(), [&](const HPtr& a, const HPtr& b) { return key(a) < key(b); });
+  if (n == 3) {
+    node->left = std::move(hs[0]);
+    std::unique_ptr<BVHNode> r(new BVHNode());
+    r->box = AABB::combine(*hs[1]->aabb(), *hs[2]->aabb());
+    r->left = std::move(hs[1]);
+    r->right = std::move(hs[2]);
+    node->right = std::move(r);
+    return node;
+  }
+  const size_t mid = n / 2;
+  std::vector<HPtr> R;
+  for (size_t i = mid; i < n; ++i) R.push_back(std::move(hs[i]));
+  hs.resize(mid);
+  node->left = build_lam(std::move(hs));
+  node->right = build_lam(std::move(R));
+  return node;
+}
+static std::unique_ptr<BVHNode> build_bvh(std::vector<HPtr> hs, bool lam) {
+  return lam ? build_lam(std::move(hs)) : build_sah(std::move(hs));
+}
 
 // ----------------------------------------------------------------- camera --
 struct Camera {  // clovers/src/camera.rs:59-126
@@ -1677,7 +1730,8 @@ struct Loader {
 static HPtr clone_for_priority(const Value& o, Loader& ld) { return ld.object(o, nullptr); }
 
 // clovers-cli/src/scenefile.rs:34-117
-static Scene* load_scene(const std::string& text, uint32_t width, uint32_t height, const std::string& base_dir) {
+static Scene* load_scene(const std::string& text, uint32_t width, uint32_t height, const std::string& base_dir,
+                         bool lam = false) {
   Value root = clv_json::parse(text);
   std::unique_ptr<Scene> sc(new Scene());
   Loader ld;
@@ -1730,8 +1784,8 @@ static Scene* load_scene(const std::string& text, uint32_t width, uint32_t heigh
   sc->object_count = hitables.size();
   if (hitables.empty()) throw std::runtime_error("scene has no objects");
   if (priority.empty()) throw std::runtime_error("scene has no priority objects (the reference's MIS BVH build panics)");
-  sc->bvh_root = build_sah(std::move(hitables));
-  sc->mis_root = build_sah(std::move(priority));
+  sc->bvh_root = build_bvh(std::move(hitables), lam);  // scenefile.rs:106-108: both trees, one algorithm
+  sc->mis_root = build_bvh(std::move(priority), lam);
   return sc.release();
 }
 
@@ -1977,6 +2031,22 @@ int orc_prim_hit(int kind, const float q[3], const float u[3], const float v[3],
   return 1;
 }
 
+// bvh: 0 longest axis midpoint, 1 surface area heuristic (BvhAlgorithm, bvh.rs:30-39)
+void* orc_scene_load_json_bvh(const char* path, uint32_t width, uint32_t height, int bvh) {
+  try {
+    std::ifstream f(path);
+    if (!f) throw std::runtime_error(std::string("cannot open scene file ") + path);
+    std::stringstream ss;
+    ss << f.rdbuf();
+    std::string p(path);
+    size_t slash = p.find_last_of('/');
+    return load_scene(ss.str(), width, height, slash == std::string::npos ? std::string(".") : p.substr(0, slash),
+                      bvh == 0);
+  } catch (std::exception& e) {
+    g_err = e.what();
+    return nullptr;
+  }
+}
 void* orc_scene_load_json(const char* path, uint32_t width, uint32_t height) {
   try {
     std::ifstream f(path);

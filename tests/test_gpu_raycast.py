@@ -165,3 +165,18 @@ def test_raycast_into_caller_arrays():
         cg.raycast(d, rays, out=(np.empty(len(rays), np.int64), np.empty(len(rays), np.float32)))
     with pytest.raises(ValueError):
         cg.raycast(d, rays, out=(np.empty(len(rays) - 1, np.uint32), np.empty(len(rays), np.float32)))
+
+
+@pytest.mark.parametrize("which", ["box", "spheres"])
+def test_lam_tree_parity(box_scene_path, spheres_scene_path, which):
+    """Ray casts through longest-axis-midpoint trees (`--bvh lam`): ids,
+    distances and visit counts equal the oracle's on its own LAM tree."""
+    path = box_scene_path if which == "box" else spheres_scene_path
+    w, h = 96, 72
+    d = cg.Scene.from_json(path, w, h, bvh="lam").upload()
+    o = oracle.Scene.from_json(path, w, h, bvh="lam")
+    cam = scenes.camera_rays(w, h, lambda pu, pv: o.camera_ray(pu, pv))
+    extra = scenes.random_rays(20000, seed=9)
+    if which == "box":
+        extra = extra * np.array([555] * 3 + [1] * 5, np.float32)
+    assert _compare(d, o, np.concatenate([cam, extra])) > 0.3
