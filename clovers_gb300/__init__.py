@@ -357,7 +357,7 @@ def resolve_srgb(xyz, width, height):
 
 def render(global_options: GlobalOptions, render_options: RenderOptions):
     """render.rs:81-183: load the scene, draw, write the requested formats."""
-    from .imageio import write_png, write_exr
+    from .imageio import format_duration, write_png, write_exr
     import time
 
     if not render_options.input.endswith(".json"):
@@ -367,7 +367,7 @@ def render(global_options: GlobalOptions, render_options: RenderOptions):
     pixels = draw(global_options, render_options, scene)
     duration = time.perf_counter() - t0
     if not global_options.quiet:
-        print("Finished render in %.3fs" % duration)
+        print("Finished render in %s" % format_duration(duration))
     written = []
     for fmt in render_options.formats:
         target = (render_options.output or os.path.join("renders", str(int(time.time())))) + "." + fmt

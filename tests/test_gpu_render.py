@@ -179,3 +179,36 @@ def test_profile_run_times_and_counts(box_scene_path):
         assert prof.ms_intersect > 0 and prof.ms_shade > 0 and prof.intersect_launches > 0
     assert runs[0] == runs[1]
     assert d.status() == 0
+
+
+def test_command_line_render_writes_png_and_exr(box_scene_path, tmp_path):
+    """python -m clovers_gb300 render (render.rs:81-183): the PNG holds the
+    resolved sRGB image with the reference's tEXt chunks, the EXR the XYZ(E)
+    film; both agree with draw() on the same options."""
+    import struct
+    import zlib
+    from clovers_gb300 import __main__ as cli
+    out = str(tmp_path / "img")
+    rc = cli.main(["-q", "render", "-i", box_scene_path, "-o", out, "-w", "40", "-h", "24", "-s", "8", "-d", "6",
+                   "-f", "png", "exr"])
+    assert rc == 0
+    png = open(out + ".png", "rb").read()
+    pos, idat, texts = 8, b"", []
+    while pos < len(png):
+        n = struct.unpack(">I", png[pos:pos + 4])[0]
+        tag = png[pos + 4:pos + 8]
+        if tag == b"IDAT":
+            idat += png[pos + 8:pos + 8 + n]
+        if tag == b"tEXt":
+            texts.append(png[pos + 8:pos + 8 + n].decode("latin-1"))
+        pos += 12 + n
+    rgb = np.frombuffer(zlib.decompress(idat), np.uint8).reshape(24, 1 + 3 * 40)[:, 1:].reshape(-1, 3)
+    assert texts[0].startswith("Comment\0Rendered with the clovers path tracing engine.") and texts[1] == "Software\0clovers"
+    ex = open(out + ".exr", "rb").read()
+    xyz_exr = np.frombuffer(ex[-(4 * 3 * 40):], "<f4").reshape(3, 40)  # last row: B, G, R planes
+    d = cg.Scene.from_json(box_scene_path, 40, 24).upload()
+    xyz = cg.draw(cg.GlobalOptions(quiet=True),
+                  cg.RenderOptions(input=box_scene_path, width=40, height=24, samples=8, max_depth=6), d)
+    assert np.allclose(xyz_exr[2], xyz.reshape(24, 40, 3)[23, :, 0], rtol=1e-5, atol=1e-7)
+    ref_rgb = cg.resolve_srgb(xyz, 40, 24)
+    assert np.abs(rgb.astype(int) - ref_rgb.astype(int)).max() <= 1
