@@ -203,8 +203,14 @@ def cpu_baseline_render(path, spp_sample):
     t0 = time.perf_counter()
     sc.render(W_IMG, H_IMG, spp_sample, DEPTH, SEED, threads=threads)
     el = time.perf_counter() - t0
+    rows, spp1 = 16, 16  # one core: a band of the image
+    t0 = time.perf_counter()
+    sc.render(W_IMG, H_IMG, spp1, DEPTH, SEED, window=(0, H_IMG // 2, W_IMG, H_IMG // 2 + rows), threads=1)
+    el1 = time.perf_counter() - t0
     return {"value": round(W_IMG * H_IMG * spp_sample / el / 1e6, 4), "unit": "Msamples/s", "cores": threads,
-            "kind": "port", "sample": "512x512 at %d spp (%.2f s)" % (spp_sample, el)}
+            "kind": "port", "sample": "%dx%d at %d spp (%.2f s)" % (W_IMG, H_IMG, spp_sample, el),
+            "one_core": {"value": round(W_IMG * rows * spp1 / el1 / 1e6, 4), "unit": "Msamples/s",
+                         "sample": "%d middle rows of %d pixels at %d spp (%.2f s)" % (rows, W_IMG, spp1, el1)}}
 
 
 CONFIGS = {
@@ -215,7 +221,7 @@ CONFIGS = {
     "c4": ("dispersive_prism", 1024, 1024, 256, 16, "dispersive prism + sphere, 1024x1024, depth 16 (plain)"),
     "box": ("enclosed_box", 512, 512, 256, 16, "enclosed box 512x512, 256 spp, depth 16"),
 }
-GOLDEN = {"c4": "prism", "box": "box", "c1": "spheres"}
+GOLDEN = {"c4": "prism", "box": "box", "c1": "spheres", "c3": "dense"}
 
 
 def config_scene_file(builder, tmp):
@@ -339,48 +345,89 @@ def run_config(args):
     print(json.dumps(line), flush=True)
 
 
-def time_to_relmse(args, gold, d, w, h, depth, film, stream, render, guided):
-    """GPU time until the relMSE of the golden crop (tests/golden/<gold>_ref.npz,
-    the oracle at 65,536 spp) reaches 1e-3: progressive passes of --chunk-spp
-    with the plain estimator, and (guided) with the online-trained guide."""
+def golden_sets(gold, w, h):
+    """The golden references of a workload (tests/golden/<gold>_ref.npz: the oracle in double precision at
+    65,536 spp): {set name: (buffer pixel indices, reference means)} for the 64x64 crop and the
+    stratified whole-image subset, and a description."""
     gpath = os.path.join(ROOT, "tests", "golden", "%s_ref.npz" % gold)
     if not os.path.exists(gpath):
         return None, None
     g = np.load(gpath)
     x0, r0, x1, r1 = [int(v) for v in g["window"]]
-    ref = g["mean"]
-    where = "oracle, 65536 spp, crop %s of %dx%d (tests/golden/%s_ref.npz)" % ([x0, r0, x1, r1], w, h, gold)
+    rr, xx = np.meshgrid(np.arange(r0, r1), np.arange(x0, x1), indexing="ij")
+    sets = {"crop": ((rr * w + xx).reshape(-1), g["mean"])}
+    if "sub_mean" in g.files:
+        sets["subset"] = (g["sub_pixels"].astype(np.int64), g["sub_mean"])
+    where = "oracle (%s), %d spp: crop %s of %dx%d, subset = centre pixel of every %dx%d cell (%d pixels); " \
+            "tests/golden/%s_ref.npz" % (str(g["precision"]) if "precision" in g.files else "f32", int(g["spp"]),
+                                         [x0, r0, x1, r1], w, h, int(g["sub_stride"]) if "sub_stride" in g.files else 0,
+                                         int(g["sub_stride"]) if "sub_stride" in g.files else 0,
+                                         len(sets["subset"][0]) if "subset" in sets else 0, gold)
+    return sets, where
 
-    def crop_relmse(total_spp):
-        img = (film.view(h, w, 3)[r0:r1, x0:x1].reshape(-1, 3) / total_spp).cpu().numpy()
-        return float(np.mean((img - ref) ** 2 / (ref ** 2 + 1e-2)))
 
+def progressive(render_pass, film, sets, w, h, max_spp, target=1e-3):
+    """Adds passes (render_pass(total_spp) -> (spp added, GPU ms)) to the film until the relMSE of every
+    golden set is <= target; returns per set the GPU time and spp at which it first got there."""
+    import torch
+    idx = {k: torch.as_tensor(v[0], device=film.device) for k, v in sets.items()}
+    total_ms, total_spp = 0.0, 0
+    first, last = {}, {}
+    while total_spp < max_spp and len(first) < len(sets):
+        n, ms = render_pass(total_spp)
+        total_ms += ms
+        total_spp += n
+        f = film.view(h * w, 3)
+        for k, (_, ref) in sets.items():
+            img = (f[idx[k]] / total_spp).cpu().numpy()
+            last[k] = float(np.mean((img - ref) ** 2 / (ref ** 2 + 1e-2)))
+            if k not in first and last[k] <= target:
+                first[k] = (total_ms, total_spp)
+    out = {}
+    for k in sets:
+        out[k] = {"reached": k in first, "gpu_ms": round(first[k][0], 2) if k in first else round(total_ms, 2),
+                  "spp": first[k][1] if k in first else total_spp, "relmse_last": last.get(k)}
+    return out, total_ms
+
+
+def time_to_relmse(args, gold, d, w, h, depth, film, stream, render, guided):
+    """GPU time until the relMSE against the golden references (crop and whole-image subset) reaches 1e-3:
+    progressive passes of --chunk-spp with the plain estimator, and (guided) with the online-trained guide."""
+    sets, where = golden_sets(gold, w, h)
+    if sets is None:
+        return None, None
     film.zero_()
-    total_ms, total_spp, chunk = 0.0, 0, args.chunk_spp
-    relmse = None
-    while total_spp < (0 if getattr(args, "guided_only", False) else args.max_spp):
-        total_ms += render(chunk, total_spp, seed=SEED + 1000)
-        total_spp += chunk
-        relmse = crop_relmse(total_spp)
-        if relmse <= 1e-3:
-            break
-    plain = {"target": 1e-3, "reached": bool(relmse is not None and relmse <= 1e-3), "gpu_ms": round(total_ms, 2),
-             "spp": total_spp, "relmse": relmse, "reference": where, "epsilon": 1e-2,
-             "estimator": "plain (BSDF + light mixture MIS)"}
+
+    def plain_pass(total_spp):
+        return args.chunk_spp, render(args.chunk_spp, total_spp, seed=SEED + 1000)
+
+    res, _ = ({}, 0) if getattr(args, "guided_only", False) else progressive(plain_pass, film, sets, w, h,
+                                                                               args.max_spp)
+    crop = res.get("crop", {})
+    plain = {"target": 1e-3, "reached": crop.get("reached", False), "gpu_ms": crop.get("gpu_ms"),
+             "spp": crop.get("spp"), "relmse": crop.get("relmse_last"), "sets": res, "reference": where,
+             "epsilon": 1e-2, "estimator": "plain (BSDF + light mixture MIS)"}
     gres = None
     if guided:  # one guided run per guide seed; the run of median GPU time stands for all
         seeds = [args.guide_seed] if args.guide_seed is not None else [int(x) for x in args.guide_seeds.split(",")]
         runs = []
         for sd in seeds:
-            r = run_guided(args, d, w, h, depth, film, stream, crop_relmse, where, sd)
+            r = run_guided(args, d, w, h, depth, film, stream, sets, where, sd)
             r["guide_seed"] = sd
             runs.append(r)
         runs.sort(key=lambda r: r["gpu_ms"] if r["reached"] else float("inf"))
         gres = dict(runs[(len(runs) - 1) // 2])
-        gres["runs"] = [{"guide_seed": r["guide_seed"], "gpu_ms": r["gpu_ms"], "spp": r["spp"], "reached": r["reached"]}
+        gres["runs"] = [{"guide_seed": r["guide_seed"], "gpu_ms": r["gpu_ms"], "spp": r["spp"], "reached": r["reached"],
+                         "subset_gpu_ms": r["sets"].get("subset", {}).get("gpu_ms")}
                         for r in sorted(runs, key=lambda r: r["guide_seed"])]
         gres["statistic"] = "median of %d guide seeds (the time to the target varies with the seed)" % len(runs)
-        gres["vs_plain_time"] = round(gres["gpu_ms"] / total_ms, 4) if total_ms > 0 else None
+        if plain["gpu_ms"]:
+            gres["vs_plain_time"] = round(gres["gpu_ms"] / plain["gpu_ms"], 4)
+        if "subset" in res and res["subset"]["reached"]:
+            sub = sorted(r["sets"]["subset"]["gpu_ms"] for r in runs if r["sets"].get("subset", {}).get("reached"))
+            if sub:
+                gres["subset_median_gpu_ms"] = sub[(len(sub) - 1) // 2]
+                gres["subset_vs_plain_time"] = round(gres["subset_median_gpu_ms"] / res["subset"]["gpu_ms"], 4)
     return plain, gres
 
 
@@ -413,12 +460,11 @@ def guided_vs_plain(args):
             "guided": guided, "guided_vs_plain_time": guided["vs_plain_time"] if guided else None}
 
 
-def run_guided(args, d, w, h, depth, film, stream, crop_relmse, where, guide_seed):
-    """Progressive guided render until the crop's relMSE reaches 1e-3: training
-    passes of --guide-pass-spp samples per pixel (the first with alpha 0), each
-    followed by --guide-steps Adam steps on its records, then passes of
-    --chunk-spp with the trained guide.  Every pass adds to the film (all are
-    unbiased); the GPU time includes rendering and training."""
+def run_guided(args, d, w, h, depth, film, stream, sets, where, guide_seed):
+    """Progressive guided render until the relMSE of every golden set reaches 1e-3: training
+    passes of --guide-pass-spp samples per pixel (the first with alpha 0), each followed by
+    --guide-steps Adam steps on its records, then passes of --chunk-spp with the trained guide.
+    Every pass adds to the film (all are unbiased); the GPU time includes rendering and training."""
     import torch
     import clovers_gb300 as cg
     from clovers_gb300 import _lib
@@ -426,9 +472,10 @@ def run_guided(args, d, w, h, depth, film, stream, crop_relmse, where, guide_see
     sp = stream.cuda_stream
     guide = cg.Guide(seed=guide_seed, learning_rate=args.guide_lr)
     film.zero_()
-    total_ms, total_spp, train_ms, k = 0.0, 0, 0.0, 0
-    relmse = None
-    while total_spp < args.max_spp:
+    state = {"k": 0, "train_ms": 0.0}
+
+    def guided_pass(total_spp):
+        k = state["k"]
         training = k < args.guide_passes
         n = args.guide_pass_spp if training else args.chunk_spp
         alpha = 0.0 if k == 0 else args.guide_alpha
@@ -442,17 +489,17 @@ def run_guided(args, d, w, h, depth, film, stream, crop_relmse, where, guide_see
             _lib.check(L.clv_guide_train(guide.handle, args.guide_steps, args.guide_batch, None, sp))
         e2.record(stream)
         e2.synchronize()
-        total_ms += e0.elapsed_time(e2)
-        train_ms += e1.elapsed_time(e2)
-        total_spp += n
-        k += 1
-        relmse = crop_relmse(total_spp)
-        if relmse <= 1e-3:
-            break
+        state["k"] = k + 1
+        state["train_ms"] += e1.elapsed_time(e2)
+        return n, e0.elapsed_time(e2)
+
+    res, _ = progressive(guided_pass, film, sets, w, h, args.max_spp)
     if guide.status():
         raise RuntimeError("guide kernels reported an error")
-    return {"target": 1e-3, "reached": bool(relmse is not None and relmse <= 1e-3), "gpu_ms": round(total_ms, 2),
-            "train_ms": round(train_ms, 2), "spp": total_spp, "relmse": relmse, "reference": where,
+    crop = res["crop"]
+    return {"target": 1e-3, "reached": crop["reached"], "gpu_ms": crop["gpu_ms"],
+            "train_ms": round(state["train_ms"], 2), "spp": crop["spp"], "relmse": crop["relmse_last"],
+            "sets": res, "reference": where,
             "estimator": "guided: alpha %.2f of Lambertian bounces from the vMF-mixture MLP (one-sample MIS with "
                          "the plain mixture); %d training passes of %d spp, %d Adam steps of %d records each" % (
                              args.guide_alpha, args.guide_passes, args.guide_pass_spp, args.guide_steps,
@@ -480,6 +527,8 @@ def main():
     ap.add_argument("--batch", action="store_true", help="measure the batched multi-scene workload")
     ap.add_argument("--batch-scenes", type=int, default=64)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline legs")
+    ap.add_argument("--no-parity", action="store_true",
+                    help="skip the check of every timed ray cast against the oracle (untimed, about 40 s of CPU)")
     ap.add_argument("--guided", action="store_true", help="with --config: also the guided time to relMSE 1e-3")
     ap.add_argument("--no-guided", action="store_true", help="skip the guided-vs-plain section of the default run")
     ap.add_argument("--no-autotune", action="store_true", help="skip the wavefront shape search before the timed render")
@@ -699,16 +748,41 @@ def main():
                              "peak": hbm_peak, "unit": "GB/s", "frac": round(r_ach / hbm_peak, 4),
                              "traffic": traffic.get("raycast_persist_kernel.bytes_per_launch"),
                              "algorithmic_bytes_per_launch": int(rbytes)}}
-        if rank == 0 and world == 1 and not args.no_cpu:
+        if rank == 0 and world == 1 and (not args.no_cpu or not args.no_parity):
             import oracle
-            om = oracle.Scene.from_mesh(v, idx)
-            n_cpu = 1 << 17
             t0 = time.perf_counter()
-            om.raycast(rays_h[:n_cpu], threads=os.cpu_count() or 1)
-            el = time.perf_counter() - t0
-            trav["cpu_baseline"] = {"value": round(n_cpu / el / 1e9, 6), "unit": "Grays/s",
-                                    "cores": os.cpu_count() or 1, "kind": "port",
-                                    "sample": "first %d of the 2^24 rays (%.2f s)" % (n_cpu, el)}
+            om = oracle.Scene.from_mesh(v, idx)  # the oracle builds its own SAH tree over the same triangles
+            build_s = time.perf_counter() - t0
+            threads = os.cpu_count() or 1
+            if not args.no_cpu:
+                n_cpu = 1 << 17
+                t0 = time.perf_counter()
+                om.raycast(rays_h[:n_cpu], threads=threads)
+                el = time.perf_counter() - t0
+                n1 = 1 << 13
+                t0 = time.perf_counter()
+                om.raycast(rays_h[:n1], threads=1)
+                el1 = time.perf_counter() - t0
+                trav["cpu_baseline"] = {"value": round(n_cpu / el / 1e9, 6), "unit": "Grays/s", "cores": threads,
+                                        "kind": "port", "sample": "first %d of the 2^24 rays (%.2f s)" % (n_cpu, el),
+                                        "one_core": {"value": round(n1 / el1 / 1e9, 7), "unit": "Grays/s",
+                                                     "sample": "first %d rays (%.2f s)" % (n1, el1)}}
+            if not args.no_parity:
+                # every ray of the timed workload against the oracle: hit ids and distance bits
+                gp = prim.cpu().numpy().view(np.uint32)
+                gt = tt.cpu().numpy()
+                t0 = time.perf_counter()
+                op, ot = om.raycast(rays_h, threads=threads)
+                cast_s = time.perf_counter() - t0
+                hit = op != 0xFFFFFFFF
+                same_id = gp == op
+                both = hit & same_id
+                ulp = np.abs(gt[both].view(np.int32).astype(np.int64) - ot[both].view(np.int32).astype(np.int64))
+                trav["parity"] = {"rays_checked": int(RAYS), "id_mismatches": int((~same_id).sum()),
+                                  "t_mismatches": int((ulp != 0).sum()), "max_t_ulp": int(ulp.max()) if ulp.size else 0,
+                                  "hits": int(hit.sum()),
+                                  "oracle": "CPU restatement of BVHNode::hit / Triangle::hit over its own SAH build "
+                                            "(%.1f s build, %.1f s cast on %d threads)" % (build_s, cast_s, threads)}
         line["traversal"] = trav
         if args.no_render:
             line.update(value=trav["value"], ms_per_step=trav["ms_per_step"])

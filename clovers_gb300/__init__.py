@@ -152,13 +152,13 @@ class DeviceScene:
         return [(r.path_slots, r.shade_blocks_per_sm, r.ms) for r in res[:n.value]]
 
 
-def render_opts(opts: RenderOptions, sample_offset=0, samples_per_thread=0, engine=0, path_slots=0):
+def render_opts(opts: RenderOptions, sample_offset=0, path_slots=0):
     if opts.sampler != "random":
         raise ClvError(_lib.CLV_E_INVALID, "only the random sampler is supported")
     if opts.mode not in _lib.MODES:
         raise ValueError("unknown render mode %r" % opts.mode)
     return _lib.RenderOptsC(opts.width, opts.height, opts.samples, opts.max_depth, _lib.MODES[opts.mode], 0,
-                            opts.seed, sample_offset, samples_per_thread, engine, path_slots)
+                            opts.seed, sample_offset, path_slots)
 
 
 def initialize(path, bvh, width, height):
@@ -167,10 +167,10 @@ def initialize(path, bvh, width, height):
 
 
 def draw(global_options: GlobalOptions, render_options: RenderOptions, scene: DeviceScene, sampler=None,
-         stats=None, engine="wavefront"):
+         stats=None):
     """draw_cpu::draw: the (height*width, 3) float32 XYZ(E) pixel buffer, row 0 at the top."""
     del global_options, sampler
-    o = render_opts(render_options, engine={"wavefront": 0, "megakernel": 1}[engine])
+    o = render_opts(render_options)
     out = np.empty((render_options.height * render_options.width, 3), dtype=np.float32)
     st = _lib.StatsC()
     check(lib().clv_render(scene.handle, ctypes.byref(o), out.ctypes.data, ctypes.byref(st)))

@@ -23,7 +23,7 @@ MODES = {"path-tracing": 0, "normal-map": 1, "bvh-test-count": 2, "primitive-tes
 class RenderOptsC(ctypes.Structure):
     _fields_ = [("width", c_u32), ("height", c_u32), ("samples", c_u32), ("max_depth", c_u32),
                 ("mode", c_u32), ("sampler", c_u32), ("seed", c_u64), ("sample_offset", c_u32),
-                ("samples_per_thread", c_u32), ("engine", c_u32), ("path_slots", c_u32)]
+                ("path_slots", c_u32)]
 
 
 class SceneInfoC(ctypes.Structure):
@@ -75,6 +75,7 @@ SIGNATURES = {
                                    ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "clv_device_status": (c_i32, [ctypes.c_void_p, P(c_u32)]),
     "clv_selftest_division": (c_i32, [c_u64, c_u64, P(c_u64)]),
+    "clv_selftest_log": (c_i32, [ctypes.c_void_p, ctypes.c_void_p, c_u64, P(c_f64), P(c_u64)]),
     "clv_kernel_launches": (c_u64, []),
     "clv_device_alloc": (c_i32, [c_u64, P(ctypes.c_void_p)]),
     "clv_device_free": (None, [ctypes.c_void_p]),
@@ -95,6 +96,7 @@ SIGNATURES = {
     "clv_guide_gradient": (c_i32, [ctypes.c_void_p, ctypes.c_void_p, c_u64, ctypes.c_void_p, P(c_f64)]),
     "clv_guide_status": (c_i32, [ctypes.c_void_p, P(c_u32)]),
     "clv_guide_selftest_mma": (c_i32, [c_u32, c_u32, c_u64, ctypes.c_void_p, P(c_f32)]),
+    "clv_guide_selftest_timeout": (c_i32, [c_u64, P(c_u32), P(c_u32)]),
     "clv_last_error": (ctypes.c_char_p, []),
     "clv_version": (ctypes.c_char_p, []),
 }

@@ -2,10 +2,9 @@
 //
 //  raycast_persist_kernel  closest-hit ray casts (the parity path), persistent
 //                  threads over rays sorted by origin
-//  render_kernel   path tracing: one thread per (pixel, chunk of samples);
-//                  camera ray -> trace (clovers-cli/src/trace.rs:21-122, as a
-//                  loop) -> film rule (draw_cpu.rs:131-142) -> f64 sums
+//  debug_kernel    the debug render modes, one ray per pixel
 //  resolve_kernel  f64 film -> mean XYZ(E) -> sRGB u8 (write.rs:39-44)
+// Path tracing is the wavefront of wavefront.cuh.
 
 #include <cuda_runtime.h>
 
@@ -13,6 +12,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <mutex>
@@ -108,6 +108,9 @@ __global__ void ray_scatter(const uint32_t* __restrict__ key, uint64_t n, uint32
 #ifndef CLV_SHADE_BLOCKS
 #define CLV_SHADE_BLOCKS 8  // shading-kernel blocks per SM when no tuned shape is set (one wave at 8 resident)
 #endif
+// Largest traversal-stack spill region (trees deeper than CLV_STACK levels):
+// deep scenes run fewer threads or path slots rather than exceed it.
+static constexpr uint64_t kSpillBudget = 4ull << 30;
 #ifndef CLV_SHSTACK
 // ray casts: the first 12 stack entries of each thread in shared memory (24 KB
 // per block, the most that keeps 9 blocks per SM; measured best of 0..24)
@@ -119,21 +122,30 @@ __global__ void ray_scatter(const uint32_t* __restrict__ key, uint64_t n, uint32
 #ifndef CLV_MINB_RAY
 #define CLV_MINB_RAY 9  // 56 registers, no spills: 36 warps per SM (measured best of 6..16)
 #endif
-template <int CPLX, bool COUNT, int WT>
+// DEEP: trees deeper than CLV_STACK levels; stack entries beyond CLV_STACK go
+// to `spill` (SpillStack, one column per thread of the grid, `cap` entries).
+template <int CPLX, bool COUNT, int WT, bool DEEP = false>
 __global__ void __launch_bounds__(128, CLV_MINB_RAY) raycast_persist_kernel(
     ClvDeviceScene S, const float4* __restrict__ rays, uint64_t n, uint32_t* __restrict__ prim,
     float* __restrict__ tout, uint32_t* __restrict__ nodes, uint32_t* __restrict__ tests, uint32_t* err,
-    unsigned long long* next, const uint32_t* __restrict__ perm) {
+    unsigned long long* next, const uint32_t* __restrict__ perm, float4* spill, int cap) {
   const int lane = threadIdx.x & 31;
   Trav T;
 #if CLV_SHSTACK
-  __shared__ float4 sh_stack[CLV_SHSTACK * 128];
-  float4 loc_stack[CLV_STACK - CLV_SHSTACK];
-  HybridStack<CLV_SHSTACK> stack{sh_stack + threadIdx.x, loc_stack};
-#else
-  float4 stack_mem[CLV_STACK];
-  float4* stack = stack_mem;
+  __shared__ float4 sh_stack[DEEP ? 1 : CLV_SHSTACK * 128];
 #endif
+  float4 loc_stack[DEEP ? CLV_STACK : CLV_STACK - CLV_SHSTACK];
+  auto stack = [&] {
+    if constexpr (DEEP) {
+      return SpillStack{loc_stack, spill + (size_t)blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x, cap};
+    } else {
+#if CLV_SHSTACK
+      return HybridStack<CLV_SHSTACK>{sh_stack + threadIdx.x, loc_stack};
+#else
+      return (float4*)loc_stack;
+#endif
+    }
+  }();
   Hit h;
   Counters c{0u, 0u};
   Ray r{};
@@ -182,196 +194,18 @@ __global__ void __launch_bounds__(128, CLV_MINB_RAY) raycast_persist_kernel(
 }
 
 struct RenderParams {
-  uint32_t width, height, spp, max_depth;
-  uint32_t sample_offset, spt, chunks;
+  uint32_t width, height;
+  uint32_t sample_offset;
   uint32_t mode;
   uint64_t seed;
   uint64_t npix;
 };
 
-__device__ __forceinline__ void rotate_wavelength(int hero, int w[4]) {  // wavelength.rs:55-60
-#pragma unroll
-  for (int j = 0; j < 4; ++j) w[j] = 380 + (hero - 380 + j * 100) % 400;
-}
-
-// The camera ray of one sample (draw_cpu.rs:113-127, camera.rs:103-126).
-__device__ __forceinline__ Ray camera_ray(const ClvDeviceScene& S, const RenderParams& P, uint32_t x, uint32_t row,
-                                          uint32_t sample, Rng& rng) {
-  rng.init(P.seed, row * P.width + x, sample);
-  const float ox = rng.f32(), oy = rng.f32();
-  float lx, ly;
-  random_in_unit_disk(rng, lx, ly);
-  const float time = rng.f32();
-  const int lambda = random_wavelength(rng);
-  const uint32_t y = P.height - 1 - row;  // draw_cpu.rs:51: buffer row 0 is the top of the image
-  const float pu = ((float)x + ox) / (float)P.width;
-  const float pv = ((float)y + oy) / (float)P.height;
-  const ClvCamera& C = S.camera;
-  lx *= C.lens_radius;
-  ly *= C.lens_radius;
-  const V off = add(scl(lx, ld3(C.u)), scl(ly, ld3(C.v)));
-  const V dir = sub(sub(add(add(ld3(C.llc), scl(pu, ld3(C.horizontal))), scl(pv, ld3(C.vertical))), ld3(C.origin)), off);
-  return Ray{add(ld3(C.origin), off), unit(dir), time, lambda};
-}
-
-// trace() as a loop: the path throughput `beta` carries the products of the
-// recursion's attenuation factors.
-__device__ void trace_path(const ClvDeviceScene& S, Ray ray, uint32_t max_depth, Rng& rng, float p[4], uint32_t* err) {
-  const int hero = ray.lambda;
-  int waves[4];
-  rotate_wavelength(hero, waves);
-  float L[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-  float beta[4] = {1.0f, 1.0f, 1.0f, 1.0f};
-  for (uint32_t depth = 0;; ++depth) {
-    if (depth > max_depth) break;
-    Hit h;
-    Rec full;
-    if (!closest_hit<2>(S, ray, CLV_EPS_ACNE, CLV_FLT_MAX, &rng, h, &full, nullptr, err)) {
-#pragma unroll
-      for (int i = 0; i < 4; ++i) L[i] += beta[i] * spd_get(S, S.background_spd, waves[i]);
-      break;
-    }
-    Rec rec;
-    hit_record(S, ray, h, full, rec);
-    const ClvMaterial& m = S.materials[rec.mat];
-    const uint32_t kind = m.kind;
-    if (kind == CLV_MAT_DIFFUSELIGHT || kind == CLV_MAT_CONELIGHT) {  // no scatter: emitted only
-#pragma unroll
-      for (int i = 0; i < 4; ++i) L[i] += beta[i] * mat_emit(S, m, ray, waves[i], rec);
-      break;
-    }
-    // emission of the remaining kinds is 0 and adds nothing
-    Ray next;
-    next.time = ray.time;
-    next.lambda = ray.lambda;
-    next.o = rec.p;
-    bool specular = true;
-    float spdf = 0.0f, mis = 1.0f;
-    if (kind == CLV_MAT_METAL) {  // metal.rs:27-51
-      const V refl = reflect(ray.d, rec.n);
-      next.d = unit(add(refl, scl(m.fuzz, random_unit_vector(rng))));
-    } else if (kind == CLV_MAT_DIELECTRIC || kind == CLV_MAT_DISPERSIVE) {  // dielectric.rs / dispersive.rs
-      const float ri = kind == CLV_MAT_DIELECTRIC ? m.refractive_index : dispersive_index(m, ray.lambda);
-      const float ratio = rec.front ? 1.0f / ri : ri;
-      const float ct = fminf(-dot(ray.d, rec.n), 1.0f);
-      const float st = sqrtf(1.0f - ct * ct);
-      if (ratio * st > 1.0f) {
-        next.d = reflect(ray.d, rec.n);
-      } else {
-        const float rp = schlick(ct, ratio);
-        next.d = rng.f32() < rp ? reflect(ray.d, rec.n) : refract(ray.d, rec.n, ratio);
-      }
-    } else {  // Lambertian (CosinePDF) or Isotropic (SpherePDF): MixturePDF with the light tree
-      specular = false;
-      const bool lamb = kind == CLV_MAT_LAMBERTIAN;
-      V gen;
-      if (rng.boolean()) {
-        gen = mis_random(S, rec.p, rng);
-      } else if (lamb) {  // CosinePDF::generate: ONB::build_from_w(normal).local(cosine dir)
-        const V w = rec.n;
-        const V a = fabsf(w.x) > 0.9f ? unit(mk(0.0f, 1.0f, 0.0f)) : unit(mk(1.0f, 0.0f, 0.0f));
-        const V vv = unit(cross(w, a));
-        const V uu = unit(cross(w, vv));
-        const V c = random_cosine_direction(rng);
-        gen = unit(add(add(scl(c.x, uu), scl(c.y, vv)), scl(c.z, w)));
-      } else {
-        gen = random_unit_vector(rng);
-      }
-      next.d = unit(gen);
-      const float light_v = mis_pdf(S, rec.p, next.d, hero, ray.time, err);
-      float bsdf_v;
-      if (lamb) {
-        const float cosine = dot(unit(next.d), rec.n);
-        bsdf_v = cosine <= 0.0f ? 0.0f : cosine / CLV_PI;
-      } else {
-        bsdf_v = 1.0f / (4.0f * CLV_PI);
-      }
-      mis = 0.5f * light_v + 0.5f * bsdf_v;
-      if (lamb) {  // Lambertian::scattering_pdf: None below the surface
-        const float c = dot(rec.n, unit(next.d));
-        if (c < 0.0f) break;
-        spdf = c / CLV_PI;
-      } else {
-        spdf = 1.0f / (4.0f * CLV_PI);
-      }
-    }
-    // attenuation: hero only on wavelength-dependent materials (trace.rs:61-70)
-    float atten[4];
-    if (m.wavelength_dependent) {
-      atten[0] = mat_color(S, m, ray, hero, rec);
-      atten[1] = atten[2] = atten[3] = 0.0f;
-    } else {
-#pragma unroll
-      for (int i = 0; i < 4; ++i) atten[i] = mat_color(S, m, ray, waves[i], rec);
-    }
-    if (specular) {
-#pragma unroll
-      for (int i = 0; i < 4; ++i) beta[i] = beta[i] * atten[i];
-    } else {
-#pragma unroll
-      for (int i = 0; i < 4; ++i) beta[i] = beta[i] * (atten[i] * spdf / mis);
-    }
-    ray = next;
-  }
-#pragma unroll
-  for (int i = 0; i < 4; ++i) p[i] = L[i];
-}
-
-__device__ __forceinline__ bool is_normal_pos(float v) {
-  const float a = fabsf(v);
-  return v > 0.0f && a >= 1.17549435e-38f && a <= 3.40282347e+38f;
-}
-
-__global__ void __launch_bounds__(128) render_kernel(ClvDeviceScene S, RenderParams P, double* __restrict__ film,
-                                                     uint32_t* err) {
-  const uint64_t total = P.npix * (uint64_t)P.chunks;
-  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; tid < total; tid += stride) {
-    const uint64_t pix = tid % P.npix;
-    const uint32_t chunk = (uint32_t)(tid / P.npix);
-    const uint32_t x = (uint32_t)(pix % P.width), row = (uint32_t)(pix / P.width);
-    const uint32_t s0 = chunk * P.spt, s1 = min(P.spp, s0 + P.spt);
-    double acc0 = 0.0, acc1 = 0.0, acc2 = 0.0;
-    for (uint32_t s = s0; s < s1; ++s) {
-      Rng rng;
-      const Ray ray = camera_ray(S, P, x, row, s + P.sample_offset, rng);
-      int waves[4];
-      rotate_wavelength(ray.lambda, waves);
-      float p[4];
-      trace_path(S, ray, P.max_depth, rng, p, err);
-      // film rule, draw_cpu.rs:131-142
-      if (p[1] == 0.0f && p[2] == 0.0f && p[3] == 0.0f) {
-        const float* c = S.cmf + 3 * (waves[0] - 380);
-        acc0 += (double)(__ldg(c) * p[0]);
-        acc1 += (double)(__ldg(c + 1) * p[0]);
-        acc2 += (double)(__ldg(c + 2) * p[0]);
-      } else {
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          if (is_normal_pos(p[i])) {
-            const float* c = S.cmf + 3 * (waves[i] - 380);
-            acc0 += (double)(__ldg(c) * p[i] / 4.0f);
-            acc1 += (double)(__ldg(c + 1) * p[i] / 4.0f);
-            acc2 += (double)(__ldg(c + 2) * p[i] / 4.0f);
-          }
-        }
-      }
-    }
-    double* f = film + 3 * pix;
-    if (P.chunks == 1) {
-      f[0] += acc0;
-      f[1] += acc1;
-      f[2] += acc2;
-    } else {
-      atomicAdd(f, acc0);
-      atomicAdd(f + 1, acc1);
-      atomicAdd(f + 2, acc2);
-    }
-  }
-}
-
 // Debug render modes (draw_cpu.rs:148-207): one centred ray per pixel.
-__global__ void debug_kernel(ClvDeviceScene S, RenderParams P, double* __restrict__ film, uint32_t* err) {
+// spill (trees deeper than CLV_STACK levels, else null): stack entries beyond
+// CLV_STACK, one column per pixel.
+__global__ void debug_kernel(ClvDeviceScene S, RenderParams P, double* __restrict__ film, uint32_t* err,
+                             float4* spill) {
   const uint64_t pix = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (pix >= P.npix) return;
   const uint32_t x = (uint32_t)(pix % P.width), row = (uint32_t)(pix / P.width);
@@ -388,7 +222,9 @@ __global__ void debug_kernel(ClvDeviceScene S, RenderParams P, double* __restric
   Hit h;
   Rec full;
   Counters c{0u, 0u};
-  const bool any = closest_hit<2>(S, r, CLV_EPS_ACNE, CLV_FLT_MAX, &rng, h, &full, &c, err);
+  float4 loc[CLV_STACK];
+  SpillStack stack{loc, spill ? spill + pix : nullptr, (uint32_t)P.npix, spill ? (int)S.max_depth_tree : CLV_STACK};
+  const bool any = closest_hit_stk<2, CLV_WT_SCENE>(S, r, CLV_EPS_ACNE, CLV_FLT_MAX, &rng, h, &full, &c, err, stack);
   if (P.mode == CLV_MODE_NORMAL_MAP) {  // normals.rs:11-37
     if (any) {
       Rec rec;
@@ -490,6 +326,45 @@ __global__ void selftest_division_kernel(uint64_t n, uint64_t seed, int mode, un
     if (__float_as_uint(q) != __float_as_uint(e) && !(q != q && e != e) && !(q == 0.0f && e == 0.0f)) ++local;
   }
   if (local) atomicAdd(bad, local);
+}
+
+// Self-test of the render path's logarithm (clv_log.h) over every f32 in
+// (0, 1] (bit patterns 1 .. 0x3F800000): the largest error in f32 ulps against
+// the GPU's double-precision log, and how many results are not the nearest
+// f32 of that value.  The media's free-flight draws take logs of draws in
+// [0, 1).
+__global__ void selftest_log_kernel(unsigned long long* max_err_bits, unsigned long long* not_nearest) {
+  const uint32_t top = 0x3F800000u;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  double worst = 0.0;
+  unsigned long long nn = 0;
+  for (uint32_t b = 1u + blockIdx.x * blockDim.x + threadIdx.x; b <= top; b += stride) {
+    const float x = __uint_as_float(b);
+    const float y = clv_math::log_f32(x);
+    const double r = log((double)x);
+    if (r != 0.0) {
+      int e;
+      frexp(fabs(r), &e);
+      const double err = fabs((double)y - r) / ldexp(1.0, e - 24);  // f32 ulp at |r|: 2^(e-24)
+      worst = fmax(worst, err);
+      if (y != (float)r) ++nn;
+    } else if (y != 0.0f) {
+      worst = 1e30;
+    }
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    worst = fmax(worst, __shfl_down_sync(0xFFFFFFFFu, worst, off));
+    nn += __shfl_down_sync(0xFFFFFFFFu, nn, off);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(max_err_bits, (unsigned long long)__double_as_longlong(worst));  // non-negative: bits order as values
+    if (nn) atomicAdd(not_nearest, nn);
+  }
+}
+__global__ void log_eval_kernel(const float* __restrict__ x, float* __restrict__ y, uint64_t n) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] = clv_math::log_f32(x[i]);
 }
 
 // --------------------------------------------------------------- host side --
@@ -649,6 +524,21 @@ struct clv_device_scene {
   unsigned long long* ray_next = nullptr;  // work counter of the persistent ray casts
   uint32_t* ray_sort = nullptr;            // ray order: histogram, keys, permutation
   uint64_t ray_sort_cap = 0;               // rays the sort scratch holds
+  float4* spill = nullptr;   // traversal stack spill of trees deeper than CLV_STACK levels
+  size_t spill_bytes = 0;
+  float4* spill_region(size_t bytes) {
+    if (bytes > spill_bytes) {
+      if (spill) cudaFree(spill);
+      spill = nullptr;
+      spill_bytes = 0;
+      ck(cudaMalloc(&spill, bytes), "cudaMalloc stack spill");
+      spill_bytes = bytes;
+    }
+    return spill;
+  }
+  bool deep() const { return view.max_depth_tree > CLV_STACK; }
+  // spilled entries per thread of a deep tree (the stack holds tree depth - 1 at most)
+  uint32_t spill_entries() const { return deep() ? view.max_depth_tree - CLV_STACK : 0u; }
   uint32_t* ray_sort_scratch(uint64_t n) {
     if (n > ray_sort_cap) {
       if (ray_sort) cudaFree(ray_sort);
@@ -669,10 +559,12 @@ struct clv_device_scene {
   ~clv_device_scene() {
     if (cap_stream) cudaStreamDestroy(cap_stream);
     if (ray_sort) cudaFree(ray_sort);
+    if (spill) cudaFree(spill);
     for (void* p : owned) cudaFree(p);  // scene arrays, error word and ray counter
     if (scratch) cudaFree(scratch);
     if (wf_mem) cudaFree(wf_mem);
     if (wf_counters) cudaFree(wf_counters);
+    if (order_mem) cudaFree(order_mem);
     if (wf_live_host) cudaFreeHost(wf_live_host);
   }
   WfState wavefront_state(uint32_t q) {
@@ -701,9 +593,30 @@ struct clv_device_scene {
     W.grec = nullptr;
     W.grec_count = nullptr;
     W.grec_cap = 0;
+    W.spill = nullptr;
+    W.stack_cap = CLV_STACK;
+    W.order = nullptr;
+    W.order_key = nullptr;
+    W.order_hist = nullptr;
     return W;
   }
   static constexpr size_t kWfSlotBytes = 16 * 5 + 48 + 8 + 16;
+  // query order of the wavefront intersect: order and key per slot, bin counts
+  void* order_mem = nullptr;
+  uint32_t order_slots = 0;
+  void query_order(WfState& W) {
+    if (W.Q > order_slots) {
+      if (order_mem) cudaFree(order_mem);
+      order_mem = nullptr;
+      order_slots = 0;
+      ck(cudaMalloc(&order_mem, (size_t)W.Q * 8 + 4096), "cudaMalloc query order");
+      order_slots = W.Q;
+    }
+    char* p = static_cast<char*>(order_mem);
+    W.order_hist = reinterpret_cast<uint32_t*>(p);
+    W.order = reinterpret_cast<uint32_t*>(p + 4096);
+    W.order_key = W.order + W.Q;
+  }
   void* ensure_scratch(size_t bytes) {
     if (bytes > scratch_bytes) {
       if (scratch) cudaFree(scratch);
@@ -760,6 +673,16 @@ static GraphExec capture_graph(clv_device_scene* d, F enqueue) {
   return g;
 }
 
+// Whether single-scene wavefront renders group their queries (wf_order_*)
+// before each intersect.  CLV_QUERY_ORDER=0 in the environment turns it off.
+static bool query_order_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("CLV_QUERY_ORDER");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+
 static uint32_t launch_grid(uint64_t work, int block) {
   const uint64_t want = (work + block - 1) / block;
   const uint64_t cap = (uint64_t)sm_count() * 16;  // persistent-style grid-stride cap
@@ -774,7 +697,6 @@ static int check_opts(const clv_device_scene* d, const clv_render_opts* o) {
   if (o->samples == 0) return fail(CLV_E_INVALID, "samples must be positive");
   if (o->sampler != 0) return fail(CLV_E_INVALID, "only the random sampler is supported (blue-noise tables are absent)");
   if (o->mode > CLV_MODE_PRIMITIVE_TEST_COUNT) return fail(CLV_E_INVALID, "unknown render mode");
-  if (o->engine > 1) return fail(CLV_E_INVALID, "unknown render engine");
   if ((uint64_t)o->width * o->height > 0x1FFFFFFFull) return fail(CLV_E_INVALID, "image too large");
   return CLV_OK;
 }
@@ -783,21 +705,10 @@ static RenderParams make_params(const clv_render_opts* o) {
   RenderParams P{};
   P.width = o->width;
   P.height = o->height;
-  P.spp = o->samples;
-  P.max_depth = o->max_depth;
   P.sample_offset = o->sample_offset;
   P.mode = o->mode;
   P.seed = o->seed;
   P.npix = (uint64_t)o->width * o->height;
-  uint32_t spt = o->samples_per_thread;
-  if (spt == 0) {
-    // enough threads to fill the GPU several times over, otherwise long chunks
-    const uint64_t target = (uint64_t)sm_count() * 2048 * 4;
-    const uint64_t chunks = std::max<uint64_t>(1, std::min<uint64_t>(o->samples, (target + P.npix - 1) / P.npix));
-    spt = (uint32_t)((o->samples + chunks - 1) / chunks);
-  }
-  P.spt = std::max<uint32_t>(1, std::min(spt, o->samples));
-  P.chunks = (o->samples + P.spt - 1) / P.spt;
   return P;
 }
 
@@ -837,7 +748,7 @@ int clv_render_profile_run(clv_device_scene* d, const clv_render_opts* o, double
   int rc = check_opts(d, o);
   if (rc) return rc;
   if (!film_dev || !out) return fail(CLV_E_INVALID, "null argument");
-  if (o->mode != CLV_MODE_PATH_TRACING || o->engine != 0)
+  if (o->mode != CLV_MODE_PATH_TRACING)
     return fail(CLV_E_INVALID, "profiling covers the wavefront path tracer only");
   // device times of the production kernels ...
   rc = render_wavefront(d, o, film_dev, (cudaStream_t)stream, out, nullptr, 0.0f, false);
@@ -873,7 +784,7 @@ int clv_autotune(clv_device_scene* d, const clv_render_opts* o, clv_tune_result*
                  uint32_t* n_results, void* stream) {
   int rc = check_opts(d, o);
   if (rc) return rc;
-  if (o->mode != CLV_MODE_PATH_TRACING || o->engine != 0)
+  if (o->mode != CLV_MODE_PATH_TRACING)
     return fail(CLV_E_INVALID, "tuning covers the wavefront path tracer only");
   cudaStream_t st = (cudaStream_t)stream;
   double* film = nullptr;
@@ -952,6 +863,39 @@ int clv_selftest_division(uint64_t n, uint64_t seed, uint64_t* mismatches) {
   }
 }
 
+int clv_selftest_log(const float* x, float* y, uint64_t n, double* max_ulp, uint64_t* not_nearest) {
+  if (!max_ulp || !not_nearest || (n && (!x || !y))) return fail(CLV_E_INVALID, "null argument");
+  void* buf = nullptr;
+  try {
+    const size_t io = (size_t)n * sizeof(float);
+    ck(cudaMalloc(&buf, 16 + 2 * io), "cudaMalloc");
+    unsigned long long* acc = static_cast<unsigned long long*>(buf);
+    ck(cudaMemset(acc, 0, 16), "cudaMemset");
+    selftest_log_kernel<<<sm_count() * 8, 256>>>(acc, acc + 1);
+    g_launches += 1;
+    if (n) {
+      float* dx = reinterpret_cast<float*>(static_cast<char*>(buf) + 16);
+      float* dy = dx + n;
+      ck(cudaMemcpy(dx, x, io, cudaMemcpyHostToDevice), "cudaMemcpy H2D");
+      log_eval_kernel<<<(uint32_t)((n + 255) / 256), 256>>>(dx, dy, n);
+      g_launches += 1;
+      ck(cudaMemcpy(y, dy, io, cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
+    }
+    unsigned long long h[2];
+    ck(cudaMemcpy(h, acc, sizeof h, cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
+    cudaFree(buf);
+    buf = nullptr;
+    double m;
+    std::memcpy(&m, &h[0], sizeof m);
+    *max_ulp = m;
+    *not_nearest = h[1];
+    return CLV_OK;
+  } catch (std::exception& e) {
+    if (buf) cudaFree(buf);
+    return fail(CLV_E_CUDA, e.what());
+  }
+}
+
 int clv_scene_load_json_text(const char* json, const char* base_dir, uint32_t width, uint32_t height, int bvh_alg,
                              clv_scene** out) {
   if (!json || !out) return fail(CLV_E_INVALID, "null argument");
@@ -959,7 +903,6 @@ int clv_scene_load_json_text(const char* json, const char* base_dir, uint32_t wi
   try {
     std::unique_ptr<clv_scene> s(new clv_scene());
     s->host = clv::load_scene_text(json, width, height, base_dir ? base_dir : ".", bvh_alg == CLV_BVH_LAM);
-    if (s->host.tree_depth > CLV_STACK) return fail(CLV_E_SCENE, "BVH deeper than the traversal stack");
     if (s->host.mis_depth > CLV_MIS_STACK) return fail(CLV_E_SCENE, "MIS tree deeper than its evaluation stack");
     *out = s.release();
     return CLV_OK;
@@ -974,7 +917,6 @@ int clv_scene_load_json(const char* path, uint32_t width, uint32_t height, int b
   try {
     std::unique_ptr<clv_scene> s(new clv_scene());
     s->host = clv::load_scene_json(path, width, height, bvh_alg == CLV_BVH_LAM);
-    if (s->host.tree_depth > CLV_STACK) return fail(CLV_E_SCENE, "BVH deeper than the traversal stack");
     if (s->host.mis_depth > CLV_MIS_STACK) return fail(CLV_E_SCENE, "MIS tree deeper than its evaluation stack");
     *out = s.release();
     return CLV_OK;
@@ -989,7 +931,6 @@ int clv_scene_from_mesh(const float* verts, uint32_t nverts, const uint32_t* ind
   try {
     std::unique_ptr<clv_scene> s(new clv_scene());
     s->host = clv::mesh_scene(verts, nverts, indices, ntris);
-    if (s->host.tree_depth > CLV_STACK) return fail(CLV_E_SCENE, "BVH deeper than the traversal stack");
     *out = s.release();
     return CLV_OK;
   } catch (std::exception& e) {
@@ -1112,8 +1053,19 @@ int clv_raycast_device(const clv_device_scene* d, const float* rays_dev, uint64_
   const int block = 128;
   g_launches += 1;
   // persistent grid: every resident block of the launch bound on every SM
-  const uint32_t grid = (uint32_t)std::max<uint64_t>(
+  uint32_t grid = (uint32_t)std::max<uint64_t>(
       1, std::min<uint64_t>((n + block - 1) / block, (uint64_t)sm_count() * CLV_MINB_RAY));
+  float4* spill = nullptr;
+  const uint32_t spill_entries = d->spill_entries();
+  if (spill_entries) {  // deep tree: fewer threads if the spill region would exceed its budget
+    const uint64_t per_block = (uint64_t)block * spill_entries * sizeof(float4);
+    grid = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(grid, kSpillBudget / per_block));
+    try {
+      spill = const_cast<clv_device_scene*>(d)->spill_region(grid * per_block);
+    } catch (std::exception& ex) {
+      return fail(CLV_E_CUDA, ex.what());
+    }
+  }
   const float4* r4 = reinterpret_cast<const float4*>(rays_dev);
   cudaStream_t st = (cudaStream_t)stream;
   cudaError_t e = cudaMemsetAsync(d->ray_next, 0, sizeof(unsigned long long), st);
@@ -1145,9 +1097,16 @@ int clv_raycast_device(const clv_device_scene* d, const float* rays_dev, uint64_
     perm = order;
   }
 #define CLV_RAYCAST(C, N, W) \
-  raycast_persist_kernel<C, N, W><<<grid, block, 0, st>>>(d->view, r4, n, prim_dev, t_dev, nodes_dev, tests_dev, d->err, nx, perm)
+  raycast_persist_kernel<C, N, W><<<grid, block, 0, st>>>(d->view, r4, n, prim_dev, t_dev, nodes_dev, tests_dev, d->err, nx, perm, nullptr, 0)
   const int wt = d->view.watertight ? 1 : 0;
-  switch ((d->view.compound_level * 2 + (count ? 1 : 0)) * 2 + wt) {
+  const int cap = (int)d->view.max_depth_tree;
+  if (spill_entries && count)
+    raycast_persist_kernel<2, true, CLV_WT_SCENE, true><<<grid, block, 0, st>>>(
+        d->view, r4, n, prim_dev, t_dev, nodes_dev, tests_dev, d->err, nx, perm, spill, cap);
+  else if (spill_entries)
+    raycast_persist_kernel<2, false, CLV_WT_SCENE, true><<<grid, block, 0, st>>>(
+        d->view, r4, n, prim_dev, t_dev, nodes_dev, tests_dev, d->err, nx, perm, spill, cap);
+  else switch ((d->view.compound_level * 2 + (count ? 1 : 0)) * 2 + wt) {
     case 0: CLV_RAYCAST(0, false, CLV_WT_OFF); break;
     case 1: CLV_RAYCAST(0, false, CLV_WT_ON); break;
     case 2: CLV_RAYCAST(0, true, CLV_WT_OFF); break;
@@ -1227,8 +1186,16 @@ static int render_wavefront(clv_device_scene* d, const clv_render_opts* o, doubl
     P.seed = o->seed;
     uint64_t q = o->path_slots ? o->path_slots : d->tuned_slots ? d->tuned_slots : (uint64_t)sm_count() * 2048 * 4;
     q = std::min<uint64_t>(q, P.total);
-    q = (q + 127) / 128 * 128;
+    const uint32_t spill_entries = d->spill_entries();
+    if (spill_entries)  // deep tree: fewer paths in flight if their stack spill would exceed its budget
+      q = std::min<uint64_t>(q, kSpillBudget / ((uint64_t)spill_entries * sizeof(float4)));
+    q = std::max<uint64_t>(128, (q + 127) / 128 * 128);
     WfState W = d->wavefront_state((uint32_t)q);
+    if (spill_entries) {
+      W.spill = d->spill_region((size_t)q * spill_entries * sizeof(float4));
+      W.stack_cap = d->view.max_depth_tree;
+    }
+    if (query_order_enabled()) d->query_order(W);
     WfCounters c0{std::min<uint64_t>(q, P.total), 0u, {0u, 0u, 0u, 0u}};
     ck(cudaMemcpyAsync(d->wf_counters, &c0, sizeof c0, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync");
     GuideDev G{};
@@ -1269,12 +1236,25 @@ static int render_wavefront(clv_device_scene* d, const clv_render_opts* o, doubl
       prof->ms_init = ms;
     }
     // one bounce: counters, closest hits, the shading passes, path ends
+    const uint32_t ogrid = std::min<uint32_t>((uint32_t)((q + 255) / 256), (uint32_t)sm_count() * 8);
     auto bounce = [&](cudaStream_t s, int k) {
       cudaMemsetAsync(&d->wf_counters->live, 0, 5 * sizeof(unsigned int), s);  // live + 4 queue lengths
       if (prof) cudaEventRecord(evs[4 * k], s);
+      if (W.order) {  // group the live slots by direction octant and origin cell
+        cudaMemsetAsync(W.order_hist, 0, (WF_KEY_BINS + 1) * sizeof(uint32_t), s);
+        wf_order_hist<<<ogrid, 256, 0, s>>>(d->view, W);
+        wf_order_scan<<<1, WF_KEY_BINS, 0, s>>>(W);
+        wf_order_scatter<<<ogrid, 256, 0, s>>>(W);
+      }
 #define CLV_ISECT(L, N, T) \
   wf_intersect<L, N, false, T><<<grid, block, 0, s>>>(d->view, W, C, d->err, N ? dcnt : nullptr, WfBatch{}, -1)
-      switch ((level * 2 + (prof && count ? 1 : 0)) * 2 + (d->view.watertight ? 1 : 0)) {
+      if (spill_entries && prof && count)
+        wf_intersect<2, true, false, CLV_WT_SCENE, true><<<grid, block, 0, s>>>(d->view, W, C, d->err, dcnt,
+                                                                                WfBatch{}, -1);
+      else if (spill_entries)
+        wf_intersect<2, false, false, CLV_WT_SCENE, true><<<grid, block, 0, s>>>(d->view, W, C, d->err, nullptr,
+                                                                                 WfBatch{}, -1);
+      else switch ((level * 2 + (prof && count ? 1 : 0)) * 2 + (d->view.watertight ? 1 : 0)) {
         case 0: CLV_ISECT(0, false, CLV_WT_OFF); break;
         case 1: CLV_ISECT(0, false, CLV_WT_ON); break;
         case 2: CLV_ISECT(0, true, CLV_WT_OFF); break;
@@ -1301,7 +1281,7 @@ static int render_wavefront(clv_device_scene* d, const clv_render_opts* o, doubl
       wf_finish<false><<<qgrid, block, 0, s>>>(d->view, P, W, C, film, WfBatch{});
       if (prof) cudaEventRecord(evs[4 * k + 3], s);
     };
-    const unsigned per_bounce = 4u + (guide ? (alpha > 0.0f ? 3u : 2u) : 0u);
+    const unsigned per_bounce = 4u + (guide ? (alpha > 0.0f ? 3u : 2u) : 0u) + (W.order ? 3u : 0u);
     if (guide) gd_prepare();
     // the batch of bounces between polls, replayed as one CUDA graph (profiling
     // runs launch directly: their events bracket single kernels)
@@ -1414,8 +1394,18 @@ int clv_render_batch(clv_device_scene* const* ds, const clv_render_opts* opts, d
                  : d0->tuned_slots    ? d0->tuned_slots
                                       : (uint64_t)sm_count() * 2048 * 4;
     q = std::min<uint64_t>(q, total);
-    q = (q + 127) / 128 * 128;
+    uint32_t spill_entries = 0, stack_cap = CLV_STACK;  // the deepest tree of the batch
+    for (uint32_t k = 0; k < n; ++k) {
+      spill_entries = std::max(spill_entries, ds[k]->spill_entries());
+      stack_cap = std::max(stack_cap, ds[k]->view.max_depth_tree);
+    }
+    if (spill_entries) q = std::min<uint64_t>(q, kSpillBudget / ((uint64_t)spill_entries * sizeof(float4)));
+    q = std::max<uint64_t>(128, (q + 127) / 128 * 128);
     WfState W = d0->wavefront_state((uint32_t)q);
+    if (spill_entries) {
+      W.spill = d0->spill_region((size_t)q * spill_entries * sizeof(float4));
+      W.stack_cap = stack_cap;
+    }
     WfCounters c0{std::min<unsigned long long>(q, total), 0u, {0u, 0u, 0u, 0u}};
     ck(cudaMemcpyAsync(d0->wf_counters, &c0, sizeof c0, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync");
     WfCounters* C = d0->wf_counters;
@@ -1434,13 +1424,16 @@ int clv_render_batch(clv_device_scene* const* ds, const clv_render_opts* opts, d
       for (int k = 0; k < batch; ++k) {
         cudaMemsetAsync(&C->live, 0, 5 * sizeof(unsigned int), s);
         // one intersect launch per traversal level present, each over its own scenes' slots
+        // (a batch with a tree deeper than CLV_STACK levels: one generic launch with a spilling stack)
         const int only = nlevels > 1 ? 0 : -1;
-        if (levels & 1u)
+        if (spill_entries)
+          wf_intersect<2, false, true, CLV_WT_SCENE, true><<<grid, block, 0, s>>>(S0, W, C, d0->err, nullptr, B, -1);
+        else if (levels & 1u)
           wf_intersect<0, false, true, CLV_WT_SCENE><<<grid, block, 0, s>>>(S0, W, C, d0->err, nullptr, B, only);
-        if (levels & 2u)
+        if (!spill_entries && (levels & 2u))
           wf_intersect<1, false, true, CLV_WT_SCENE><<<grid, block, 0, s>>>(S0, W, C, d0->err, nullptr, B,
                                                                             only < 0 ? -1 : 1);
-        if (levels & 4u)
+        if (!spill_entries && (levels & 4u))
           wf_intersect<2, false, true, CLV_WT_SCENE><<<grid, block, 0, s>>>(S0, W, C, d0->err, nullptr, B,
                                                                             only < 0 ? -1 : 2);
         wf_shade_specular<true><<<qgrid, block, 0, s>>>(S0, P0, W, C, d0->err, B);
@@ -1452,7 +1445,7 @@ int clv_render_batch(clv_device_scene* const* ds, const clv_render_opts* opts, d
     for (uint64_t it = 0;; it += batch) {
       if (graph.exec) ck(cudaGraphLaunch(graph.exec, st), "cudaGraphLaunch");
       else bounces(st);
-      g_launches += (3 + nlevels) * batch;
+      g_launches += (3 + (spill_entries ? 1 : nlevels)) * batch;
       ck(cudaGetLastError(), "wavefront launch");
       ck(cudaMemcpyAsync(d0->wf_live_host, &C->live, sizeof(unsigned int), cudaMemcpyDeviceToHost, st),
          "cudaMemcpyAsync");
@@ -1476,7 +1469,7 @@ int clv_render_guided(clv_device_scene* d, const clv_render_opts* o, clv_guide* 
   int rc = check_opts(d, o);
   if (rc) return rc;
   if (!g || !film_dev) return fail(CLV_E_INVALID, "null argument");
-  if (o->mode != CLV_MODE_PATH_TRACING || o->engine != 0)
+  if (o->mode != CLV_MODE_PATH_TRACING)
     return fail(CLV_E_INVALID, "guided renders use the wavefront path tracer");
   if (!(alpha >= 0.0f && alpha <= 1.0f)) return fail(CLV_E_INVALID, "alpha must lie in [0, 1]");
   rc = render_wavefront(d, o, film_dev, (cudaStream_t)stream, nullptr, g, alpha);
@@ -1495,18 +1488,18 @@ int clv_render_device(clv_device_scene* d, const clv_render_opts* o, double* fil
   int rc = check_opts(d, o);
   if (rc) return rc;
   if (!film_dev) return fail(CLV_E_INVALID, "null film");
+  if (o->mode == CLV_MODE_PATH_TRACING) return render_wavefront(d, o, film_dev, (cudaStream_t)stream, nullptr);
   const int block = 128;
-  if (o->mode == CLV_MODE_PATH_TRACING && o->engine == 0)
-    return render_wavefront(d, o, film_dev, (cudaStream_t)stream, nullptr);
   const RenderParams P = make_params(o);
-  g_launches += 1;
-  if (o->mode == CLV_MODE_PATH_TRACING) {
-    render_kernel<<<launch_grid(P.npix * P.chunks, block), block, 0, (cudaStream_t)stream>>>(d->view, P, film_dev,
-                                                                                             d->err);
-  } else {
-    debug_kernel<<<(uint32_t)((P.npix + block - 1) / block), block, 0, (cudaStream_t)stream>>>(d->view, P, film_dev,
-                                                                                               d->err);
+  float4* spill = nullptr;
+  try {
+    if (d->spill_entries()) spill = d->spill_region((size_t)P.npix * d->spill_entries() * sizeof(float4));
+  } catch (std::exception& ex) {
+    return fail(CLV_E_CUDA, ex.what());
   }
+  g_launches += 1;
+  debug_kernel<<<(uint32_t)((P.npix + block - 1) / block), block, 0, (cudaStream_t)stream>>>(d->view, P, film_dev,
+                                                                                             d->err, spill);
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail(CLV_E_CUDA, std::string("render launch: ") + cudaGetErrorString(e));
   return CLV_OK;
@@ -1661,11 +1654,14 @@ extern "C" int clv_render_device_noalloc(clv_device_scene* d, const clv_render_o
   int rc = check_opts(d, o);
   if (rc) return rc;
   if (!film_dev) return fail(CLV_E_INVALID, "null film");
-  if (o->mode != CLV_MODE_PATH_TRACING || o->engine != 0)
+  if (o->mode != CLV_MODE_PATH_TRACING)
     return fail(CLV_E_INVALID, "the no-allocation render covers the wavefront path tracer only");
   if (o->path_slots > CLV_NOALLOC_SLOTS)
     return fail(CLV_E_INVALID, "path_slots " + std::to_string(o->path_slots) + " exceeds the static scratch of " +
                                    std::to_string(CLV_NOALLOC_SLOTS) + " paths");
+  if (d->deep())
+    return fail(CLV_E_INVALID, "the no-allocation render takes BVHs of at most " + std::to_string(CLV_STACK) +
+                                   " levels (this one has " + std::to_string(d->view.max_depth_tree) + ")");
   void* base = nullptr;
   rc = noalloc_scratch_address(&base);
   if (rc) return rc;
@@ -1678,7 +1674,9 @@ extern "C" int clv_render_device_noalloc(clv_device_scene* d, const clv_render_o
   P.npix = (uint64_t)o->width * o->height;
   P.total = P.npix * o->samples;
   P.seed = o->seed;
-  uint64_t q = o->path_slots ? o->path_slots : CLV_NOALLOC_SLOTS;
+  // the scene's tuned shape (clv_autotune) where it fits the static array
+  uint64_t q = o->path_slots ? o->path_slots : std::min<uint64_t>(d->tuned_slots ? d->tuned_slots : CLV_NOALLOC_SLOTS,
+                                                                  CLV_NOALLOC_SLOTS);
   q = std::min<uint64_t>(q, P.total);
   q = (q + 127) / 128 * 128;  // at most CLV_NOALLOC_SLOTS, itself a multiple of 128
   // carve counters and path state out of the static array (the layout of clv_device_scene::wavefront_state)
@@ -1700,9 +1698,15 @@ extern "C" int clv_render_device_noalloc(clv_device_scene* d, const clv_render_o
   W.grec = nullptr;
   W.grec_count = nullptr;
   W.grec_cap = 0;
+  W.spill = nullptr;
+  W.stack_cap = CLV_STACK;
+  W.order = nullptr;
+  W.order_key = nullptr;
+  W.order_hist = nullptr;
   const int block = 128;
   const uint32_t grid = (uint32_t)((q + block - 1) / block);
-  const uint32_t qgrid = std::min<uint32_t>(grid, (uint32_t)sm_count() * CLV_SHADE_BLOCKS);
+  const uint32_t qgrid =
+      std::min<uint32_t>(grid, (uint32_t)sm_count() * (d->tuned_shade ? d->tuned_shade : CLV_SHADE_BLOCKS));
   // the array keeps the previous call's contents: counters are reset here and
   // wf_init rewrites every path slot
   noalloc_counters_init<<<1, 1, 0, st>>>(C, std::min<uint64_t>(q, P.total));

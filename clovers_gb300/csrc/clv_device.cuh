@@ -21,6 +21,7 @@
 #include <math_constants.h>
 #include <stdint.h>
 
+#include "clv_log.h"
 #include "device_types.h"
 #include "rng.cuh"
 
@@ -32,7 +33,7 @@ namespace clvd {
 #define CLV_EPS_MEDIUM 0.0001f
 #define CLV_FLT_MAX 3.40282347e+38f
 #define CLV_DEG2RAD (3.14159265358979323846f / 180.0f)
-#define CLV_STACK 64       // traversal stack entries (host rejects deeper trees)
+#define CLV_STACK 64       // traversal stack entries in local memory (deeper trees spill: SpillStack)
 #define CLV_MIS_STACK 32   // MIS tree evaluation stack
 #define CLV_NEST 6         // wrapper nesting depth handled by the object interpreter
 #ifndef CLV_MINB
@@ -419,7 +420,8 @@ __device__ __noinline__ bool ObjEval<LEVEL>::hit(const ClvDeviceScene& S, uint32
       if (r1.t < 0.0f) r1.t = 0.0f;
       float rl = len(r.d);
       float inside = (r2.t - r1.t) * rl;
-      float hd = o.p[0] * logf(rng->f32());
+      // the project's own f32 log: the same bits as the CPU oracle's (clv_log.h)
+      float hd = o.p[0] * clv_math::log_f32(rng->f32());
       if (hd > inside) return false;
       rec.t = r1.t + hd / rl;
       rec.p = at(r, rec.t);
@@ -811,6 +813,29 @@ template <int SH>
 __device__ __forceinline__ float4 st_get(HybridStack<SH>& s, int i) {
   return i < SH ? s.sh[i * 128] : s.loc[i - SH];
 }
+// Stack for trees deeper than CLV_STACK levels: the first CLV_STACK entries in
+// local memory, the rest in a global spill region where entry k of thread t
+// sits at region[(k - CLV_STACK) * stride + t] (the threads of a warp side by
+// side).  cap = entries available (the scene's tree depth needs at most
+// depth - 1: one deferred far child per level of the current path).
+struct SpillStack {
+  float4* loc;
+  float4* glob;     // region + t
+  uint32_t stride;  // threads that share the region
+  int cap;
+};
+__device__ __forceinline__ void st_put(SpillStack& s, int i, float4 v) {
+  if (i < CLV_STACK) s.loc[i] = v;
+  else s.glob[(size_t)(i - CLV_STACK) * s.stride] = v;
+}
+__device__ __forceinline__ float4 st_get(SpillStack& s, int i) {
+  return i < CLV_STACK ? s.loc[i] : s.glob[(size_t)(i - CLV_STACK) * s.stride];
+}
+// Entries a stack holds.
+__device__ __forceinline__ int st_cap(float4*) { return CLV_STACK; }
+template <int SH>
+__device__ __forceinline__ int st_cap(HybridStack<SH>&) { return CLV_STACK; }
+__device__ __forceinline__ int st_cap(SpillStack& s) { return s.cap; }
 
 // Three-input f32 max / min (NaN inputs ignored, as fmaxf / fminf do).
 __device__ __forceinline__ float max3f(float a, float b, float c) {
@@ -947,7 +972,7 @@ __device__ __forceinline__ bool trav_step(const ClvDeviceScene& S, const Ray& r,
         if (both && lh && rh) {
           left_next = ld < rd;
           next = left_next ? L : Rr;
-          if (T.sp < CLV_STACK) {
+          if (T.sp < st_cap(stack)) {
             st_put(stack, T.sp++, make_float4(__uint_as_float(left_next ? Rr : L), fmaxf(ld, rd), left_next ? NR : NL,
                                               left_next ? FR : FL));
           } else if (err) {
@@ -982,7 +1007,7 @@ __device__ __forceinline__ bool trav_step(const ClvDeviceScene& S, const Ray& r,
             if (wide) slab_wide(fb, R, fN, fF);
             else slab(fb, r.o, R.inv, fN, fF);
           }
-          if (T.sp < CLV_STACK) {
+          if (T.sp < st_cap(stack)) {
             st_put(stack, T.sp++, make_float4(__uint_as_float(far), fmaxf(ld, rd), fN, fF));
           } else if (err) {
             atomicOr(err, CLV_ERR_STACK);
@@ -1058,11 +1083,10 @@ __device__ bool closest_hit(const ClvDeviceScene& S, const Ray& r, float tmin, f
 // one, and the leaf then runs once for all of them.  Every lane
 // still makes exactly closest_hit's sequence of node visits and leaf tests,
 // only later in time, so hits and counts are unchanged.
-template <int CPLX, int WT>
+template <int CPLX, int WT, class STK>
 __device__ __forceinline__ bool closest_hit_warp(const ClvDeviceScene& S, const Ray& r, bool go, float tmin, float tmax,
-                                                 Rng* rng, Hit& hit, Rec* full, Counters* cnt, uint32_t* err) {
-  float4 stack_mem[CLV_STACK];
-  float4* stack = stack_mem;
+                                                 Rng* rng, Hit& hit, Rec* full, Counters* cnt, uint32_t* err,
+                                                 STK& stack) {
   Trav T;
   T.found = false;
   T.ref = CLV_REF_EMPTY;
@@ -1076,6 +1100,13 @@ __device__ __forceinline__ bool closest_hit_warp(const ClvDeviceScene& S, const 
     if (active && (!at_chain || chains == act)) active = trav_step<CPLX, WT>(S, r, T, stack, rng, hit, full, cnt, err);
   }
   return go && T.found;
+}
+template <int CPLX, int WT>
+__device__ __forceinline__ bool closest_hit_warp(const ClvDeviceScene& S, const Ray& r, bool go, float tmin, float tmax,
+                                                 Rng* rng, Hit& hit, Rec* full, Counters* cnt, uint32_t* err) {
+  float4 stack_mem[CLV_STACK];
+  float4* stack = stack_mem;
+  return closest_hit_warp<CPLX, WT>(S, r, go, tmin, tmax, rng, hit, full, cnt, err, stack);
 }
 
 // Full record of the closest hit (deterministic rebuild for primitives).

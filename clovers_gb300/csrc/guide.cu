@@ -100,11 +100,13 @@ __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-// Waits for phase `parity` of the barrier, for about one second at most.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+// Waits for phase `parity` of the barrier for at most `limit` SM clocks (by
+// default about one second); false when the wait ran out.
+#define GD_WAIT_CLOCKS 2000000000ll
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, long long limit = GD_WAIT_CLOCKS) {
   const long long t0 = clock64();
   while (!mbar_try(bar, parity))
-    if (clock64() - t0 > 2000000000ll) return false;
+    if (clock64() - t0 > limit) return false;
   return true;
 }
 __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
@@ -814,6 +816,38 @@ __global__ void __launch_bounds__(128, 1) guide_selftest_kernel(uint32_t N, uint
   }
 }
 
+// Self-test of the bounded-wait error path: the kernel initialises an
+// mbarrier for one arrival that never comes -- nothing asynchronous is
+// issued, no copy and no MMA -- so mbar_wait runs out after `limit` clocks.
+// The kernel then does what the production kernels do on a timeout: raise
+// CLV_ERR_GUIDE, free its TMEM, return.  done[0] = 1 once the TMEM is freed.
+__global__ void __launch_bounds__(128) guide_wait_selftest_kernel(uint32_t* err, long long limit, uint32_t* done) {
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ uint32_t tslot;
+  const uint32_t tid = threadIdx.x, warp = tid >> 5;
+  if (warp == 0) {
+    tmem_alloc(smem_u32(&tslot), 32);
+    tmem_relinquish();
+  }
+  if (tid == 0) {
+    mbar_init(smem_u32(&bar), 1);
+    mbar_init_fence();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tslot;
+  const bool ok = __syncthreads_and(mbar_wait(smem_u32(&bar), 0, limit)) != 0;
+  if (!ok && tid == 0) atomicOr(err, CLV_ERR_GUIDE);
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    tmem_dealloc(tmem, 32);
+  }
+  __syncthreads();
+  if (tid == 0) done[0] = 1u;
+}
+
 }  // namespace gd
 
 // ------------------------------------------------------------------- host --
@@ -1173,6 +1207,33 @@ int clv_guide_selftest_mma(uint32_t n, uint32_t k, uint64_t seed, float* d_out, 
     buf = nullptr;
     if (fl) return clv_internal_fail(CLV_E_DEVICE, "tensor-core wait timed out");
     *max_abs_err = e;
+  } catch (std::exception& ex) {
+    if (buf) cudaFree(buf);
+    return clv_internal_fail(CLV_E_CUDA, ex.what());
+  }
+  return CLV_OK;
+}
+
+// Runs guide_wait_selftest_kernel with a wait limit of `clocks` SM clocks
+// (about 1 ms at 2e6).  flags receives the error bits the kernel raised
+// (CLV_ERR_GUIDE expected) and freed = 1 when it reached its TMEM release.
+int clv_guide_selftest_timeout(uint64_t clocks, uint32_t* flags, uint32_t* freed) {
+  if (!flags || !freed) return clv_internal_fail(CLV_E_INVALID, "null argument");
+  if (clocks == 0 || clocks > 4000000000ull) return clv_internal_fail(CLV_E_INVALID, "clocks must lie in (0, 4e9]");
+  void* buf = nullptr;
+  try {
+    ckg(cudaMalloc(&buf, 8), "cudaMalloc");
+    uint32_t* d = static_cast<uint32_t*>(buf);
+    ckg(cudaMemset(buf, 0, 8), "cudaMemset");
+    guide_wait_selftest_kernel<<<1, 128>>>(d, (long long)clocks, d + 1);
+    clv_internal_count_launches(1);
+    ckg(cudaGetLastError(), "selftest launch");
+    uint32_t h[2] = {0u, 0u};
+    ckg(cudaMemcpy(h, buf, sizeof h, cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
+    cudaFree(buf);
+    buf = nullptr;
+    *flags = h[0];
+    *freed = h[1];
   } catch (std::exception& ex) {
     if (buf) cudaFree(buf);
     return clv_internal_fail(CLV_E_CUDA, ex.what());

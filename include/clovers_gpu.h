@@ -52,8 +52,6 @@ typedef struct clv_render_opts {
   uint32_t sampler;             /* 0 = random (default); 1 = blue noise: unsupported */
   uint64_t seed;                /* stream seed; identical seeds give identical images */
   uint32_t sample_offset;       /* index of the first sample (progressive rendering) */
-  uint32_t samples_per_thread;  /* megakernel only: samples per thread, 0 = automatic */
-  uint32_t engine;              /* 0 = wavefront (default), 1 = single megakernel */
   uint32_t path_slots;          /* wavefront paths in flight, 0 = automatic */
 } clv_render_opts;
 
@@ -293,6 +291,22 @@ int clv_render_profile_run(clv_device_scene* dscene, const clv_render_opts* opts
 /* Checks the traversal's fast slab division (reciprocal + one FMA correction)
  * against IEEE division on n random operand pairs; mismatches must be 0. */
 int clv_selftest_division(uint64_t n, uint64_t seed, uint64_t* mismatches);
+
+/* Checks the render path's own natural logarithm (used by ConstantMedium's
+ * free-flight draw, clovers/src/objects/constant_medium.rs:102, in place of
+ * the library logf whose last bit differs between CUDA and host libms) over
+ * every f32 in (0, 1]: max_ulp = largest error in f32 ulps against the GPU's
+ * double-precision log, not_nearest = results that are not the nearest f32 of
+ * it.  With x and y (host arrays of n floats) it also evaluates the routine on
+ * x, for bitwise comparison with the CPU build of the same routine. */
+int clv_selftest_log(const float* x, float* y, uint64_t n, double* max_ulp, uint64_t* not_nearest);
+
+/* Exercises the guide kernels' bounded-wait error path: one CTA allocates
+ * TMEM, waits on an mbarrier that nothing arrives on (no copy or MMA is in
+ * flight) for `clocks` SM clocks, then raises the timeout flag, frees its
+ * TMEM and returns.  flags = the error bits raised (CLV_ERR_GUIDE, 8),
+ * freed = 1 when the kernel reached its TMEM release. */
+int clv_guide_selftest_timeout(uint64_t clocks, uint32_t* flags, uint32_t* freed);
 
 #ifdef __cplusplus
 }

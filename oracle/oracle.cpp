@@ -41,17 +41,27 @@
 #include <thread>
 #include <vector>
 
+#include "../clovers_gb300/csrc/clv_log.h"
 #include "../clovers_gb300/csrc/json.hpp"
 #include "../clovers_gb300/csrc/spectral_tables.h"
 
 namespace orc {
 
+#ifdef ORC_DOUBLE
+// The quality reference: the same algorithm with Float = f64, the reference's
+// own precision switch (clovers/src/lib.rs:97-98).  Scene values still come in
+// as f32 (the scene the GPU renders), then every operation runs in double.
+typedef double Float;
+#define FL(x) x
+#else
 typedef float Float;
-static const Float PI = 3.14159265358979323846f;                 // core::f32::consts::PI
-static const Float EPSILON_SHADOW_ACNE = 0.001f;                 // clovers/src/lib.rs:114
-static const Float EPSILON_RECT_THICKNESS = 0.0001f;             // clovers/src/lib.rs:116
-static const Float EPSILON_CONSTANT_MEDIUM = 0.0001f;            // clovers/src/lib.rs:119
-static const Float RADS_PER_DEG = 3.14159265358979323846f / 180.0f;  // f32::to_radians
+#define FL(x) x##f
+#endif
+static const Float PI = FL(3.14159265358979323846);                 // core::f32::consts::PI
+static const Float EPSILON_SHADOW_ACNE = FL(0.001);                 // clovers/src/lib.rs:114
+static const Float EPSILON_RECT_THICKNESS = FL(0.0001);             // clovers/src/lib.rs:116
+static const Float EPSILON_CONSTANT_MEDIUM = FL(0.0001);            // clovers/src/lib.rs:119
+static const Float RADS_PER_DEG = FL(3.14159265358979323846) / FL(180.0);  // f32::to_radians
 static const int MIN_WAVELENGTH = 380, MAX_WAVELENGTH = 780, SPECTRUM_SIZE = 400;  // wavelength.rs:14-20
 static const int WAVE_SAMPLE_COUNT = 4;                          // wavelength.rs:25
 
@@ -81,6 +91,15 @@ static inline Float rmax(Float a, Float b) { return std::fmax(a, b); }
 static inline Float midpoint(Float a, Float b) { return (Float)(((double)a + (double)b) / 2.0); }
 // Rust f32::clamp: NaN passes through
 static inline Float rclamp(Float x, Float lo, Float hi) { return x < lo ? lo : (x > hi ? hi : x); }
+// Natural log of a uniform draw (the free-flight distance of
+// constant_medium.rs:102, Rust's ln).  The f32 build uses the project's own
+// logarithm (clv_log.h), whose bits the GPU reproduces exactly; the f64 build
+// uses the host libm's double log.
+#ifdef ORC_DOUBLE
+static inline Float ln(Float x) { return std::log(x); }
+#else
+static inline Float ln(Float x) { return clv_math::log_f32(x); }
+#endif
 
 // -------------------------------------------------------------------- rng --
 // Counter-based stream (see header).  SplitMix64: Steele, Lea, Flood 2014.
@@ -99,11 +118,11 @@ struct Rng {
     return (uint32_t)(mix64(key + (uint64_t)counter * 0x9E3779B97F4A7C15ull) >> 32);
   }
   // rand: Standard f32 = (u32 >> 8) * 2^-24, uniform in [0,1)
-  Float next_f32() { return (Float)(next_u32() >> 8) * 5.9604644775390625e-8f; }
+  Float next_f32() { return (Float)(next_u32() >> 8) * FL(5.9604644775390625e-8); }
   // rand: Standard bool = sign bit of a u32 draw
   bool next_bool() { return (int32_t)next_u32() < 0; }
   // uniform in [-1, 1)
-  Float next_sym() { return 2.0f * next_f32() - 1.0f; }
+  Float next_sym() { return FL(2.0) * next_f32() - FL(1.0); }
 };
 static const int REJECTION_LIMIT = 64;
 
@@ -112,26 +131,26 @@ static Vec3 random_unit_vector(Rng& rng) {
   for (int i = 0; i < REJECTION_LIMIT; ++i) {
     Float x1 = rng.next_sym(), x2 = rng.next_sym();
     Float sum = x1 * x1 + x2 * x2;
-    if (sum >= 1.0f) continue;
-    Float factor = 2.0f * std::sqrt(1.0f - sum);
-    return normalize(Vec3(x1 * factor, x2 * factor, 1.0f - 2.0f * sum));
+    if (sum >= FL(1.0)) continue;
+    Float factor = FL(2.0) * std::sqrt(FL(1.0) - sum);
+    return normalize(Vec3(x1 * factor, x2 * factor, FL(1.0) - FL(2.0) * sum));
   }
-  return Vec3(0.0f, 0.0f, 1.0f);
+  return Vec3(FL(0.0), FL(0.0), FL(1.0));
 }
 // rand_distr UnitDisc (rejection), clovers/src/random.rs:18-21
 static void random_in_unit_disk(Rng& rng, Float& ox, Float& oy) {
   for (int i = 0; i < REJECTION_LIMIT; ++i) {
     Float x1 = rng.next_sym(), x2 = rng.next_sym();
-    if (x1 * x1 + x2 * x2 <= 1.0f) { ox = x1; oy = x2; return; }
+    if (x1 * x1 + x2 * x2 <= FL(1.0)) { ox = x1; oy = x2; return; }
   }
-  ox = 0.0f; oy = 0.0f;
+  ox = FL(0.0); oy = FL(0.0);
 }
 // clovers/src/random.rs:25-36
 static Vec3 random_cosine_direction(Rng& rng) {
   Float r1 = rng.next_f32();
   Float r2 = rng.next_f32();
-  Float z = std::sqrt(1.0f - r2);
-  Float phi = 2.0f * PI * r1;
+  Float z = std::sqrt(FL(1.0) - r2);
+  Float phi = FL(2.0) * PI * r1;
   Float x = std::cos(phi) * std::sqrt(r2);
   Float y = std::sin(phi) * std::sqrt(r2);
   return Vec3(x, y, z);
@@ -152,15 +171,15 @@ static void rotate_wavelength(int hero, int out[4]) {
 // clovers/src/wavelength.rs:63-66
 static Float gaussian(Float x, Float alpha, Float mu, Float s1, Float s2) {
   Float t = (x - mu) / (x < mu ? s1 : s2);
-  return alpha * std::exp(-(t * t) / 2.0f);
+  return alpha * std::exp(-(t * t) / FL(2.0));
 }
 // clovers/src/wavelength.rs:71-83
 static void wavelength_into_xyz(int lambda, Float out[3]) {
   Float l = (Float)lambda;
-  Float x = 0.0f + gaussian(l, 1.056f, 599.8f, 37.9f, 31.0f) + gaussian(l, 0.362f, 442.0f, 16.0f, 26.7f) +
-            gaussian(l, -0.065f, 501.1f, 20.4f, 26.2f);
-  Float y = gaussian(l, 0.821f, 568.8f, 46.9f, 40.5f) + gaussian(l, 0.286f, 530.9f, 16.3f, 31.1f);
-  Float z = gaussian(l, 1.217f, 437.0f, 11.8f, 36.0f) + gaussian(l, 0.681f, 459.0f, 26.0f, 13.8f);
+  Float x = FL(0.0) + gaussian(l, FL(1.056), FL(599.8), FL(37.9), FL(31.0)) + gaussian(l, FL(0.362), FL(442.0), FL(16.0), FL(26.7)) +
+            gaussian(l, -FL(0.065), FL(501.1), FL(20.4), FL(26.2));
+  Float y = gaussian(l, FL(0.821), FL(568.8), FL(46.9), FL(40.5)) + gaussian(l, FL(0.286), FL(530.9), FL(16.3), FL(31.1));
+  Float z = gaussian(l, FL(1.217), FL(437.0), FL(11.8), FL(36.0)) + gaussian(l, FL(0.681), FL(459.0), FL(26.0), FL(13.8));
   out[0] = x; out[1] = y; out[2] = z;
 }
 
@@ -289,10 +308,10 @@ static void bradford(const double src_w[3], const double dst_w[3], double out[9]
 static const double W_D65[3] = {0.95047, 1.0, 1.08883};
 static const double W_E[3] = {1.0, 1.0, 1.0};
 static Float srgb_decode(Float c) {
-  return c <= 0.04045f ? c / 12.92f : std::pow((c + 0.055f) / 1.055f, 2.4f);
+  return c <= FL(0.04045) ? c / FL(12.92) : std::pow((c + FL(0.055)) / FL(1.055), FL(2.4));
 }
 static Float srgb_encode(Float c) {
-  return c <= 0.0031308f ? c * 12.92f : 1.055f * std::pow(c, 1.0f / 2.4f) - 0.055f;
+  return c <= FL(0.0031308) ? c * FL(12.92) : FL(1.055) * std::pow(c, FL(1.0) / FL(2.4)) - FL(0.055);
 }
 static void apply3(const double m[9], const Float in[3], Float out[3]) {
   for (int r = 0; r < 3; ++r)
@@ -325,9 +344,9 @@ static void xyz_e_to_srgb8(const Float xyz[3], uint8_t out[3]) {
   apply3(t, xyz, lin);
   for (int i = 0; i < 3; ++i) {
     Float e = srgb_encode(lin[i]);
-    Float v = std::round(e * 255.0f);
-    if (!(v > 0.0f)) v = 0.0f;  // NaN and negatives -> 0 (saturating cast)
-    if (v > 255.0f) v = 255.0f;
+    Float v = std::round(e * FL(255.0));
+    if (!(v > FL(0.0))) v = FL(0.0);  // NaN and negatives -> 0 (saturating cast)
+    if (v > FL(255.0)) v = FL(255.0);
     out[i] = (uint8_t)v;
   }
 }
@@ -346,7 +365,7 @@ struct Interval {
   }
   Interval expand(Float delta) const { return Interval(min - delta, max + delta); }
   Float size() const { return max - min; }
-  Float center() const { return min + 0.5f * size(); }
+  Float center() const { return min + FL(0.5) * size(); }
 };
 
 struct Ray {
@@ -370,18 +389,18 @@ struct AABB {
   // the conservative box test of watertight scenes (not the reference's)
   // and a zero direction component constrains nothing while the origin lies
   // within that slab (inclusive), missing otherwise
-  static Float widen_exit(Float f) { return std::fmax(f, f + std::fabs(f) * 7.1525574e-7f); }
+  static Float widen_exit(Float f) { return std::fmax(f, f + std::fabs(f) * FL(7.1525574e-7)); }
   bool hit(const Ray& ray, Float tmin, Float tmax, bool wide = false) const {
     if (wide) {
       Float n = -INFINITY, f = INFINITY;
       for (int a = 0; a < 3; ++a) {
         const Interval& ax = axis(a);
         const Float o = ray.origin[a];
-        if (ray.direction[a] == 0.0f) {
+        if (ray.direction[a] == FL(0.0)) {
           if (o < ax.min || o > ax.max) return false;
           continue;
         }
-        Float adinv = 1.0f / ray.direction[a];
+        Float adinv = FL(1.0) / ray.direction[a];
         Float t0 = (ax.min - o) * adinv, t1 = (ax.max - o) * adinv;
         n = std::fmax(n, std::fmin(t0, t1));
         f = std::fmin(f, std::fmax(t0, t1));
@@ -390,7 +409,7 @@ struct AABB {
     }
     for (int a = 0; a < 3; ++a) {
       const Interval& ax = axis(a);
-      Float adinv = 1.0f / ray.direction[a];
+      Float adinv = FL(1.0) / ray.direction[a];
       Float t0 = (ax.min - ray.origin[a]) * adinv;
       Float t1 = (ax.max - ray.origin[a]) * adinv;
       if (t0 < t1) {
@@ -421,7 +440,7 @@ struct AABB {
       const Interval* ax[3] = {&x, &y, &z};
       for (int a = 0; a < 3; ++a) {
         const Float o = ray.origin[a], d = ray.direction[a];
-        if (d == 0.0f) {
+        if (d == FL(0.0)) {
           if (o < ax[a]->min || o > ax[a]->max) return false;
           continue;
         }
@@ -430,7 +449,7 @@ struct AABB {
         tmax = std::fmin(tmax, std::fmax(t1, t2));
       }
       tmax = widen_exit(tmax);
-      if (tmax >= tmin && tmax > 0.0f) { out = tmin; return true; }
+      if (tmax >= tmin && tmax > FL(0.0)) { out = tmin; return true; }
       return false;
     }
     Float tx1 = (x.min - ray.origin.x) / ray.direction.x;
@@ -444,12 +463,12 @@ struct AABB {
     Float tz2 = (z.max - ray.origin.z) / ray.direction.z;
     tmin = rmax(tmin, rmin(tz1, tz2));
     tmax = rmin(tmax, rmax(tz1, tz2));
-    if (tmax >= tmin && tmax > 0.0f) { out = tmin; return true; }
+    if (tmax >= tmin && tmax > FL(0.0)) { out = tmin; return true; }
     return false;
   }
   Float area() const {
     Vec3 e = Vec3(x.max, y.max, z.max) - Vec3(x.min, y.min, z.min);
-    return 2.0f * (e.x * e.y + e.y * e.z + e.x * e.z);
+    return FL(2.0) * (e.x * e.y + e.y * e.z + e.x * e.z);
   }
   Vec3 centroid() const { return Vec3(x.center(), y.center(), z.center()); }
   AABB offset(Vec3 o) const {
@@ -469,7 +488,7 @@ struct HitRecord {
   int gid = -1;  // index of the top-level (BVH leaf) object that was hit
   // clovers/src/hitrecord.rs:36-43
   void set_face_normal(const Ray& ray, Vec3 outward) {
-    front_face = dot(ray.direction, outward) < 0.0f;
+    front_face = dot(ray.direction, outward) < FL(0.0);
     normal = front_face ? outward : -outward;
   }
 };
@@ -481,28 +500,28 @@ struct Texture {
   SPD even, odd;  // SolidColor uses `even`
   Float density = 0;
   int illuminant = 0;
-  Float intensity = 1.0f;
+  Float intensity = FL(1.0);
   Float color(int lambda, const HitRecord& rec) const {
     switch (kind) {
       case TEX_SOLID: return even.get(lambda);
       case TEX_SPATIAL: {
         Float d = density * PI;
-        Float s = 1.0f * std::sin(d * rec.position.x) * std::sin(d * rec.position.y) * std::sin(d * rec.position.z);
-        return s < 0.0f ? odd.get(lambda) : even.get(lambda);
+        Float s = FL(1.0) * std::sin(d * rec.position.x) * std::sin(d * rec.position.y) * std::sin(d * rec.position.z);
+        return s < FL(0.0) ? odd.get(lambda) : even.get(lambda);
       }
       case TEX_SURFACE: {
         Float d = density * PI;
-        Float s = 1.0f * std::sin(d * rec.u) * std::sin(d * rec.v);
-        return s < 0.0f ? odd.get(lambda) : even.get(lambda);
+        Float s = FL(1.0) * std::sin(d * rec.u) * std::sin(d * rec.v);
+        return s < FL(0.0) ? odd.get(lambda) : even.get(lambda);
       }
       default: {
         Float c = clv_tables::kIlluminants[illuminant][lambda - MIN_WAVELENGTH] * intensity;
-        return rclamp(c, 0.0f, 1.0f);
+        return rclamp(c, FL(0.0), FL(1.0));
       }
     }
   }
   Float emit(int lambda) const {
-    if (kind != TEX_ILLUMINANT) return 0.0f;
+    if (kind != TEX_ILLUMINANT) return FL(0.0);
     return clv_tables::kIlluminants[illuminant][lambda - MIN_WAVELENGTH] * intensity;
   }
 };
@@ -517,41 +536,41 @@ struct ScatterRecord {
   Vec3 pdf_w;  // CosinePDF normal
 };
 // clovers/src/materials.rs:188-207
-static Vec3 reflect(Vec3 v, Vec3 n) { return normalize(v - 2.0f * dot(v, n) * n); }
+static Vec3 reflect(Vec3 v, Vec3 n) { return normalize(v - FL(2.0) * dot(v, n) * n); }
 static Vec3 refract(Vec3 v, Vec3 n, Float ratio) {
   Float cos_theta = -dot(v, n);
-  cos_theta = rmin(cos_theta, 1.0f);
+  cos_theta = rmin(cos_theta, FL(1.0));
   Vec3 par = ratio * (v + cos_theta * n);
-  Vec3 perp = -std::sqrt(1.0f - norm_squared(par)) * n;
+  Vec3 perp = -std::sqrt(FL(1.0) - norm_squared(par)) * n;
   return normalize(par + perp);
 }
 static Float schlick(Float cosine, Float ri) {
-  Float r0 = (1.0f - ri) / (1.0f + ri);
+  Float r0 = (FL(1.0) - ri) / (FL(1.0) + ri);
   r0 = r0 * r0;
-  return r0 + (1.0f - r0) * std::pow(1.0f - cosine, 5.0f);
+  return r0 + (FL(1.0) - r0) * std::pow(FL(1.0) - cosine, FL(5.0));
 }
 
 struct Material {
   int kind = M_LAMBERTIAN;
   Texture tex;                  // albedo / emit
   Float fuzz = 0;               // Metal
-  Float refractive_index = 1.5f;  // Dielectric
+  Float refractive_index = FL(1.5);  // Dielectric
   SPD color;                    // Dielectric colour
-  Float cauchy_a = 1.5046f, cauchy_b = 0.0042f;  // Dispersive
+  Float cauchy_a = FL(1.5046), cauchy_b = FL(0.0042);  // Dispersive
   bool sellmeier = false;       // Dispersive, Sellmeier form (extension)
   Float sell_b[3] = {0, 0, 0}, sell_c[3] = {0, 0, 0};
-  Float spread = 10.0f;         // ConeLight
+  Float spread = FL(10.0);         // ConeLight
   bool thin_film = false;
-  Float tf_ior = 1.5f, tf_thickness = 500.0f;
+  Float tf_ior = FL(1.5), tf_thickness = FL(500.0);
 
   bool is_wavelength_dependent() const { return thin_film || kind == M_DISPERSIVE; }  // materials.rs:90-92
 
   // clovers/src/materials/dispersive.rs:80-83 (Cauchy); Sellmeier is this build's extension
   Float dispersive_index(int lambda) const {
-    Float wave_micros = (Float)lambda / 1000.0f;
+    Float wave_micros = (Float)lambda / FL(1000.0);
     if (!sellmeier) return cauchy_a + (cauchy_b / (wave_micros * wave_micros));
     Float l2 = wave_micros * wave_micros;
-    Float s = 1.0f;
+    Float s = FL(1.0);
     for (int i = 0; i < 3; ++i) s = s + sell_b[i] * l2 / (l2 - sell_c[i]);
     return std::sqrt(s);
   }
@@ -578,12 +597,12 @@ struct Material {
       case M_DIELECTRIC:
       case M_DISPERSIVE: {  // dielectric.rs:37-81, dispersive.rs:58-123
         Float ri = kind == M_DIELECTRIC ? refractive_index : dispersive_index(ray.wavelength);
-        Float ratio = rec.front_face ? 1.0f / ri : ri;
+        Float ratio = rec.front_face ? FL(1.0) / ri : ri;
         Vec3 d = ray.direction;
-        Float cos_theta = rmin(-dot(d, rec.normal), 1.0f);
-        Float sin_theta = std::sqrt(1.0f - cos_theta * cos_theta);
+        Float cos_theta = rmin(-dot(d, rec.normal), FL(1.0));
+        Float sin_theta = std::sqrt(FL(1.0) - cos_theta * cos_theta);
         Vec3 sdir;
-        if (ratio * sin_theta > 1.0f) {
+        if (ratio * sin_theta > FL(1.0)) {
           sdir = reflect(d, rec.normal);
         } else {
           Float rp = schlick(cos_theta, ratio);
@@ -603,50 +622,50 @@ struct Material {
   bool scattering_pdf(const HitRecord& rec, const Ray& scattered, Float& out) const {
     if (kind == M_LAMBERTIAN) {
       Float c = dot(rec.normal, normalize(scattered.direction));
-      if (c < 0.0f) return false;
+      if (c < FL(0.0)) return false;
       out = c / PI;
       return true;
     }
-    if (kind == M_ISOTROPIC) { out = 1.0f / (4.0f * PI); return true; }
+    if (kind == M_ISOTROPIC) { out = FL(1.0) / (FL(4.0) * PI); return true; }
     return false;
   }
   Float emit(const Ray& ray, int lambda, const HitRecord& rec) const {
     if (kind == M_DIFFUSELIGHT) {  // diffuse_light.rs:41-53
-      if (!rec.front_face) return 0.0f;
+      if (!rec.front_face) return FL(0.0);
       return tex.kind == TEX_ILLUMINANT ? tex.emit(lambda) : tex.color(lambda, rec);
     }
     if (kind == M_CONELIGHT) {  // cone_light.rs:43-66
-      if (!rec.front_face) return 0.0f;
+      if (!rec.front_face) return FL(0.0);
       Float spread_radians = spread * RADS_PER_DEG;
       Float angle = std::acos(-dot(ray.direction, rec.normal) / (norm(ray.direction) * norm(rec.normal)));
-      if (angle > spread_radians) return 0.0f;
+      if (angle > spread_radians) return FL(0.0);
       return tex.kind == TEX_ILLUMINANT ? tex.emit(lambda) : tex.color(lambda, rec);
     }
-    return 0.0f;
+    return FL(0.0);
   }
   Float kind_color(const Ray& ray, int lambda, const HitRecord& rec) const {
     (void)ray;
     switch (kind) {
       case M_DIELECTRIC: return color.get(lambda);
-      case M_DISPERSIVE: return 1.0f;
+      case M_DISPERSIVE: return FL(1.0);
       case M_CONELIGHT:
-      case M_DIFFUSELIGHT: return rclamp(tex.color(lambda, rec), 0.0f, 1.0f);
+      case M_DIFFUSELIGHT: return rclamp(tex.color(lambda, rec), FL(0.0), FL(1.0));
       default: return tex.color(lambda, rec);
     }
   }
   // clovers/src/materials.rs:95-102, thin_film.rs:31-54
   Float color_of(const Ray& ray, int lambda, const HitRecord& rec) const {
-    Float tf = 1.0f;
+    Float tf = FL(1.0);
     if (thin_film) {
-      Float n1 = 1.0f, n2 = tf_ior;
+      Float n1 = FL(1.0), n2 = tf_ior;
       Float n_ratio = n1 / n2;
       Float cos1 = -dot(ray.direction, rec.normal);
-      Float sin1 = std::sqrt(1.0f - cos1 * cos1);
+      Float sin1 = std::sqrt(FL(1.0) - cos1 * cos1);
       Float sin2 = n_ratio * sin1;
-      Float cos2 = std::sqrt(1.0f - (sin2 * sin2));
-      Float opd = 2.0f * tf_ior * tf_thickness * cos2;
+      Float cos2 = std::sqrt(FL(1.0) - (sin2 * sin2));
+      Float opd = FL(2.0) * tf_ior * tf_thickness * cos2;
       Float m = opd / (Float)lambda;
-      tf = 1.0f + std::cos(m * 2.0f * PI);
+      tf = FL(1.0) + std::cos(m * FL(2.0) * PI);
     }
     return kind_color(ray, lambda, rec) * tf;
   }
@@ -682,7 +701,7 @@ struct Hitable {
 struct Empty : Hitable {  // clovers/src/hitable.rs:38-72
   bool hit(const Ray&, Float, Float, Rng*, HitRecord&, Counters*) const override { return false; }
   const AABB* aabb() const override { return nullptr; }
-  Float pdf_value(Vec3, Vec3, int, Float, Rng*) const override { return 0.0f; }
+  Float pdf_value(Vec3, Vec3, int, Float, Rng*) const override { return FL(0.0); }
   Vec3 centroid() const override { return Vec3(0, 0, 0); }
   bool is_empty() const override { return true; }
 };
@@ -704,8 +723,8 @@ struct Sphere : Hitable {  // clovers/src/objects/sphere.rs
     Vec3 t = (p - center) / radius;
     Float phi = std::atan2(t.z, t.x);
     Float theta = std::asin(t.y);
-    u = 1.0f - (phi + PI) / (2.0f * PI);
-    v = (theta + PI / 2.0f) / PI;
+    u = FL(1.0) - (phi + PI) / (FL(2.0) * PI);
+    v = (theta + PI / FL(2.0)) / PI;
   }
   bool hit(const Ray& ray, Float dmin, Float dmax, Rng*, HitRecord& out, Counters* c) const override {
     if (c) c->prims++;
@@ -714,7 +733,7 @@ struct Sphere : Hitable {  // clovers/src/objects/sphere.rs
     Float half_b = dot(oc, ray.direction);
     Float cc = norm_squared(oc) - radius * radius;
     Float disc = half_b * half_b - a * cc;
-    if (disc > 0.0f) {
+    if (disc > FL(0.0)) {
       Float root = std::sqrt(disc);
       for (int k = 0; k < 2; ++k) {
         Float d = k == 0 ? (-half_b - root) / a : (-half_b + root) / a;
@@ -736,10 +755,10 @@ struct Sphere : Hitable {  // clovers/src/objects/sphere.rs
   Float pdf_value(Vec3 origin, Vec3 direction, int lambda, Float time, Rng* rng) const override {
     Ray r{origin, direction, time, lambda};
     HitRecord rec;
-    if (!hit(r, EPSILON_SHADOW_ACNE, INFINITY, rng, rec, nullptr)) return 0.0f;
-    Float cos_theta_max = std::sqrt(1.0f - radius * radius / norm_squared(center - origin));
-    Float solid_angle = 2.0f * PI * (1.0f - cos_theta_max);
-    return 1.0f / solid_angle;
+    if (!hit(r, EPSILON_SHADOW_ACNE, INFINITY, rng, rec, nullptr)) return FL(0.0);
+    Float cos_theta_max = std::sqrt(FL(1.0) - radius * radius / norm_squared(center - origin));
+    Float solid_angle = FL(2.0) * PI * (FL(1.0) - cos_theta_max);
+    return FL(1.0) / solid_angle;
   }
   Vec3 random(Vec3 origin, Rng& rng) const override;
   bool has_random() const override { return true; }
@@ -765,7 +784,7 @@ struct MovingSphere : Hitable {  // clovers/src/objects/moving_sphere.rs
     Float half_b = dot(oc, ray.direction);
     Float cc = norm_squared(oc) - radius * radius;
     Float disc = half_b * half_b - a * cc;
-    if (disc > 0.0f) {
+    if (disc > FL(0.0)) {
       Float root = std::sqrt(disc);
       for (int k = 0; k < 2; ++k) {
         Float d = k == 0 ? (-half_b - root) / a : (-half_b + root) / a;
@@ -776,8 +795,8 @@ struct MovingSphere : Hitable {  // clovers/src/objects/moving_sphere.rs
           Vec3 t = (out.position - center(ray.time)) / radius;
           Float phi = std::atan2(t.z, t.x);
           Float theta = std::asin(t.y);
-          out.u = 1.0f - (phi + PI) / (2.0f * PI);
-          out.v = (theta + PI / 2.0f) / PI;
+          out.u = FL(1.0) - (phi + PI) / (FL(2.0) * PI);
+          out.v = (theta + PI / FL(2.0)) / PI;
           out.material = material;
           out.set_face_normal(ray, outward);
           tag_gid(out, gid);
@@ -788,8 +807,8 @@ struct MovingSphere : Hitable {  // clovers/src/objects/moving_sphere.rs
     return false;
   }
   const AABB* aabb() const override { return &box; }
-  Float pdf_value(Vec3, Vec3, int, Float, Rng*) const override { return 0.0f; }
-  Vec3 centroid() const override { return center(0.5f); }
+  Float pdf_value(Vec3, Vec3, int, Float, Rng*) const override { return FL(0.0); }
+  Vec3 centroid() const override { return center(FL(0.5)); }
 };
 
 // Shared plane-primitive state for Quad and Triangle (quad.rs:61-83, triangle.rs:61-101)
@@ -810,21 +829,21 @@ struct Planar : Hitable {
     const int kz = ad[0] > ad[1] ? (ad[0] > ad[2] ? 0 : 2) : (ad[1] > ad[2] ? 1 : 2);
     int kx = (kz + 1) % 3, ky = (kx + 1) % 3;
     auto cmp = [](const Vec3& a, int i) { return i == 0 ? a.x : (i == 1 ? a.y : a.z); };
-    if (cmp(dd, kz) < 0.0f) std::swap(kx, ky);
-    const Float sx = cmp(dd, kx) / cmp(dd, kz), sy = cmp(dd, ky) / cmp(dd, kz), sz = 1.0f / cmp(dd, kz);
+    if (cmp(dd, kz) < FL(0.0)) std::swap(kx, ky);
+    const Float sx = cmp(dd, kx) / cmp(dd, kz), sy = cmp(dd, ky) / cmp(dd, kz), sz = FL(1.0) / cmp(dd, kz);
     const Vec3 A = corner[0] - ray.origin, B = corner[1] - ray.origin, C = corner[2] - ray.origin;
     const Float Ax = cmp(A, kx) - sx * cmp(A, kz), Ay = cmp(A, ky) - sy * cmp(A, kz);
     const Float Bx = cmp(B, kx) - sx * cmp(B, kz), By = cmp(B, ky) - sy * cmp(B, kz);
     const Float Cx = cmp(C, kx) - sx * cmp(C, kz), Cy = cmp(C, ky) - sy * cmp(C, kz);
     Float U = Cx * By - Cy * Bx, V = Ax * Cy - Ay * Cx, W = Bx * Ay - By * Ax;
-    if (U == 0.0f || V == 0.0f || W == 0.0f) {
+    if (U == FL(0.0) || V == FL(0.0) || W == FL(0.0)) {
       U = (Float)((double)Cx * By - (double)Cy * Bx);
       V = (Float)((double)Ax * Cy - (double)Ay * Cx);
       W = (Float)((double)Bx * Ay - (double)By * Ax);
     }
-    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+    if ((U < FL(0.0) || V < FL(0.0) || W < FL(0.0)) && (U > FL(0.0) || V > FL(0.0) || W > FL(0.0))) return false;
     const Float det = U + V + W;
-    if (det == 0.0f) return false;
+    if (det == FL(0.0)) return false;
     const Float T = U * (sz * cmp(A, kz)) + V * (sz * cmp(B, kz)) + W * (sz * cmp(C, kz));
     t = T / det;
     if (!(t >= dmin && t <= dmax)) return false;
@@ -842,7 +861,7 @@ struct Planar : Hitable {
     d = -(dot(normal, q));
     w = n / dot(n, n);
     if (tri) {
-      area = norm(n) / 2.0f;
+      area = norm(n) / FL(2.0);
       Vec3 c1 = q, c2 = q + u, c3 = q + v;
       box = AABB(Interval(rmin(rmin(c1.x, c2.x), c3.x), rmax(rmax(c1.x, c2.x), c3.x)),
                  Interval(rmin(rmin(c1.y, c2.y), c3.y), rmax(rmax(c1.y, c2.y), c3.y)),
@@ -869,8 +888,8 @@ struct Planar : Hitable {
       Vec3 ph = p - q;
       alpha = dot(w, cross(ph, v));
       beta = dot(w, cross(u, ph));
-      bool inside = (alpha >= 0.0f && alpha <= 1.0f) && (beta >= 0.0f && beta <= 1.0f);
-      if (triangle) inside = inside && (alpha + beta <= 1.0f);
+      bool inside = (alpha >= FL(0.0) && alpha <= FL(1.0)) && (beta >= FL(0.0) && beta <= FL(1.0));
+      if (triangle) inside = inside && (alpha + beta <= FL(1.0));
       if (!inside) return false;
     }
     out.distance = t;
@@ -886,7 +905,7 @@ struct Planar : Hitable {
   Float pdf_value(Vec3 origin, Vec3 direction, int lambda, Float time, Rng* rng) const override {
     Ray r{origin, direction, time, lambda};
     HitRecord rec;
-    if (!hit(r, EPSILON_SHADOW_ACNE, INFINITY, rng, rec, nullptr)) return 0.0f;
+    if (!hit(r, EPSILON_SHADOW_ACNE, INFINITY, rng, rec, nullptr)) return FL(0.0);
     Float dist2 = rec.distance * rec.distance * norm_squared(direction);
     Float cosine = std::fabs(dot(direction, rec.normal)) / norm(direction);
     return dist2 / (cosine * area);
@@ -899,12 +918,12 @@ struct Planar : Hitable {
       return (pa + (b * v)) - origin;
     }
     Float a = rng.next_f32(), b = rng.next_f32();
-    if (a + b > 1.0f) { a = 1.0f - a; b = 1.0f - b; }
+    if (a + b > FL(1.0)) { a = FL(1.0) - a; b = FL(1.0) - b; }
     return (q + (a * u) + (b * v)) - origin;
   }
   bool has_random() const override { return true; }
   Vec3 centroid() const override {
-    return triangle ? q + (u / 4.0f) + (v / 4.0f) : q + (u / 2.0f) + (v / 2.0f);
+    return triangle ? q + (u / FL(4.0)) + (v / FL(4.0)) : q + (u / FL(2.0)) + (v / FL(2.0));
   }
 };
 
@@ -912,7 +931,7 @@ struct Planar : Hitable {
 struct ONB {
   Vec3 u, v, w;
   explicit ONB(Vec3 w_) : w(w_) {
-    Vec3 a = std::fabs(w.x) > 0.9f ? normalize(Vec3(0, 1, 0)) : normalize(Vec3(1, 0, 0));
+    Vec3 a = std::fabs(w.x) > FL(0.9) ? normalize(Vec3(0, 1, 0)) : normalize(Vec3(1, 0, 0));
     v = normalize(cross(w, a));
     u = normalize(cross(w, v));
   }
@@ -924,10 +943,10 @@ Vec3 Sphere::random(Vec3 origin, Rng& rng) const {
   ONB uvw(normalize(offset));
   Float r1 = rng.next_f32();
   Float r2 = rng.next_f32();
-  Float z = 1.0f + r2 * (std::sqrt(1.0f - radius * radius / dist2) - 1.0f);
-  Float phi = 2.0f * PI * r1;
-  Float x = std::cos(phi) * std::sqrt(1.0f - z * z);
-  Float y = std::sin(phi) * std::sqrt(1.0f - z * z);
+  Float z = FL(1.0) + r2 * (std::sqrt(FL(1.0) - radius * radius / dist2) - FL(1.0));
+  Float phi = FL(2.0) * PI * r1;
+  Float x = std::cos(phi) * std::sqrt(FL(1.0) - z * z);
+  Float y = std::sin(phi) * std::sqrt(FL(1.0) - z * z);
   return uvw.local(normalize(Vec3(x, y, z)));
 }
 
@@ -965,8 +984,8 @@ struct Boxy : Hitable {  // clovers/src/objects/boxy.rs
   }
   const AABB* aabb() const override { return &box; }
   Float pdf_value(Vec3 o, Vec3 d, int l, Float t, Rng* rng) const override {
-    Float sum = 0.0f;
-    for (auto& s : sides) sum += s->pdf_value(o, d, l, t, rng) / 6.0f;
+    Float sum = FL(0.0);
+    for (auto& s : sides) sum += s->pdf_value(o, d, l, t, rng) / FL(6.0);
     return sum;
   }
   Vec3 centroid() const override { return box.centroid(); }
@@ -994,7 +1013,7 @@ struct HitableList : Hitable {  // clovers/src/hitable.rs:123-195
     return any;
   }
   const AABB* aabb() const override { return &box; }
-  Float pdf_value(Vec3, Vec3, int, Float, Rng*) const override { return 0.0f; }
+  Float pdf_value(Vec3, Vec3, int, Float, Rng*) const override { return FL(0.0); }
   Vec3 centroid() const override { return box.centroid(); }
   bool is_list() const override { return true; }
 };
@@ -1016,9 +1035,9 @@ struct RotateY : Hitable {  // clovers/src/objects/rotate.rs
       for (int j = 0; j < 2; ++j)
         for (int k = 0; k < 2; ++k) {
           Float fi = (Float)i, fj = (Float)j, fk = (Float)k;
-          Float x = fi * b->x.max + (1.0f - fi) * b->x.min;
-          Float y = fj * b->y.max + (1.0f - fj) * b->y.min;
-          Float z = fk * b->z.max + (1.0f - fk) * b->z.min;
+          Float x = fi * b->x.max + (FL(1.0) - fi) * b->x.min;
+          Float y = fj * b->y.max + (FL(1.0) - fj) * b->y.min;
+          Float z = fk * b->z.max + (FL(1.0) - fk) * b->z.min;
           Float nx = cos_t * x + sin_t * z;
           Float nz = -sin_t * x + cos_t * z;
           Vec3 t(nx, y, nz);
@@ -1052,7 +1071,7 @@ struct RotateY : Hitable {  // clovers/src/objects/rotate.rs
     return true;
   }
   const AABB* aabb() const override { return has_box ? &box : nullptr; }
-  Float pdf_value(Vec3, Vec3, int, Float, Rng*) const override { return 0.0f; }
+  Float pdf_value(Vec3, Vec3, int, Float, Rng*) const override { return FL(0.0); }
   Vec3 centroid() const override { return object->centroid(); }
 };
 
@@ -1091,7 +1110,7 @@ struct ConstantMedium : Hitable {  // clovers/src/objects/constant_medium.rs
   ConstantMedium(HPtr b, Float density, const Texture& tex) : boundary(std::move(b)) {
     phase.kind = M_ISOTROPIC;
     phase.tex = tex;
-    neg_inv_density = -1.0f / density;
+    neg_inv_density = -FL(1.0) / density;
   }
   bool hit(const Ray& ray, Float dmin, Float dmax, Rng* rng, HitRecord& out, Counters* c) const override {
     HitRecord r1, r2;
@@ -1100,11 +1119,11 @@ struct ConstantMedium : Hitable {  // clovers/src/objects/constant_medium.rs
     if (r1.distance < dmin) r1.distance = dmin;
     if (r2.distance > dmax) r2.distance = dmax;
     if (r1.distance >= r2.distance) return false;
-    if (r1.distance < 0.0f) r1.distance = 0.0f;
+    if (r1.distance < FL(0.0)) r1.distance = FL(0.0);
     Float ray_length = norm(ray.direction);
     Float inside = (r2.distance - r1.distance) * ray_length;
     if (!rng) throw std::runtime_error("ConstantMedium needs randomness");
-    Float hit_distance = neg_inv_density * std::log(rng->next_f32());
+    Float hit_distance = neg_inv_density * ln(rng->next_f32());
     if (hit_distance > inside) return false;
     out.distance = r1.distance + hit_distance / ray_length;
     out.position = ray.evaluate(out.distance);
@@ -1213,7 +1232,7 @@ static Float evaluate_sah(const std::vector<HPtr>& hs, int axis, Float pos) {
 // surface_area_heuristic.rs:81-132
 static void find_best_split(const std::vector<HPtr>& hs, int& best_axis, Float& best_pos) {
   best_axis = 0;
-  best_pos = 0.0f;
+  best_pos = FL(0.0);
   Float best_cost = INFINITY;
   for (int axis = 0; axis < 3; ++axis) {
     Float bmin = INFINITY, bmax = -INFINITY;
@@ -1223,7 +1242,7 @@ static void find_best_split(const std::vector<HPtr>& hs, int& best_axis, Float& 
       bmax = rmax(bmax, cv);
     }
     if (bmin == bmax) continue;
-    Float scale = (bmax - bmin) / 8.0f;
+    Float scale = (bmax - bmin) / FL(8.0);
     for (int i = 0; i < 8; ++i) {
       Float cand = bmin + (Float)i * scale;
       Float cost = evaluate_sah(hs, axis, cand);
@@ -1334,17 +1353,17 @@ struct Camera {  // clovers/src/camera.rs:59-126
   Vec3 llc, horizontal, vertical, origin, u, v, w;
   Float lens_radius = 0;
   void init(Vec3 look_from, Vec3 look_at, Vec3 up, Float vfov, Float aspect, Float aperture, Float focus) {
-    lens_radius = aperture / 2.0f;
-    Float theta = vfov * PI / 180.0f;
-    Float half_height = std::tan(theta / 2.0f);
+    lens_radius = aperture / FL(2.0);
+    Float theta = vfov * PI / FL(180.0);
+    Float half_height = std::tan(theta / FL(2.0));
     Float half_width = aspect * half_height;
     origin = look_from;
     w = normalize(look_from - look_at);
     u = normalize(cross(up, w));
     v = normalize(cross(w, u));
     llc = origin - (half_width * focus) * u - (half_height * focus) * v - focus * w;
-    horizontal = (2.0f * half_width * focus) * u;
-    vertical = (2.0f * half_height * focus) * v;
+    horizontal = (FL(2.0) * half_width * focus) * u;
+    vertical = (FL(2.0) * half_height * focus) * v;
   }
   Ray get_ray(Float pu, Float pv, Float lx, Float ly, Float time, int lambda) const {
     lx *= lens_radius;
@@ -1409,7 +1428,7 @@ static void color_init(const Value& v, Float out[3]) {
     if (!s.empty() && s[0] == '#') s = s.substr(1);
     if (s.size() == 3) s = std::string{s[0], s[0], s[1], s[1], s[2], s[2]};
     if (s.size() != 6) throw std::runtime_error("bad hex colour");
-    for (int i = 0; i < 3; ++i) t[i] = (Float)(hexval(s[2 * i]) * 16 + hexval(s[2 * i + 1])) / 255.0f;
+    for (int i = 0; i < 3; ++i) t[i] = (Float)(hexval(s[2 * i]) * 16 + hexval(s[2 * i + 1])) / FL(255.0);
     srgb_to_xyz_e(t, out);
   } else if (k == "srgb") {
     json_rgb(c, t, "srgb");
@@ -1441,7 +1460,7 @@ static int illuminant_index(const std::string& kind) {
 }
 static Texture texture_default() {
   Texture t;
-  Float g[3] = {0.5f, 0.5f, 0.5f};
+  Float g[3] = {FL(0.5), FL(0.5), FL(0.5)};
   t.kind = TEX_SOLID;
   t.even = SPD(g);
   return t;
@@ -1455,17 +1474,17 @@ static Texture texture_init(const Value& v) {
     t.kind = TEX_SOLID;
     t.even = SPD(xyz);
   } else if (kind == "SpatialChecker" || kind == "SurfaceChecker") {
-    Float ev[3] = {0.8f, 0.8f, 0.8f}, od[3] = {0.5f, 0.5f, 0.5f};
+    Float ev[3] = {FL(0.8), FL(0.8), FL(0.8)}, od[3] = {FL(0.5), FL(0.5), FL(0.5)};
     if (v.has("even")) color_init(v.at("even"), ev);
     if (v.has("odd")) color_init(v.at("odd"), od);
     t.kind = kind == "SpatialChecker" ? TEX_SPATIAL : TEX_SURFACE;
     t.even = SPD(ev);
     t.odd = SPD(od);
-    t.density = v.has("density") ? v.at("density").as_f32() : (kind == "SpatialChecker" ? 1.0f : 10.0f);
+    t.density = v.has("density") ? v.at("density").as_f32() : (kind == "SpatialChecker" ? FL(1.0) : FL(10.0));
   } else if (kind.rfind(kIllumPrefix, 0) == 0) {
     t.kind = TEX_ILLUMINANT;
     t.illuminant = illuminant_index(kind);
-    t.intensity = v.has("intensity") ? v.at("intensity").as_f32() : 1.0f;
+    t.intensity = v.has("intensity") ? v.at("intensity").as_f32() : FL(1.0);
   } else {
     throw std::runtime_error("unknown texture kind: " + kind);
   }
@@ -1480,11 +1499,11 @@ static Material material_init(const Value& v) {
   } else if (kind == "Metal") {
     m.kind = M_METAL;
     m.tex = v.has("albedo") ? texture_init(v.at("albedo")) : texture_default();
-    m.fuzz = v.has("fuzz") ? v.at("fuzz").as_f32() : 0.0f;
+    m.fuzz = v.has("fuzz") ? v.at("fuzz").as_f32() : FL(0.0);
   } else if (kind == "Dielectric") {
     m.kind = M_DIELECTRIC;
-    m.refractive_index = v.has("refractive_index") ? v.at("refractive_index").as_f32() : 1.5f;
-    Float c[3] = {1.0f, 1.0f, 1.0f};
+    m.refractive_index = v.has("refractive_index") ? v.at("refractive_index").as_f32() : FL(1.5);
+    Float c[3] = {FL(1.0), FL(1.0), FL(1.0)};
     if (v.has("color")) {
       Vec3 x = json_vec3(v.at("color"), "color");
       c[0] = x.x; c[1] = x.y; c[2] = x.z;
@@ -1512,8 +1531,8 @@ static Material material_init(const Value& v) {
   if (v.has("thin_film") && !v.at("thin_film").is_null()) {
     const Value& tf = v.at("thin_film");
     m.thin_film = true;
-    m.tf_ior = tf.has("refractive_index") ? tf.at("refractive_index").as_f32() : 1.5f;
-    m.tf_thickness = tf.has("thickness") ? tf.at("thickness").as_f32() : 500.0f;
+    m.tf_ior = tf.has("refractive_index") ? tf.at("refractive_index").as_f32() : FL(1.5);
+    m.tf_thickness = tf.has("thickness") ? tf.at("thickness").as_f32() : FL(500.0);
   }
   return m;
 }
@@ -1696,8 +1715,8 @@ struct Loader {
     if (kind == "Sphere")
       return HPtr(new Sphere(json_vec3(o.at("center"), "center"), o.at("radius").as_f32(), material_ref(o.find("material"))));
     if (kind == "MovingSphere")
-      return HPtr(new MovingSphere(json_vec3(o.at("center_0"), "center_0"), json_vec3(o.at("center_1"), "center_1"), 0.0f,
-                                   1.0f, o.at("radius").as_f32(), material_ref(o.find("material"))));
+      return HPtr(new MovingSphere(json_vec3(o.at("center_0"), "center_0"), json_vec3(o.at("center_1"), "center_1"), FL(0.0),
+                                   FL(1.0), o.at("radius").as_f32(), material_ref(o.find("material"))));
     if (kind == "Quad" || kind == "Triangle")
       return HPtr(new Planar(json_vec3(o.at("q"), "q"), json_vec3(o.at("u"), "u"), json_vec3(o.at("v"), "v"),
                              material_ref(o.find("material")), kind == "Triangle"));
@@ -1706,7 +1725,7 @@ struct Loader {
                            material_ref(o.find("material"))));
     if (kind == "ConstantMedium") {
       HPtr b = object(o.at("boundary"), nullptr);
-      Float density = o.has("density") ? o.at("density").as_f32() : 0.1f;
+      Float density = o.has("density") ? o.at("density").as_f32() : FL(0.1);
       Texture t = o.has("texture") ? texture_init(o.at("texture")) : texture_default();
       return HPtr(new ConstantMedium(std::move(b), density, t));
     }
@@ -1755,7 +1774,7 @@ static Scene* load_scene(const std::string& text, uint32_t width, uint32_t heigh
   }
   sc->materials.emplace_back(new Material());  // SharedMaterial::default(): Lambertian, grey 0.5
   {
-    Float g[3] = {0.5f, 0.5f, 0.5f};
+    Float g[3] = {FL(0.5), FL(0.5), FL(0.5)};
     sc->materials.back()->tex.even = SPD(g);
   }
   ld.shared.emplace_back(std::string(), sc->materials.back().get());
@@ -1792,7 +1811,7 @@ static Scene* load_scene(const std::string& text, uint32_t width, uint32_t heigh
 static Scene* mesh_scene(const float* verts, uint32_t nverts, const uint32_t* idx, uint32_t ntris) {
   std::unique_ptr<Scene> sc(new Scene());
   sc->materials.emplace_back(new Material());
-  Float g[3] = {0.5f, 0.5f, 0.5f};
+  Float g[3] = {FL(0.5), FL(0.5), FL(0.5)};
   sc->materials.back()->tex.even = SPD(g);
   const Material* m = sc->materials.back().get();
   std::vector<HPtr> hs;
@@ -1821,11 +1840,11 @@ static void trace(const Ray& ray, const Scene& sc, uint32_t depth, uint32_t max_
   Float bg[4];
   for (int i = 0; i < 4; ++i) bg[i] = sc.background_spd.get(waves[i]);
   if (depth > max_depth) {
-    for (int i = 0; i < 4; ++i) out[i] = 0.0f;
+    for (int i = 0; i < 4; ++i) out[i] = FL(0.0);
     return;
   }
   HitRecord rec;
-  if (!sc.bvh_root->hit(ray, EPSILON_SHADOW_ACNE, 3.40282347e+38f, &rng, rec, nullptr)) {
+  if (!sc.bvh_root->hit(ray, EPSILON_SHADOW_ACNE, FL(3.40282347e+38), &rng, rec, nullptr)) {
     for (int i = 0; i < 4; ++i) out[i] = bg[i];
     return;
   }
@@ -1840,7 +1859,7 @@ static void trace(const Ray& ray, const Scene& sc, uint32_t depth, uint32_t max_
   Float atten[4];
   if (m->is_wavelength_dependent()) {
     atten[0] = m->color_of(ray, hero, rec);
-    atten[1] = atten[2] = atten[3] = 0.0f;
+    atten[1] = atten[2] = atten[3] = FL(0.0);
   } else {
     for (int i = 0; i < 4; ++i) atten[i] = m->color_of(ray, waves[i], rec);
   }
@@ -1865,13 +1884,13 @@ static void trace(const Ray& ray, const Scene& sc, uint32_t depth, uint32_t max_
   Float bsdf_v;
   if (srec.pdf == PDF_COSINE) {
     Float cosine = dot(normalize(direction), srec.pdf_w);
-    bsdf_v = cosine <= 0.0f ? 0.0f : cosine / PI;
+    bsdf_v = cosine <= FL(0.0) ? FL(0.0) : cosine / PI;
   } else if (srec.pdf == PDF_SPHERE) {
-    bsdf_v = 1.0f / (4.0f * PI);
+    bsdf_v = FL(1.0) / (FL(4.0) * PI);
   } else {
-    bsdf_v = 0.0f;
+    bsdf_v = FL(0.0);
   }
-  Float mis = 0.5f * light_v + 0.5f * bsdf_v;
+  Float mis = FL(0.5) * light_v + FL(0.5) * bsdf_v;
   Float spdf;
   if (!m->scattering_pdf(rec, sray, spdf)) {
     for (int i = 0; i < 4; ++i) out[i] = emitted[i];
@@ -1921,14 +1940,14 @@ static void render_pixel(const Scene& sc, uint32_t x, uint32_t r, uint32_t width
     rotate_wavelength(ray.wavelength, waves);
     Float p[4];
     trace(ray, sc, 0, max_depth, rng, p);
-    if (p[1] == 0.0f && p[2] == 0.0f && p[3] == 0.0f) {
+    if (p[1] == FL(0.0) && p[2] == FL(0.0) && p[3] == FL(0.0)) {
       const Float* c = cmf_table[waves[0] - 380];
       for (int k = 0; k < 3; ++k) acc[k] += (double)(c[k] * p[0]);
     } else {
       for (int i = 0; i < 4; ++i) {
-        if (std::isnormal(p[i]) && p[i] > 0.0f) {
+        if (std::isnormal(p[i]) && p[i] > FL(0.0)) {
           const Float* c = cmf_table[waves[i] - 380];
-          for (int k = 0; k < 3; ++k) acc[k] += (double)(c[k] * p[i] / 4.0f);
+          for (int k = 0; k < 3; ++k) acc[k] += (double)(c[k] * p[i] / FL(4.0));
         }
       }
     }
@@ -1976,11 +1995,23 @@ int orc_spectral_power(float x, float y, float z, int lambda, float* out) {
     return -1;
   }
 }
-void orc_wavelength_into_xyz(int lambda, float out[3]) { wavelength_into_xyz(lambda, out); }
+void orc_wavelength_into_xyz(int lambda, float out[3]) {
+  Float o[3];
+  wavelength_into_xyz(lambda, o);
+  for (int k = 0; k < 3; ++k) out[k] = (float)o[k];
+}
 void orc_rotate_wavelength(int hero, int out[4]) { rotate_wavelength(hero, out); }
-void orc_srgb_to_xyz_e(const float rgb[3], float out[3]) { srgb_to_xyz_e(rgb, out); }
+void orc_srgb_to_xyz_e(const float rgb[3], float out[3]) {
+  const Float in[3] = {rgb[0], rgb[1], rgb[2]};
+  Float o[3];
+  srgb_to_xyz_e(in, o);
+  for (int k = 0; k < 3; ++k) out[k] = (float)o[k];
+}
 void orc_xyz_e_to_srgb8(const float* xyz, uint64_t n, uint8_t* rgb) {
-  for (uint64_t i = 0; i < n; ++i) xyz_e_to_srgb8(xyz + 3 * i, rgb + 3 * i);
+  for (uint64_t i = 0; i < n; ++i) {
+    const Float in[3] = {xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]};
+    xyz_e_to_srgb8(in, rgb + 3 * i);
+  }
 }
 // Interval / AABB known-answer helpers: box = {xmin,xmax,ymin,ymax,zmin,zmax} (Interval::new order-normalises)
 float orc_aabb_area(const float b[6]) {
@@ -2002,7 +2033,7 @@ void orc_aabb_combine(const float a[6], const float b[6], float out[6]) {
 // ray = {ox,oy,oz,tmin,dx,dy,dz,tmax}
 int orc_aabb_hit(const float b[6], const float ray[8]) {
   AABB a(Interval(b[0], b[1]), Interval(b[2], b[3]), Interval(b[4], b[5]));
-  Ray r{Vec3(ray[0], ray[1], ray[2]), Vec3(ray[4], ray[5], ray[6]), 0.0f, 600};
+  Ray r{Vec3(ray[0], ray[1], ray[2]), Vec3(ray[4], ray[5], ray[6]), FL(0.0), 600};
   return a.hit(r, ray[3], ray[7]) ? 1 : 0;
 }
 void orc_interval(float a, float b, float out[4]) {
@@ -2022,11 +2053,11 @@ int orc_prim_hit(int kind, const float q[3], const float u[3], const float v[3],
   const AABB* b = h->aabb();
   float bb[6] = {b->x.min, b->x.max, b->y.min, b->y.max, b->z.min, b->z.max};
   std::memcpy(box_out, bb, sizeof bb);
-  Ray r{Vec3(ray[0], ray[1], ray[2]), Vec3(ray[4], ray[5], ray[6]), 0.0f, 600};
+  Ray r{Vec3(ray[0], ray[1], ray[2]), Vec3(ray[4], ray[5], ray[6]), FL(0.0), 600};
   HitRecord rec;
   if (!h->hit(r, ray[3], ray[7], nullptr, rec, nullptr)) return 0;
   float o[10] = {rec.distance, rec.position.x, rec.position.y, rec.position.z, rec.normal.x, rec.normal.y,
-                 rec.normal.z, rec.u, rec.v, rec.front_face ? 1.0f : 0.0f};
+                 rec.normal.z, rec.u, rec.v, rec.front_face ? FL(1.0) : FL(0.0)};
   std::memcpy(rec_out, o, sizeof o);
   return 1;
 }
@@ -2098,7 +2129,7 @@ uint64_t orc_scene_object_count(void* s) { return static_cast<Scene*>(s)->object
 
 // Camera rays for given sample parameters (parity of the ray generator).
 void orc_camera_ray(void* s, float pu, float pv, float lx, float ly, float out[6]) {
-  Ray r = static_cast<Scene*>(s)->camera.get_ray(pu, pv, lx, ly, 0.0f, 600);
+  Ray r = static_cast<Scene*>(s)->camera.get_ray(pu, pv, lx, ly, FL(0.0), 600);
   float o[6] = {r.origin.x, r.origin.y, r.origin.z, r.direction.x, r.direction.y, r.direction.z};
   std::memcpy(out, o, sizeof o);
 }
@@ -2120,13 +2151,13 @@ int orc_raycast(void* s, const float* rays, uint64_t n, uint32_t* prim, float* t
     uint64_t e = std::min<uint64_t>(n, (blk + 1) * 1024);
     for (uint64_t i = blk * 1024; i < e; ++i) {
       const float* r = rays + 8 * i;
-      Ray ray{Vec3(r[0], r[1], r[2]), Vec3(r[4], r[5], r[6]), 0.0f, 600};
+      Ray ray{Vec3(r[0], r[1], r[2]), Vec3(r[4], r[5], r[6]), FL(0.0), 600};
       HitRecord rec;
       Counters c;
       Rng rng(0, (uint32_t)i, 0);
       bool h = sc->bvh_root->hit(ray, r[3], r[7], &rng, rec, &c);
       prim[i] = h ? (uint32_t)rec.gid : 0xFFFFFFFFu;
-      t[i] = h ? rec.distance : 0.0f;
+      t[i] = h ? rec.distance : FL(0.0);
       if (nodes) nodes[i] = (uint32_t)c.nodes;
       if (prims) prims[i] = (uint32_t)c.prims;
     }
@@ -2166,6 +2197,39 @@ int orc_render(void* s, uint32_t width, uint32_t height, uint32_t spp, uint32_t 
   }
 }
 
+// The per-pixel sums of film deposits for a list of buffer pixels (index
+// r * width + x), e.g. a stratified subset of the image; one work unit per pixel.
+int orc_render_pixels(void* s, uint32_t width, uint32_t height, uint32_t spp, uint32_t max_depth, uint64_t seed,
+                      const uint32_t* pixels, uint64_t n, uint32_t sample_offset, double* xyz_out, int threads) {
+  try {
+    Scene* sc = static_cast<Scene*>(s);
+    ensure_cmf();
+    for (uint64_t i = 0; i < n; ++i)
+      if (pixels[i] >= (uint64_t)width * height) throw std::runtime_error("pixel index outside the image");
+    std::atomic<int> failed(0);
+    std::string msg;
+    parallel_for(n, threads, [&](uint64_t i) {
+      try {
+        render_pixel(*sc, pixels[i] % width, pixels[i] / width, width, height, spp, max_depth, seed, sample_offset,
+                     xyz_out + 3 * i);
+      } catch (std::exception& e) {
+        if (!failed.exchange(1)) msg = e.what();
+      }
+    });
+    if (failed) throw std::runtime_error(msg);
+    return 0;
+  } catch (std::exception& e) {
+    g_err = e.what();
+    return -1;
+  }
+}
+
+// ln of n f32 values through the render path's logarithm (clv_log.h), the
+// routine the GPU's media use.
+void orc_log_f32(const float* x, uint64_t n, float* y) {
+  for (uint64_t i = 0; i < n; ++i) y[i] = clv_math::log_f32(x[i]);
+}
+
 // Debug render modes (clovers-cli/src/draw_cpu.rs:148-207): one ray per pixel
 // through its corner (x / width, y / height), no lens offset, with a drawn
 // wavelength and time.  Mode 1 colours the hit normal (normals.rs:11-37),
@@ -2184,31 +2248,31 @@ int orc_render_debug(void* s, uint32_t width, uint32_t height, uint32_t mode, ui
         Rng rng(seed, (uint32_t)pix, sample_offset);
         const int lambda = random_wavelength(rng);
         const Float time = rng.next_f32();
-        const Ray ray = sc->camera.get_ray((Float)x / (Float)width, (Float)y / (Float)height, 0.0f, 0.0f, time, lambda);
+        const Ray ray = sc->camera.get_ray((Float)x / (Float)width, (Float)y / (Float)height, FL(0.0), FL(0.0), time, lambda);
         HitRecord rec;
         Counters c;
-        const bool any = sc->bvh_root->hit(ray, EPSILON_SHADOW_ACNE, 3.40282347e+38f, &rng, rec, &c);
+        const bool any = sc->bvh_root->hit(ray, EPSILON_SHADOW_ACNE, FL(3.40282347e+38), &rng, rec, &c);
         float* o = rgb_out + 3 * pix;
-        o[0] = o[1] = o[2] = 0.0f;
+        o[0] = o[1] = o[2] = FL(0.0);
         if (mode == 1) {
           if (any) {
             const Vec3 n{-rec.normal.x, rec.normal.y, -rec.normal.z};
-            o[0] = 0.5f + 0.5f * n.x;
-            o[1] = 0.5f + 0.5f * n.y;
-            o[2] = n.z < 0.0f ? 0.0f : n.z;
+            o[0] = FL(0.5) + FL(0.5) * n.x;
+            o[1] = FL(0.5) + FL(0.5) * n.y;
+            o[2] = n.z < FL(0.0) ? FL(0.0) : n.z;
           }
         } else {
           const uint64_t d = mode == 2 ? c.nodes : c.prims;
           if (d <= 255) {
-            o[0] = o[1] = o[2] = (Float)d / 255.0f;
+            o[0] = o[1] = o[2] = (Float)d / FL(255.0);
           } else if (d <= 511) {
-            o[0] = 1.0f;
-            o[1] = 1.0f;
+            o[0] = FL(1.0);
+            o[1] = FL(1.0);
           } else if (d <= 1023) {
-            o[0] = 1.0f;
-            o[1] = 0.5f;
+            o[0] = FL(1.0);
+            o[1] = FL(0.5);
           } else {
-            o[0] = 1.0f;
+            o[0] = FL(1.0);
           }
         }
       }
@@ -2230,7 +2294,9 @@ int orc_trace_sample(void* s, uint32_t width, uint32_t height, uint32_t x, uint3
     float ro[6] = {ray.origin.x, ray.origin.y, ray.origin.z, ray.direction.x, ray.direction.y, ray.direction.z};
     std::memcpy(ray_out, ro, sizeof ro);
     rotate_wavelength(ray.wavelength, waves_out);
-    trace(ray, *sc, 0, max_depth, rng, p_out);
+    Float p[4];
+    trace(ray, *sc, 0, max_depth, rng, p);
+    for (int k = 0; k < 4; ++k) p_out[k] = (float)p[k];
     return 0;
   } catch (std::exception& e) {
     g_err = e.what();

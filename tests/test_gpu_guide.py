@@ -168,3 +168,24 @@ def test_trained_guide_lowers_caustic_error():
     print("prism crop at %d spp: plain relMSE %.4g, guided %.4g" % (spp, e_plain, e_guided))
     assert e_guided < 0.8 * e_plain
     assert guide.status() == 0
+
+
+def test_bounded_wait_runs_out_and_frees_tmem():
+    """A wait on an mbarrier that nothing arrives on (no copy, no MMA in
+    flight) gives up after its clock limit: the kernel raises the guide's
+    timeout flag, frees its TMEM and returns; the context stays usable and a
+    normal guide call afterwards works."""
+    L = _lib.lib()
+    flags, freed = ctypes.c_uint32(), ctypes.c_uint32()
+    _lib.check(L.clv_guide_selftest_timeout(2000000, ctypes.byref(flags), ctypes.byref(freed)))
+    assert flags.value == 8  # CLV_ERR_GUIDE
+    assert freed.value == 1
+    g = cg.Guide(seed=3)
+    params = random_params(4)
+    g.set_params(params)
+    q = np.random.default_rng(5).random((300, 8)).astype(np.float32)
+    q[:, 7] = 0.0
+    out = g.forward(q)
+    ref = oracle.guide_forward(params, q)
+    assert np.linalg.norm(out - ref) <= 1e-2 * np.linalg.norm(ref)
+    assert g.status() == 0

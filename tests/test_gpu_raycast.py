@@ -34,6 +34,18 @@ def test_triangle_soup_parity(ntris, nrays):
         assert frac > 0.1
 
 
+def test_full_depth_tree_parity():
+    """The ray-cast workload's own tree: 2^20 random triangles (SAH, depth 29),
+    2^20 of its random rays; ids, distance bits and traversal counts equal the
+    oracle's on every ray."""
+    v, i = scenes.triangle_soup(1 << 20, seed=2)
+    rays = scenes.random_rays(1 << 20, seed=3)
+    h = cg.Scene.from_mesh(v, i)
+    assert h.info()["tree_depth"] >= 25
+    frac = _compare(h.upload(), oracle.Scene.from_mesh(v, i), rays)
+    assert frac > 0.5
+
+
 def test_shared_edges_and_grid_rays():
     # a regular grid mesh: many rays hit edges and vertices shared by two or more triangles
     n = 64

@@ -28,21 +28,20 @@ def relmse(img, ref, eps=1e-2):
     return float(np.mean((img - ref) ** 2 / (ref ** 2 + eps)))
 
 
-def _render(path, w, h, spp, depth, seed, engine="wavefront", **kw):
+def _render(path, w, h, spp, depth, seed, **kw):
     d = cg.Scene.from_json(path, w, h).upload()
     opts = cg.RenderOptions(input=path, width=w, height=h, samples=spp, max_depth=depth, seed=seed, **kw)
     stats = {}
-    img = cg.draw(cg.GlobalOptions(quiet=True), opts, d, stats=stats, engine=engine)
+    img = cg.draw(cg.GlobalOptions(quiet=True), opts, d, stats=stats)
     assert stats["device_errors"] == 0
     return img.astype(np.float64), stats
 
 
-@pytest.mark.parametrize("engine", ["wavefront", "megakernel"])
 @pytest.mark.parametrize("scene_fixture,w,h,spp,depth", [("box_scene_path", 48, 48, 32, 16),
                                                          ("spheres_scene_path", 64, 36, 16, 50)])
-def test_same_seed_matches_oracle(request, scene_fixture, w, h, spp, depth, engine):
+def test_same_seed_matches_oracle(request, scene_fixture, w, h, spp, depth):
     path = request.getfixturevalue(scene_fixture)
-    img, stats = _render(path, w, h, spp, depth, seed=1234, engine=engine)
+    img, stats = _render(path, w, h, spp, depth, seed=1234)
     ref = oracle.Scene.from_json(path, w, h).render(w, h, spp, depth, seed=1234) / spp
     assert stats["samples"] == w * h * spp
     err = relmse(img, ref)
@@ -90,10 +89,9 @@ def test_resolve_matches_oracle_conversion():
 def test_debug_modes_match_oracle(request, tmp_path, which, mode):
     """Normal map, BVH test count and primitive test count (draw_cpu.rs:148-207):
     the GPU's linear sRGB per pixel equals the oracle's on the same random
-    streams.  Exactly on scenes without media; the kitchen sink's media draw
-    free-flight distances through logf, whose last bit CUDA and the host libm
-    may round apart, so there a thousandth of the pixels may differ.  The sink
-    also holds a moving sphere, placed at each ray's time."""
+    streams, on every pixel, media included (their free-flight draws go through
+    the project's own log, the same bits on both sides).  The sink also holds a
+    moving sphere, placed at each ray's time."""
     import ctypes
     from clovers_gb300 import _lib
     if which == "sink":
@@ -111,7 +109,7 @@ def test_debug_modes_match_oracle(request, tmp_path, which, mode):
     ref = oracle.Scene.from_json(path, w, h).render_debug(w, h, mode, 21)
     same = np.all(gpu == ref, axis=1).mean()
     print("%s mode %d: %.4f of pixels identical" % (which, mode, same))
-    assert same >= (0.999 if which == "sink" else 1.0)
+    assert same == 1.0
     assert ref.max() > 0
     assert d.status() == 0
 

@@ -18,7 +18,7 @@ import clovers_gb300 as cg
 import oracle
 from clovers_gb300 import scenes
 
-REFERENCE = os.environ.get("CLOVERS_REFERENCE", "/root/reference")  # where the reference's files are read
+REFERENCE = os.environ.get("CLOVERS_REFERENCE", "")  # a checkout of the reference (its scenes/ folder)
 
 
 @pytest.fixture(scope="module")
@@ -37,7 +37,8 @@ def test_kitchen_sink_loads_identically(sink_path):
     assert info["compound"] > 5 and info["triangles"] >= 8
 
 
-@pytest.mark.skipif(not os.path.isdir(os.path.join(REFERENCE, "scenes")), reason="reference checkout not present")
+@pytest.mark.skipif(not REFERENCE or not os.path.isdir(os.path.join(REFERENCE, "scenes")),
+                    reason="CLOVERS_REFERENCE does not name a reference checkout")
 def test_reference_scene_files_load_like_the_oracle(monkeypatch):
     monkeypatch.chdir(REFERENCE)  # the reference's scenes name mesh paths relative to its root
     checked = 0
@@ -63,19 +64,18 @@ def test_reference_scene_files_load_like_the_oracle(monkeypatch):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("engine", ["wavefront", "megakernel"])
-def test_kitchen_sink_same_seed(sink_path, engine):
+def test_kitchen_sink_same_seed(sink_path):
     w, h, spp, depth = 80, 60, 16, 12
     d = cg.Scene.from_json(sink_path, w, h).upload()
     assert d.info["compound"] > 0
     stats = {}
     img = cg.draw(cg.GlobalOptions(quiet=True), cg.RenderOptions(width=w, height=h, samples=spp, max_depth=depth,
-                                                                 seed=77), d, stats=stats, engine=engine)
+                                                                 seed=77), d, stats=stats)
     assert stats["device_errors"] == 0
     ref = oracle.Scene.from_json(sink_path, w, h).render(w, h, spp, depth, seed=77) / spp
     err = float(np.mean((img - ref) ** 2 / (ref ** 2 + 1e-2)))
     close = np.all(np.abs(img - ref) <= 1e-4 * (np.abs(ref) + 1e-3), axis=1).mean()
-    print("kitchen sink %s: relMSE %.3g, pixels within tolerance %.4f" % (engine, err, close))
+    print("kitchen sink: relMSE %.3g, pixels within tolerance %.4f" % (err, close))
     assert err <= 1e-3
     assert close >= 0.95
 
@@ -92,18 +92,15 @@ def test_kitchen_sink_raycast_parity(sink_path):
     rays = np.concatenate([cam, extra])
     prim, t, nodes, tests = cg.raycast(d, rays, with_counts=True)
     oprim, ot, onodes, otests = o.raycast(rays, with_counts=True)
-    # media sample their free-flight distance with log(), whose last bit differs between CUDA and the
-    # host libm: for hits on a medium (top-level objects 11 and 12) distances agree within 4 ulp and the
-    # traversal counts may differ; everything else is bit-exact.
+    # media (top-level objects 11 and 12) draw their free-flight distance through the
+    # project's own log (clv_log.h), the same bits on both sides: every ray is exact,
+    # media hits included
     media = np.isin(oprim, [11, 12])
-    assert np.array_equal(prim[~media], oprim[~media])
-    hit = (oprim != 0xFFFFFFFF) & ~media
+    assert media.sum() > 100
+    assert np.array_equal(prim, oprim), "hit ids differ on %d rays" % int((prim != oprim).sum())
+    hit = oprim != 0xFFFFFFFF
     assert np.array_equal(t[hit].view(np.uint32), ot[hit].view(np.uint32))
-    mh = media & (prim == oprim)
-    ulps = np.abs(t[mh].view(np.int32).astype(np.int64) - ot[mh].view(np.int32).astype(np.int64))
-    assert ulps.size == 0 or ulps.max() <= 4
-    assert (prim[media] == oprim[media]).mean() > 0.99
-    bad = np.nonzero(((nodes != onodes) | (tests != otests)) & ~media)[0]
+    bad = np.nonzero((nodes != onodes) | (tests != otests))[0]
     if bad.size:
         for k in bad[:8]:
             print("ray %d %s prim %d/%d nodes %d/%d tests %d/%d" % (k, rays[k].tolist(), prim[k], oprim[k], nodes[k],
