@@ -27,8 +27,8 @@ import make_golden  # noqa: E402
 EPS = 1e-2
 # workload -> (spp used by the check, relMSE bound of the crop, of the whole-image subset)
 BOUNDS_CPU = {"box": (64, 8e-3, 3.5e-3)}
-BOUNDS_GPU = {"box": (256, 2.0e-3, 8.0e-4), "prism": (1024, 1.15e-2, 1.1e-3), "spheres": (256, None, None),
-              "dense": (64, None, None)}
+BOUNDS_GPU = {"box": (256, 2.0e-3, 8.0e-4), "prism": (1024, 1.15e-2, 1.1e-3), "spheres": (256, 3.6e-4, 6.0e-4),
+              "dense": (64, 7.0e-3, 4.1e-3)}
 
 
 def relmse(img, ref):
