@@ -564,7 +564,6 @@ struct clv_device_scene {
     if (scratch) cudaFree(scratch);
     if (wf_mem) cudaFree(wf_mem);
     if (wf_counters) cudaFree(wf_counters);
-    if (order_mem) cudaFree(order_mem);
     if (wf_live_host) cudaFreeHost(wf_live_host);
   }
   WfState wavefront_state(uint32_t q) {
@@ -595,28 +594,9 @@ struct clv_device_scene {
     W.grec_cap = 0;
     W.spill = nullptr;
     W.stack_cap = CLV_STACK;
-    W.order = nullptr;
-    W.order_key = nullptr;
-    W.order_hist = nullptr;
     return W;
   }
   static constexpr size_t kWfSlotBytes = 16 * 5 + 48 + 8 + 16;
-  // query order of the wavefront intersect: order and key per slot, bin counts
-  void* order_mem = nullptr;
-  uint32_t order_slots = 0;
-  void query_order(WfState& W) {
-    if (W.Q > order_slots) {
-      if (order_mem) cudaFree(order_mem);
-      order_mem = nullptr;
-      order_slots = 0;
-      ck(cudaMalloc(&order_mem, (size_t)W.Q * 8 + 4096), "cudaMalloc query order");
-      order_slots = W.Q;
-    }
-    char* p = static_cast<char*>(order_mem);
-    W.order_hist = reinterpret_cast<uint32_t*>(p);
-    W.order = reinterpret_cast<uint32_t*>(p + 4096);
-    W.order_key = W.order + W.Q;
-  }
   void* ensure_scratch(size_t bytes) {
     if (bytes > scratch_bytes) {
       if (scratch) cudaFree(scratch);
@@ -671,16 +651,6 @@ static GraphExec capture_graph(clv_device_scene* d, F enqueue) {
   }
   g.exec = ex;
   return g;
-}
-
-// Whether single-scene wavefront renders group their queries (wf_order_*)
-// before each intersect.  CLV_QUERY_ORDER=0 in the environment turns it off.
-static bool query_order_enabled() {
-  static const bool on = [] {
-    const char* e = std::getenv("CLV_QUERY_ORDER");
-    return !(e && e[0] == '0');
-  }();
-  return on;
 }
 
 static uint32_t launch_grid(uint64_t work, int block) {
@@ -1195,7 +1165,6 @@ static int render_wavefront(clv_device_scene* d, const clv_render_opts* o, doubl
       W.spill = d->spill_region((size_t)q * spill_entries * sizeof(float4));
       W.stack_cap = d->view.max_depth_tree;
     }
-    if (query_order_enabled()) d->query_order(W);
     WfCounters c0{std::min<uint64_t>(q, P.total), 0u, {0u, 0u, 0u, 0u}};
     ck(cudaMemcpyAsync(d->wf_counters, &c0, sizeof c0, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync");
     GuideDev G{};
@@ -1236,16 +1205,9 @@ static int render_wavefront(clv_device_scene* d, const clv_render_opts* o, doubl
       prof->ms_init = ms;
     }
     // one bounce: counters, closest hits, the shading passes, path ends
-    const uint32_t ogrid = std::min<uint32_t>((uint32_t)((q + 255) / 256), (uint32_t)sm_count() * 8);
     auto bounce = [&](cudaStream_t s, int k) {
       cudaMemsetAsync(&d->wf_counters->live, 0, 5 * sizeof(unsigned int), s);  // live + 4 queue lengths
       if (prof) cudaEventRecord(evs[4 * k], s);
-      if (W.order) {  // group the live slots by direction octant and origin cell
-        cudaMemsetAsync(W.order_hist, 0, (WF_KEY_BINS + 1) * sizeof(uint32_t), s);
-        wf_order_hist<<<ogrid, 256, 0, s>>>(d->view, W);
-        wf_order_scan<<<1, WF_KEY_BINS, 0, s>>>(W);
-        wf_order_scatter<<<ogrid, 256, 0, s>>>(W);
-      }
 #define CLV_ISECT(L, N, T) \
   wf_intersect<L, N, false, T><<<grid, block, 0, s>>>(d->view, W, C, d->err, N ? dcnt : nullptr, WfBatch{}, -1)
       if (spill_entries && prof && count)
@@ -1281,7 +1243,7 @@ static int render_wavefront(clv_device_scene* d, const clv_render_opts* o, doubl
       wf_finish<false><<<qgrid, block, 0, s>>>(d->view, P, W, C, film, WfBatch{});
       if (prof) cudaEventRecord(evs[4 * k + 3], s);
     };
-    const unsigned per_bounce = 4u + (guide ? (alpha > 0.0f ? 3u : 2u) : 0u) + (W.order ? 3u : 0u);
+    const unsigned per_bounce = 4u + (guide ? (alpha > 0.0f ? 3u : 2u) : 0u);
     if (guide) gd_prepare();
     // the batch of bounces between polls, replayed as one CUDA graph (profiling
     // runs launch directly: their events bracket single kernels)
@@ -1700,9 +1662,6 @@ extern "C" int clv_render_device_noalloc(clv_device_scene* d, const clv_render_o
   W.grec_cap = 0;
   W.spill = nullptr;
   W.stack_cap = CLV_STACK;
-  W.order = nullptr;
-  W.order_key = nullptr;
-  W.order_hist = nullptr;
   const int block = 128;
   const uint32_t grid = (uint32_t)((q + block - 1) / block);
   const uint32_t qgrid =

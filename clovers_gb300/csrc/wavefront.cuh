@@ -40,11 +40,6 @@ struct WfState {
   // beyond CLV_STACK of slot i at spill[(k - CLV_STACK) * Q + i], stack_cap in all
   float4* spill;
   uint32_t stack_cap;
-  // query order (null: slot order): the intersect's thread t takes slot order[t]
-  // for t < order_hist[WF_KEY_BINS] (the live slots, grouped by wf_order_key)
-  uint32_t* order;
-  uint32_t* order_key;   // key of each slot (WF_KEY_NONE: not live)
-  uint32_t* order_hist;  // WF_KEY_BINS counts -> offsets, then the live count
 };
 
 #define WF_Q_FINISH 0  // misses, emitters and paths ended in the shade kernels
@@ -122,88 +117,6 @@ __device__ __forceinline__ void wf_start_path(const ClvDeviceScene& S, const WfP
   W.meta[i] = make_uint4(pixel, 0u, rng.counter, 1u | (sid << 8));
   W.key[i] = make_uint2((uint32_t)rng.key, (uint32_t)(rng.key >> 32));
   if (W.gslot) W.gslot[i] = make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u);
-}
-
-// ---- query order --------------------------------------------------------
-// Before each intersect the live slots are grouped by a 9-bit key: the octant
-// of the direction (3 bits) and the cell of the origin in a 4x4x4 grid over
-// the scene box (6 bits, Morton order).  Lanes of a warp then trace rays that
-// start close together and head the same way, so they visit the same nodes in
-// the same order and reach leaves together (fewer idle lanes per warp
-// instruction, shared L1 lines).  A slot's own traversal is unchanged; only
-// which thread traces it moves, so hits, counts and films are unchanged.
-#define WF_KEY_BINS 512u
-#define WF_KEY_NONE 0xFFFFFFFFu
-__device__ __forceinline__ uint32_t wf_order_key(const ClvDeviceScene& S, float4 o, float4 d) {
-  uint32_t cell = 0;
-#pragma unroll
-  for (int a = 0; a < 3; ++a) {
-    const float lo = S.root_box[2 * a], hi = S.root_box[2 * a + 1];
-    const float v = a == 0 ? o.x : (a == 1 ? o.y : o.z);
-    const float c = hi > lo ? (v - lo) * (4.0f / (hi - lo)) : 0.0f;
-    const uint32_t k = c > 0.0f ? (uint32_t)fminf(c, 3.0f) : 0u;
-    cell |= ((k & 1u) << a) | ((k >> 1) << (a + 3));  // Morton order of the 2-bit coordinates
-  }
-  const uint32_t oct = (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u);
-  return (oct << 6) | cell;
-}
-// Keys and bin counts of every slot (histogram in shared memory, one global
-// atomic per non-empty bin and block).
-__global__ void __launch_bounds__(256) wf_order_hist(ClvDeviceScene S, WfState W) {
-  __shared__ uint32_t h[WF_KEY_BINS];
-  for (uint32_t b = threadIdx.x; b < WF_KEY_BINS; b += blockDim.x) h[b] = 0u;
-  __syncthreads();
-  const uint32_t stride = gridDim.x * blockDim.x;
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < W.Q; i += stride) {
-    uint32_t k = WF_KEY_NONE;
-    if (W.meta[i].w & 1u) {
-      k = wf_order_key(S, W.o_time[i], W.d_lambda[i]);
-      atomicAdd(&h[k], 1u);
-    }
-    W.order_key[i] = k;
-  }
-  __syncthreads();
-  for (uint32_t b = threadIdx.x; b < WF_KEY_BINS; b += blockDim.x)
-    if (h[b]) atomicAdd(&W.order_hist[b], h[b]);
-}
-// Exclusive scan of the bin counts (one block of WF_KEY_BINS threads); the
-// live count goes to order_hist[WF_KEY_BINS].
-__global__ void __launch_bounds__(WF_KEY_BINS) wf_order_scan(WfState W) {
-  __shared__ uint32_t warp_sum[WF_KEY_BINS / 32];
-  const uint32_t t = threadIdx.x, lane = t & 31, w = t >> 5;
-  const uint32_t v = W.order_hist[t];
-  uint32_t incl = v;
-#pragma unroll
-  for (int off = 1; off < 32; off <<= 1) {
-    const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, off);
-    if (lane >= (uint32_t)off) incl += y;
-  }
-  if (lane == 31) warp_sum[w] = incl;
-  __syncthreads();
-  uint32_t before = 0;
-  for (uint32_t k = 0; k < w; ++k) before += warp_sum[k];
-  W.order_hist[t] = before + incl - v;
-  if (t == WF_KEY_BINS - 1) W.order_hist[WF_KEY_BINS] = before + incl;
-}
-// Places every live slot in its bin's range: per block and bin one global
-// atomic reserves the block's part, ranks within it come from shared memory.
-__global__ void __launch_bounds__(256) wf_order_scatter(WfState W) {
-  __shared__ uint32_t cnt[WF_KEY_BINS], base[WF_KEY_BINS];
-  const uint32_t stride = gridDim.x * blockDim.x;
-  for (uint32_t r = blockIdx.x * blockDim.x; r < W.Q; r += stride) {  // rounds of one slot per thread
-    for (uint32_t b = threadIdx.x; b < WF_KEY_BINS; b += blockDim.x) cnt[b] = 0u;
-    __syncthreads();
-    const uint32_t i = r + threadIdx.x;
-    const uint32_t k = i < W.Q ? W.order_key[i] : WF_KEY_NONE;
-    uint32_t rank = 0;
-    if (k != WF_KEY_NONE) rank = atomicAdd(&cnt[k], 1u);
-    __syncthreads();
-    for (uint32_t b = threadIdx.x; b < WF_KEY_BINS; b += blockDim.x)
-      if (cnt[b]) base[b] = atomicAdd(&W.order_hist[b], cnt[b]);
-    __syncthreads();
-    if (k != WF_KEY_NONE) W.order[base[k] + rank] = i;
-    __syncthreads();
-  }
 }
 
 template <bool BATCH>
@@ -371,8 +284,7 @@ __device__ __forceinline__ int intersect_slot(const ClvDeviceScene& S, const WfS
 template <int CPLX, bool COUNT, bool BATCH, int WT, bool DEEP = false>
 __global__ void __launch_bounds__(128, CPLX == 1 ? CLV_MINB_CHAIN : CLV_MINB) wf_intersect(ClvDeviceScene S, WfState W, WfCounters* C, uint32_t* err,
                                                               unsigned long long* cnt, WfBatch B, int only_level) {
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (W.order) i = i < W.order_hist[WF_KEY_BINS] ? W.order[i] : 0xFFFFFFFFu;  // grouped query order
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   Counters c{0u, 0u};
   uint32_t live = 0;
   const uint4 m = i < W.Q ? W.meta[i] : make_uint4(0u, 0u, 0u, 0u);

@@ -103,7 +103,7 @@ def test_gradient_matches_oracle():
 
 
 def _scene(name):
-    _, w, h, depth, win = make_golden.WORKLOADS[name]
+    w, h, depth, win = make_golden.WORKLOADS[name][1:5]
     with tempfile.TemporaryDirectory() as tmp:
         d = cg.Scene.from_json(make_golden.scene_file(name, tmp), w, h).upload()
     return d, w, h, depth, win
