@@ -291,7 +291,121 @@ def run_batch(args):
                                    "0-3 smoke boxes, 128^2-1024^2, 16-512 spp, depth %d" % (n, DEPTH),
                        "samples_per_step": samples, "triangles": tris, "scene_load_s": round(load_s, 2)},
             "one_by_one": {"ms": round(t_seq, 3), "value": round(samples / (t_seq / 1e3) / 1e6, 3)}}
+    conv = batch_convergence(args, dev, tmp)
+    if conv:
+        line["time_to_relmse"] = conv
     print(json.dumps(line), flush=True)
+
+
+def batch_convergence(args, dev, tmp):
+    """GPU time to relMSE <= 1e-3 per scene for the batch scenes with a golden reference
+    (tests/golden/batch_ref.npz: the oracle in double precision, 65,536 spp, a stratified pixel subset):
+    progressive passes of --chunk-spp, (a) the scenes rendered together by clv_render_batch (a scene leaves
+    the batch once it has converged), (b) each scene alone by clv_render_device, (c) each scene alone with
+    the online-trained guide (clv_render_guided)."""
+    import torch
+    import clovers_gb300 as cg
+    from clovers_gb300 import _lib
+    gpath = os.path.join(ROOT, "tests", "golden", "batch_ref.npz")
+    if not os.path.exists(gpath):
+        return None
+    g = np.load(gpath)
+    L = _lib.lib()
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    ids = [int(k) for k in g["scenes"]]
+    size = {k: tuple(int(v) for v in g["s%d_size" % k]) for k in ids}
+    films = {k: torch.zeros(size[k][0] * size[k][1] * 3, dtype=torch.float64, device="cuda") for k in ids}
+    sets = {k: (torch.as_tensor(g["s%d_pixels" % k].astype(np.int64), device="cuda"), g["s%d_mean" % k]) for k in ids}
+    chunk, target = args.chunk_spp, 1e-3
+
+    def relmse(k, total_spp):
+        w, h = size[k]
+        img = (films[k].view(h * w, 3)[sets[k][0]] / total_spp).cpu().numpy()
+        ref = sets[k][1]
+        return float(np.mean((img - ref) ** 2 / (ref ** 2 + 1e-2)))
+
+    def opts(k, offset, seed):
+        w, h = size[k]
+        o = cg.render_opts(cg.RenderOptions(width=w, height=h, samples=chunk, max_depth=DEPTH, seed=seed))
+        o.sample_offset = offset
+        return o
+
+    def timed(fn):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1)
+
+    max_pass = max(1, args.max_spp // chunk)
+    seed = SEED + 3000
+    # (a) together
+    for f in films.values():
+        f.zero_()
+    todo, t, res_batch, npass = list(ids), 0.0, {}, 0
+    while todo and npass < max_pass:
+        n = len(todo)
+        handles = (ctypes.c_void_p * n)(*[dev[k].handle.value for k in todo])
+        optarr = (_lib.RenderOptsC * n)(*[opts(k, npass * chunk, seed + k) for k in todo])
+        ptrs = (ctypes.c_void_p * n)(*[films[k].data_ptr() for k in todo])
+        t += timed(lambda: _lib.check(L.clv_render_batch(handles, optarr, ptrs, n, sp)))
+        npass += 1
+        for k in list(todo):
+            e = relmse(k, npass * chunk)
+            if e <= target:
+                res_batch[k] = {"gpu_ms": round(t, 2), "spp": npass * chunk, "relmse": e}
+                todo.remove(k)
+    for k in todo:
+        res_batch[k] = {"gpu_ms": None, "spp": npass * chunk, "reached": False}
+    t_batch_all = t
+    # (b) alone, plain; (c) alone, guided
+    res_alone, res_guided = {}, {}
+    for k in ids:
+        films[k].zero_()
+        t, npass, e = 0.0, 0, None
+        while npass < max_pass:
+            o = opts(k, npass * chunk, seed + k)
+            t += timed(lambda: _lib.check(L.clv_render_device(dev[k].handle, ctypes.byref(o), films[k].data_ptr(),
+                                                              sp)))
+            npass += 1
+            e = relmse(k, npass * chunk)
+            if e <= target:
+                break
+        res_alone[k] = {"gpu_ms": round(t, 2), "spp": npass * chunk, "relmse": e, "reached": e <= target}
+        if args.guided:
+            films[k].zero_()
+            guide = cg.Guide(seed=args.guide_seed if args.guide_seed is not None else 7, learning_rate=args.guide_lr)
+            t, npass, total, e = 0.0, 0, 0, None
+            while total < args.max_spp:
+                training = npass < args.guide_passes
+                nspp = args.guide_pass_spp if training else chunk
+                w, h = size[k]
+                o = cg.render_opts(cg.RenderOptions(width=w, height=h, samples=nspp, max_depth=DEPTH, seed=seed + k))
+                o.sample_offset = total
+                alpha = 0.0 if npass == 0 else args.guide_alpha
+
+                def step():
+                    _lib.check(L.clv_render_guided(dev[k].handle, ctypes.byref(o), guide.handle, alpha,
+                                                   films[k].data_ptr(), sp))
+                    if training:
+                        _lib.check(L.clv_guide_train(guide.handle, args.guide_steps, args.guide_batch, None, sp))
+                t += timed(step)
+                npass += 1
+                total += nspp
+                e = relmse(k, total)
+                if e <= target:
+                    break
+            res_guided[k] = {"gpu_ms": round(t, 2), "spp": total, "relmse": e, "reached": e <= target}
+    out = {"target": target, "reference": "oracle (f64), 65536 spp, stratified pixel subsets (tests/golden/batch_ref.npz)",
+           "pass_spp": chunk, "scenes": ids, "batched": {str(k): v for k, v in res_batch.items()},
+           "batched_total_ms": round(t_batch_all, 2), "alone": {str(k): v for k, v in res_alone.items()},
+           "alone_total_ms": round(sum(v["gpu_ms"] for v in res_alone.values()), 2)}
+    if res_guided:
+        out["guided_alone"] = {str(k): v for k, v in res_guided.items()}
+        out["guided_alone_total_ms"] = round(sum(v["gpu_ms"] for v in res_guided.values()), 2)
+    return out
 
 
 def run_config(args):

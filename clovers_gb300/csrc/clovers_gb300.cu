@@ -386,6 +386,107 @@ void ck(cudaError_t e, const char* what) {
   if (e != cudaSuccess) throw CudaError(std::string(what) + ": " + cudaGetErrorString(e));
 }
 
+// Blocks of device memory, pinned words and streams that destroyed device
+// scenes release are kept for the next scene on the same device: a host that
+// uploads its scene for every frame would otherwise pay cudaMalloc / cudaFree
+// of the path state (about 190 MB) every frame, and cudaFree synchronises the
+// device.  A released block is reused for a request of at least half its size;
+// at most kPoolBlocks blocks are kept, larger surpluses are freed.
+namespace pool {
+struct Block {
+  int dev;
+  void* p;
+  size_t bytes;
+};
+static std::mutex mu;
+static std::vector<Block> blocks;
+static std::vector<std::pair<int, cudaStream_t>> streams;
+static std::vector<unsigned int*> pinned;
+static constexpr size_t kPoolBlocks = 8;
+static int device() {
+  int d = 0;
+  cudaGetDevice(&d);
+  return d;
+}
+// Device memory of at least `bytes`; *got receives the size of the block.
+static void* alloc(size_t bytes, size_t* got, const char* what) {
+  const int dev = device();
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    size_t best = blocks.size();
+    for (size_t k = 0; k < blocks.size(); ++k)
+      if (blocks[k].dev == dev && blocks[k].bytes >= bytes && blocks[k].bytes / 2 <= bytes &&
+          (best == blocks.size() || blocks[k].bytes < blocks[best].bytes))
+        best = k;
+    if (best < blocks.size()) {
+      const Block b = blocks[best];
+      blocks.erase(blocks.begin() + (std::ptrdiff_t)best);
+      *got = b.bytes;
+      return b.p;
+    }
+  }
+  void* p = nullptr;
+  ck(cudaMalloc(&p, bytes), what);
+  *got = bytes;
+  return p;
+}
+// Hands a block back (the device is synchronised first: the releasing scene's
+// kernels may still be running on a stream the library does not know).
+static void release(void* p, size_t bytes) {
+  if (!p) return;
+  cudaDeviceSynchronize();
+  cudaGetLastError();
+  std::lock_guard<std::mutex> lock(mu);
+  blocks.push_back(Block{device(), p, bytes});
+  if (blocks.size() > kPoolBlocks) {  // free the oldest
+    cudaFree(blocks.front().p);
+    blocks.erase(blocks.begin());
+  }
+}
+static cudaStream_t stream() {
+  const int dev = device();
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    for (size_t k = 0; k < streams.size(); ++k)
+      if (streams[k].first == dev) {
+        const cudaStream_t st = streams[k].second;
+        streams.erase(streams.begin() + (std::ptrdiff_t)k);
+        return st;
+      }
+  }
+  cudaStream_t st = nullptr;
+  if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return st;
+}
+static void release_stream(cudaStream_t st) {
+  if (!st) return;
+  std::lock_guard<std::mutex> lock(mu);
+  if (streams.size() < kPoolBlocks) streams.emplace_back(device(), st);
+  else cudaStreamDestroy(st);
+}
+static unsigned int* pinned_word() {
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    if (!pinned.empty()) {
+      unsigned int* w = pinned.back();
+      pinned.pop_back();
+      return w;
+    }
+  }
+  unsigned int* w = nullptr;
+  ck(cudaMallocHost(&w, sizeof(unsigned int)), "cudaMallocHost");
+  return w;
+}
+static void release_pinned(unsigned int* w) {
+  if (!w) return;
+  std::lock_guard<std::mutex> lock(mu);
+  pinned.push_back(w);
+}
+}  // namespace pool
+
 // A scene's device arrays in one allocation: `add` records each array at a
 // 256-byte aligned offset, `commit` allocates once and copies every array
 // straight from its host vector, with one synchronisation at the end.
@@ -409,9 +510,8 @@ struct UploadPack {
     total += (bytes + 255) / 256 * 256;
     return off;
   }
-  char* commit(std::vector<void*>& owned) {
-    void* base = nullptr;
-    ck(cudaMalloc(&base, std::max<size_t>(total, 256)), "cudaMalloc scene");
+  char* commit(std::vector<void*>& owned, size_t* owned_bytes) {
+    void* base = pool::alloc(std::max<size_t>(total, 256), owned_bytes, "cudaMalloc scene");
     owned.push_back(base);
     char* b = static_cast<char*>(base);
     for (const Item& it : items) {
@@ -503,6 +603,7 @@ static uint32_t compound_level(const clv::HostScene& h) {
   return level;
 }
 
+
 struct clv_device_scene {
   ClvDeviceScene view{};
   std::vector<void*> owned;
@@ -514,6 +615,7 @@ struct clv_device_scene {
   size_t scratch_bytes = 0;
   // wavefront path state, sized on first use
   void* wf_mem = nullptr;
+  size_t wf_bytes = 0;
   uint32_t wf_slots = 0;
   WfCounters* wf_counters = nullptr;
   unsigned int* wf_live_host = nullptr;  // pinned
@@ -524,15 +626,16 @@ struct clv_device_scene {
   unsigned long long* ray_next = nullptr;  // work counter of the persistent ray casts
   uint32_t* ray_sort = nullptr;            // ray order: histogram, keys, permutation
   uint64_t ray_sort_cap = 0;               // rays the sort scratch holds
+  size_t ray_sort_bytes = 0;
+  size_t owned_bytes = 0;                  // the scene arrays' block (owned[0])
   float4* spill = nullptr;   // traversal stack spill of trees deeper than CLV_STACK levels
   size_t spill_bytes = 0;
   float4* spill_region(size_t bytes) {
     if (bytes > spill_bytes) {
-      if (spill) cudaFree(spill);
+      pool::release(spill, spill_bytes);
       spill = nullptr;
       spill_bytes = 0;
-      ck(cudaMalloc(&spill, bytes), "cudaMalloc stack spill");
-      spill_bytes = bytes;
+      spill = static_cast<float4*>(pool::alloc(bytes, &spill_bytes, "cudaMalloc stack spill"));
     }
     return spill;
   }
@@ -541,41 +644,41 @@ struct clv_device_scene {
   uint32_t spill_entries() const { return deep() ? view.max_depth_tree - CLV_STACK : 0u; }
   uint32_t* ray_sort_scratch(uint64_t n) {
     if (n > ray_sort_cap) {
-      if (ray_sort) cudaFree(ray_sort);
+      pool::release(ray_sort, ray_sort_bytes);
       ray_sort = nullptr;
       ray_sort_cap = 0;
-      ck(cudaMalloc(&ray_sort, (CLV_SORT_BINS + 2 * n) * sizeof(uint32_t)), "cudaMalloc ray order");
+      ray_sort = static_cast<uint32_t*>(
+          pool::alloc((CLV_SORT_BINS + 2 * n) * sizeof(uint32_t), &ray_sort_bytes, "cudaMalloc ray order"));
       ray_sort_cap = n;
     }
     return ray_sort;
   }
   cudaStream_t capture_stream() {
-    if (!cap_stream && cudaStreamCreateWithFlags(&cap_stream, cudaStreamNonBlocking) != cudaSuccess) {
-      cudaGetLastError();
-      cap_stream = nullptr;
-    }
+    if (!cap_stream) cap_stream = pool::stream();
     return cap_stream;
   }
+  size_t counters_bytes = 0;
   ~clv_device_scene() {
-    if (cap_stream) cudaStreamDestroy(cap_stream);
-    if (ray_sort) cudaFree(ray_sort);
-    if (spill) cudaFree(spill);
-    for (void* p : owned) cudaFree(p);  // scene arrays, error word and ray counter
-    if (scratch) cudaFree(scratch);
-    if (wf_mem) cudaFree(wf_mem);
-    if (wf_counters) cudaFree(wf_counters);
-    if (wf_live_host) cudaFreeHost(wf_live_host);
+    pool::release_stream(cap_stream);
+    pool::release(ray_sort, ray_sort_bytes);
+    pool::release(spill, spill_bytes);
+    if (!owned.empty()) pool::release(owned[0], owned_bytes);  // scene arrays, error word and ray counter
+    pool::release(scratch, scratch_bytes);
+    pool::release(wf_mem, wf_bytes);
+    pool::release(wf_counters, counters_bytes);
+    pool::release_pinned(wf_live_host);
   }
   WfState wavefront_state(uint32_t q) {
     if (q > wf_slots) {
-      if (wf_mem) cudaFree(wf_mem);
+      pool::release(wf_mem, wf_bytes);
       wf_mem = nullptr;
       wf_slots = 0;
-      ck(cudaMalloc(&wf_mem, (size_t)q * kWfSlotBytes), "cudaMalloc path state");
+      wf_mem = pool::alloc((size_t)q * kWfSlotBytes, &wf_bytes, "cudaMalloc path state");
       wf_slots = q;
     }
-    if (!wf_counters) ck(cudaMalloc(&wf_counters, sizeof(WfCounters)), "cudaMalloc");
-    if (!wf_live_host) ck(cudaMallocHost(&wf_live_host, sizeof(unsigned int)), "cudaMallocHost");
+    if (!wf_counters)
+      wf_counters = static_cast<WfCounters*>(pool::alloc(sizeof(WfCounters), &counters_bytes, "cudaMalloc"));
+    if (!wf_live_host) wf_live_host = pool::pinned_word();
     char* p = static_cast<char*>(wf_mem);
     const size_t n = wf_slots;
     WfState W;
@@ -599,11 +702,10 @@ struct clv_device_scene {
   static constexpr size_t kWfSlotBytes = 16 * 5 + 48 + 8 + 16;
   void* ensure_scratch(size_t bytes) {
     if (bytes > scratch_bytes) {
-      if (scratch) cudaFree(scratch);
+      pool::release(scratch, scratch_bytes);
       scratch = nullptr;
       scratch_bytes = 0;
-      ck(cudaMalloc(&scratch, bytes), "cudaMalloc scratch");
-      scratch_bytes = bytes;
+      scratch = pool::alloc(bytes, &scratch_bytes, "cudaMalloc scratch");
     }
     return scratch;
   }
@@ -972,7 +1074,7 @@ int clv_scene_upload(const clv_scene* s, clv_device_scene** out) {
     v.tri_verts = nullptr;
     if (s->watertight && !h.tri_verts.empty()) pk.add(h.tri_verts, &v.tri_verts);
     const size_t off_err = pk.reserve(sizeof(uint32_t)), off_next = pk.reserve(sizeof(unsigned long long));
-    char* base = pk.commit(d->owned);
+    char* base = pk.commit(d->owned, &d->owned_bytes);
     d->err = reinterpret_cast<uint32_t*>(base + off_err);
     d->ray_next = reinterpret_cast<unsigned long long*>(base + off_next);
     v.root = h.root;
@@ -1309,15 +1411,27 @@ int clv_render_batch(clv_device_scene* const* ds, const clv_render_opts* opts, d
   cudaStream_t st = (cudaStream_t)stream;
   void* dmem = nullptr;
   try {
+    // The work items are laid out scene after scene, the scenes ordered by the
+    // traversal level they need (a stable sort), so that for most of the render
+    // the live paths belong to one level and the other levels' intersect
+    // launches find next to nothing to do.  Films and random streams stay with
+    // their scenes.
+    std::vector<uint32_t> order(n);
+    for (uint32_t k = 0; k < n; ++k) order[k] = k;
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) {
+      return ds[a]->view.compound_level < ds[b]->view.compound_level;
+    });
     std::vector<ClvDeviceScene> views(n);
     std::vector<WfParams> params(n);
     std::vector<unsigned long long> prefix(n + 1, 0ull);
-    std::vector<double*> fl(films, films + n);
+    std::vector<double*> fl(n);
     uint32_t levels = 0;  // bit L: some scene needs traversal level L
-    for (uint32_t k = 0; k < n; ++k) {
-      views[k] = ds[k]->view;
+    for (uint32_t j = 0; j < n; ++j) {
+      const uint32_t k = order[j];
+      views[j] = ds[k]->view;
+      fl[j] = films[k];
       const clv_render_opts& o = opts[k];
-      WfParams& P = params[k];
+      WfParams& P = params[j];
       P.width = o.width;
       P.height = o.height;
       P.max_depth = o.max_depth;
@@ -1325,7 +1439,7 @@ int clv_render_batch(clv_device_scene* const* ds, const clv_render_opts* opts, d
       P.npix = (uint64_t)o.width * o.height;
       P.total = P.npix * o.samples;
       P.seed = o.seed;
-      prefix[k + 1] = prefix[k] + P.total;
+      prefix[j + 1] = prefix[j] + P.total;
       levels |= 1u << ds[k]->view.compound_level;
     }
     const int nlevels = __builtin_popcount(levels);

@@ -193,6 +193,45 @@ __device__ __forceinline__ void encode_col(unsigned char* tile, uint32_t col, co
   st_bf16(tile + gd_cofs(175, col, GD_TILE), 1.0f);
 }
 
+// Part of a row of the encoded-input tile: the features of inputs [J0, J1)
+// and, with RAW, the raw inputs and the constant 1 (columns 168..175).  Two
+// threads share a row in the training kernel, one part each.
+template <int J0, int J1, bool RAW>
+__device__ __forceinline__ void encode_row_part(unsigned char* tile, uint32_t row, const float u[7]) {
+#pragma unroll
+  for (int j = J0; j < J1; ++j) {
+    float v[24];
+    freq_row(u[j], v);
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch) {
+      const uint4 w = make_uint4(pack_bf16(v[8 * ch], v[8 * ch + 1]), pack_bf16(v[8 * ch + 2], v[8 * ch + 3]),
+                                 pack_bf16(v[8 * ch + 4], v[8 * ch + 5]), pack_bf16(v[8 * ch + 6], v[8 * ch + 7]));
+      *reinterpret_cast<uint4*>(tile + gd_cofs(row, 24 * j + 8 * ch, GD_IN)) = w;
+    }
+  }
+  if (RAW) {
+    const uint4 w = make_uint4(pack_bf16(u[0], u[1]), pack_bf16(u[2], u[3]), pack_bf16(u[4], u[5]),
+                               pack_bf16(u[6], 1.0f));
+    *reinterpret_cast<uint4*>(tile + gd_cofs(row, 168, GD_IN)) = w;
+  }
+}
+// The same part of column `col` of the transposed tile.
+template <int J0, int J1, bool RAW>
+__device__ __forceinline__ void encode_col_part(unsigned char* tile, uint32_t col, const float u[7]) {
+#pragma unroll
+  for (int j = J0; j < J1; ++j) {
+    float v[24];
+    freq_row(u[j], v);
+#pragma unroll
+    for (int e = 0; e < 24; ++e) st_bf16(tile + gd_cofs(24 * j + e, col, GD_TILE), v[e]);
+  }
+  if (RAW) {
+#pragma unroll
+    for (int j = 0; j < 7; ++j) st_bf16(tile + gd_cofs(168 + j, col, GD_TILE), u[j]);
+    st_bf16(tile + gd_cofs(175, col, GD_TILE), 1.0f);
+  }
+}
+
 // ---------------------------------------------------------------- vMF head --
 struct Mix {
   float mu[GD_LOBES][3];
@@ -370,8 +409,69 @@ __device__ __forceinline__ uint64_t hidden_epilogue(uint32_t trow, unsigned char
   return mask;
 }
 
+// Half of hidden_epilogue: columns [C0, C0 + 32) of this thread's row; the
+// returned mask holds bit u - C0 for each unit u > 0.
+template <int C0, bool TT = true>
+__device__ __forceinline__ uint32_t hidden_epilogue_half(uint32_t trow, unsigned char* a_tile, unsigned char* t_tile,
+                                                         uint32_t row) {
+  uint32_t mask = 0;
+#pragma unroll
+  for (int cc = 0; cc < 2; ++cc) {
+    const int c = C0 / 16 + cc;
+    float v[16];
+    tmem_ld16(trow + 16u * c, v);
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+      float h = fmaxf(v[i], 0.0f);
+      if (16 * c + i == GD_H - 1) h = 1.0f;
+      v[i] = h;
+      if (h > 0.0f) mask |= 1u << (16 * cc + i);
+    }
+#pragma unroll
+    for (int hh = 0; hh < 2; ++hh) {
+      const float* p = v + 8 * hh;
+      *reinterpret_cast<uint4*>(a_tile + gd_cofs(row, 16 * c + 8 * hh, GD_H)) =
+          make_uint4(pack_bf16(p[0], p[1]), pack_bf16(p[2], p[3]), pack_bf16(p[4], p[5]), pack_bf16(p[6], p[7]));
+    }
+    if (TT) {
+#pragma unroll
+      for (int i = 0; i < 16; ++i) st_bf16(t_tile + gd_cofs(16 * c + i, row, GD_TILE), v[i]);
+    }
+  }
+  return mask;
+}
+// Half of backward_epilogue over the same columns (mask from hidden_epilogue_half).
+template <int C0>
+__device__ __forceinline__ void backward_epilogue_half(uint32_t trow, uint32_t mask, unsigned char* a_tile,
+                                                       unsigned char* t_tile, uint32_t row) {
+#pragma unroll
+  for (int cc = 0; cc < 2; ++cc) {
+    const int c = C0 / 16 + cc;
+    float v[16];
+    tmem_ld16(trow + 16u * c, v);
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+      const int unit = 16 * c + i;
+      v[i] = (unit != GD_H - 1 && ((mask >> (16 * cc + i)) & 1u)) ? v[i] : 0.0f;
+    }
+    if (a_tile) {
+#pragma unroll
+      for (int hh = 0; hh < 2; ++hh) {
+        const float* p = v + 8 * hh;
+        *reinterpret_cast<uint4*>(a_tile + gd_cofs(row, 16 * c + 8 * hh, GD_H)) =
+            make_uint4(pack_bf16(p[0], p[1]), pack_bf16(p[2], p[3]), pack_bf16(p[4], p[5]), pack_bf16(p[6], p[7]));
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < 16; ++i) st_bf16(t_tile + gd_cofs(16 * c + i, row, GD_TILE), v[i]);
+  }
+}
+
+// Eight warps: warps w and w + 4 read the same TMEM lanes, so every query of
+// a tile has two threads, which split its encoding and its hidden-layer
+// epilogues; the first of the two evaluates the vMF head (and draws from it).
 template <int SRC>
-__global__ void __launch_bounds__(128) guide_infer_kernel(GuideDev G, GdQueue Q, ArrayIO A) {
+__global__ void __launch_bounds__(256) guide_infer_kernel(GuideDev G, GdQueue Q, ArrayIO A) {
   extern __shared__ __align__(1024) unsigned char smem[];
   unsigned char* sw = smem;
   unsigned char* sx = smem + GD_B_FWD;
@@ -379,6 +479,8 @@ __global__ void __launch_bounds__(128) guide_infer_kernel(GuideDev G, GdQueue Q,
   uint64_t* bars = reinterpret_cast<uint64_t*>(sh + GD_TILE * GD_H * 2);
   uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 2);
   const uint32_t tid = threadIdx.x, warp = tid >> 5;
+  const uint32_t quad = warp & 3u, half = warp >> 2;
+  const uint32_t row = quad * 32u + (tid & 31u);
   const uint32_t n = SRC == SRC_QUEUE ? *Q.count : A.n;
   const uint32_t ntiles = (n + GD_TILE - 1) / GD_TILE;
   if (blockIdx.x >= ntiles) return;  // uniform over the CTA
@@ -396,17 +498,16 @@ __global__ void __launch_bounds__(128) guide_infer_kernel(GuideDev G, GdQueue Q,
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tslot;
-  const uint32_t trow = tmem + ((warp * 32u) << 16);
+  const uint32_t trow = tmem + ((quad * 32u) << 16);
   if (tid == 0) bulk_load(sw, G.wblob, GD_B_FWD, bw);
   bool ok = __syncthreads_and(mbar_wait(bw, 0)) != 0;
   uint32_t phase = 0;
   const uint32_t a_x = smem_u32(sx), a_h = smem_u32(sh), b_w = smem_u32(sw);
   for (uint32_t tile = blockIdx.x; ok && tile < ntiles; tile += gridDim.x) {
-    const uint32_t qi = tile * GD_TILE + tid;
+    const uint32_t qi = tile * GD_TILE + row;
     const bool valid = qi < n;
     float u[7] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
     uint32_t slot = 0;
-    float4 hv = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     if (valid) {
       if (SRC == SRC_QUEUE) {
         slot = Q.queue[qi];
@@ -419,50 +520,56 @@ __global__ void __launch_bounds__(128) guide_infer_kernel(GuideDev G, GdQueue Q,
         u[4] = sat(0.5f - 0.5f * dl.y);
         u[5] = sat(0.5f - 0.5f * dl.z);
         u[6] = ((float)__float_as_int(dl.w) - 380.0f) * 0.0025f;
-        hv = Q.hit[slot];
       } else {
         const float4 a = A.in[2 * qi], b = A.in[2 * qi + 1];
         u[0] = a.x; u[1] = a.y; u[2] = a.z; u[3] = a.w;
         u[4] = b.x; u[5] = b.y; u[6] = b.z;
       }
     }
-    encode_row(sx, tid, u);
+    if (half == 0) encode_row_part<0, 4, false>(sx, row, u);
+    else encode_row_part<4, 7, true>(sx, row, u);
     ok = run_mma(bm, phase, [&] { mma_gemm(tmem, a_x, b_w + GD_B_W1, GD_IN, GD_H, false); });
     if (!ok) break;
-    hidden_epilogue(trow, sh, nullptr, tid);
+    if (half == 0) hidden_epilogue_half<0, false>(trow, sh, nullptr, row);
+    else hidden_epilogue_half<32, false>(trow, sh, nullptr, row);
     ok = run_mma(bm, phase, [&] { mma_gemm(tmem, a_h, b_w + GD_B_W2, GD_H, GD_H, false); });
     if (!ok) break;
-    hidden_epilogue(trow, sh, nullptr, tid);
+    if (half == 0) hidden_epilogue_half<0, false>(trow, sh, nullptr, row);
+    else hidden_epilogue_half<32, false>(trow, sh, nullptr, row);
     ok = run_mma(bm, phase, [&] { mma_gemm(tmem, a_h, b_w + GD_B_W3, GD_H, GD_H, false); });
     if (!ok) break;
-    hidden_epilogue(trow, sh, nullptr, tid);
+    if (half == 0) hidden_epilogue_half<0, false>(trow, sh, nullptr, row);
+    else hidden_epilogue_half<32, false>(trow, sh, nullptr, row);
     ok = run_mma(bm, phase, [&] { mma_gemm(tmem, a_h, b_w + GD_B_W4, GD_H, GD_OUTP, false); });
     if (!ok) break;
-    float o[GD_OUTP];
-    tmem_ld16(trow, o);
-    tmem_ld16(trow + 16u, o + 16);
-    tmem_ld16(trow + 32u, o + 32);
-    tc_fence_before();  // the next tile's MMAs overwrite these columns after a barrier
-    if (valid) {
-      if (SRC == SRC_ARRAY) {
+    if (half == 0) {
+      float o[GD_OUTP];
+      tmem_ld16(trow, o);
+      tmem_ld16(trow + 16u, o + 16);
+      tmem_ld16(trow + 32u, o + 32);
+      tc_fence_before();  // the next tile's MMAs overwrite these columns after a barrier
+      if (valid) {
+        if (SRC == SRC_ARRAY) {
 #pragma unroll
-        for (int i = 0; i < GD_OUT; ++i) A.out[(size_t)GD_OUT * qi + i] = o[i];
-      } else {
-        Mix m;
-        make_mix(o, m);
-        float x = hv.x, y = hv.y, z = hv.z;
-        if (hv.w != 0.0f) {  // this bounce samples the guide
-          const uint2 k = Q.key[slot];
-          clvd::Rng rng;
-          rng.key = (uint64_t)k.x | ((uint64_t)k.y << 32);
-          rng.counter = Q.meta[slot].z;
-          const float u0 = rng.f32(), u1 = rng.f32(), u2 = rng.f32();
-          mix_sample(m, u0, u1, u2, x, y, z);
-          Q.meta[slot].z = rng.counter;
+          for (int i = 0; i < GD_OUT; ++i) A.out[(size_t)GD_OUT * qi + i] = o[i];
+        } else {
+          Mix m;
+          make_mix(o, m);
+          const float4 hv = Q.hit[slot];
+          float x = hv.x, y = hv.y, z = hv.z;
+          if (hv.w != 0.0f) {  // this bounce samples the guide
+            const uint2 k = Q.key[slot];
+            clvd::Rng rng;
+            rng.key = (uint64_t)k.x | ((uint64_t)k.y << 32);
+            rng.counter = Q.meta[slot].z;
+            const float u0 = rng.f32(), u1 = rng.f32(), u2 = rng.f32();
+            mix_sample(m, u0, u1, u2, x, y, z);
+            Q.meta[slot].z = rng.counter;
+          }
+          float v[GD_LOBES];
+          const float q = mix_pdf(m, x, y, z, v);
+          Q.hit[slot] = make_float4(x, y, z, q);
         }
-        float v[GD_LOBES];
-        const float q = mix_pdf(m, x, y, z, v);
-        Q.hit[slot] = make_float4(x, y, z, q);
       }
     }
   }
@@ -529,8 +636,12 @@ __device__ __forceinline__ void backward_epilogue(uint32_t trow, uint64_t mask, 
 }
 
 // Adds the loss gradient of records [0, n) (GD_REC_F4 float4 each) into
-// grad (sums, fp32) and the loss sum into *loss.
-__global__ void __launch_bounds__(128, 1) guide_train_kernel(const unsigned char* __restrict__ wblob,
+// grad (sums, fp32) and the loss sum into *loss.  Eight warps: warps w and
+// w + 4 read the same TMEM lanes (rows 32 (w mod 4) ..), so every row of a
+// tile has two threads, which split its encoding (inputs 0-3 | 4-6 and the
+// raw inputs) and its hidden-layer epilogues (units 0-31 | 32-63); the
+// first of the two evaluates the vMF head and its gradient.
+__global__ void __launch_bounds__(256, 1) guide_train_kernel(const unsigned char* __restrict__ wblob,
                                                              const float4* __restrict__ rec, uint32_t n,
                                                              float* __restrict__ grad, double* __restrict__ loss,
                                                              uint32_t* err) {
@@ -542,7 +653,9 @@ __global__ void __launch_bounds__(128, 1) guide_train_kernel(const unsigned char
   unsigned char* sht = smem + GT_HT;
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + GT_BAR);
   uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 2);
-  const uint32_t tid = threadIdx.x, warp = tid >> 5;
+  const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t quad = warp & 3u, half = warp >> 2;
+  const uint32_t row = quad * 32u + lane;  // tile row (record) of this thread
   const uint32_t ntiles = (n + GD_TILE - 1) / GD_TILE;
   if (blockIdx.x >= ntiles) return;
   const uint32_t bw = smem_u32(&bars[0]), bm = smem_u32(&bars[1]);
@@ -559,7 +672,7 @@ __global__ void __launch_bounds__(128, 1) guide_train_kernel(const unsigned char
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tslot;
-  const uint32_t trow = tmem + ((warp * 32u) << 16);
+  const uint32_t trow = tmem + ((quad * 32u) << 16);
   if (tid == 0) bulk_load(sw, wblob, GD_B_ALL, bw);
   bool ok = __syncthreads_and(mbar_wait(bw, 0)) != 0;
   uint32_t phase = 0;
@@ -568,72 +681,86 @@ __global__ void __launch_bounds__(128, 1) guide_train_kernel(const unsigned char
   bool first = true;
   double lsum = 0.0;
   for (uint32_t tile = blockIdx.x; ok && tile < ntiles; tile += gridDim.x) {
-    const uint32_t r = tile * GD_TILE + tid;
+    const uint32_t r = tile * GD_TILE + row;
     float u[7] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
     float wx = 0.0f, wy = 0.0f, wz = 1.0f, f = 0.0f;
     if (r < n) {
       const float4 a = rec[GD_REC_F4 * (size_t)r], b = rec[GD_REC_F4 * (size_t)r + 1];
-      const float4 c = rec[GD_REC_F4 * (size_t)r + 2];
       u[0] = a.x; u[1] = a.y; u[2] = a.z; u[3] = a.w;
       u[4] = b.x; u[5] = b.y; u[6] = b.z;
-      wx = c.x; wy = c.y; wz = c.z;
-      f = (c.w > 0.0f && c.w < 3.0e38f) ? c.w : 0.0f;
+      if (half == 0) {
+        const float4 c = rec[GD_REC_F4 * (size_t)r + 2];
+        wx = c.x; wy = c.y; wz = c.z;
+        f = (c.w > 0.0f && c.w < 3.0e38f) ? c.w : 0.0f;
+      }
     }
     // forward
-    encode_row(sx, tid, u);
+    if (half == 0) encode_row_part<0, 4, false>(sx, row, u);
+    else encode_row_part<4, 7, true>(sx, row, u);
     ok = run_mma(bm, phase, [&] { mma_gemm(tmem + GT_DF, a_x, b_w + GD_B_W1, GD_IN, GD_H, false); });
     if (!ok) break;
-    const uint64_t m1 = hidden_epilogue(trow + GT_DF, sa, sht, tid);
+    uint32_t m1, m2, m3;
+    if (half == 0) m1 = hidden_epilogue_half<0>(trow + GT_DF, sa, sht, row);
+    else m1 = hidden_epilogue_half<32>(trow + GT_DF, sa, sht, row);
     ok = run_mma(bm, phase, [&] { mma_gemm(tmem + GT_DF, a_a, b_w + GD_B_W2, GD_H, GD_H, false); });
     if (!ok) break;
-    const uint64_t m2 = hidden_epilogue(trow + GT_DF, sa, sht + GT_HT_BYTES, tid);
+    if (half == 0) m2 = hidden_epilogue_half<0>(trow + GT_DF, sa, sht + GT_HT_BYTES, row);
+    else m2 = hidden_epilogue_half<32>(trow + GT_DF, sa, sht + GT_HT_BYTES, row);
     ok = run_mma(bm, phase, [&] { mma_gemm(tmem + GT_DF, a_a, b_w + GD_B_W3, GD_H, GD_H, false); });
     if (!ok) break;
-    const uint64_t m3 = hidden_epilogue(trow + GT_DF, sa, sht + 2 * GT_HT_BYTES, tid);
+    if (half == 0) m3 = hidden_epilogue_half<0>(trow + GT_DF, sa, sht + 2 * GT_HT_BYTES, row);
+    else m3 = hidden_epilogue_half<32>(trow + GT_DF, sa, sht + 2 * GT_HT_BYTES, row);
     ok = run_mma(bm, phase, [&] { mma_gemm(tmem + GT_DF, a_a, b_w + GD_B_W4, GD_H, GD_OUTP, false); });
     if (!ok) break;
-    float o[GD_OUTP];
-    tmem_ld16(trow + GT_DF, o);
-    tmem_ld16(trow + GT_DF + 16u, o + 16);
-    tmem_ld16(trow + GT_DF + 32u, o + 32);
-    // loss gradient of the head
-    float d[GD_OUTP];
+    if (half == 0) {
+      float o[GD_OUTP];
+      tmem_ld16(trow + GT_DF, o);
+      tmem_ld16(trow + GT_DF + 16u, o + 16);
+      tmem_ld16(trow + GT_DF + 32u, o + 32);
+      // loss gradient of the head
+      float d[GD_OUTP];
 #pragma unroll
-    for (int i = 0; i < GD_OUTP; ++i) d[i] = 0.0f;
-    if (f > 0.0f) {
-      Mix m;
-      make_mix(o, m);
-      lsum += (double)mix_grad(m, wx, wy, wz, f, d);
+      for (int i = 0; i < GD_OUTP; ++i) d[i] = 0.0f;
+      if (f > 0.0f) {
+        Mix m;
+        make_mix(o, m);
+        lsum += (double)mix_grad(m, wx, wy, wz, f, d);
+      }
+#pragma unroll
+      for (int c = 0; c < GD_OUTP / 8; ++c)
+        *reinterpret_cast<uint4*>(sa + gd_cofs(row, 8 * c, GD_OUTP)) =
+            make_uint4(pack_bf16(d[8 * c], d[8 * c + 1]), pack_bf16(d[8 * c + 2], d[8 * c + 3]),
+                       pack_bf16(d[8 * c + 4], d[8 * c + 5]), pack_bf16(d[8 * c + 6], d[8 * c + 7]));
+#pragma unroll
+      for (int i = 0; i < GD_OUTP; ++i) st_bf16(szt + gd_cofs(i, row, GD_TILE), d[i]);
     }
-#pragma unroll
-    for (int c = 0; c < GD_OUTP / 8; ++c)
-      *reinterpret_cast<uint4*>(sa + gd_cofs(tid, 8 * c, GD_OUTP)) =
-          make_uint4(pack_bf16(d[8 * c], d[8 * c + 1]), pack_bf16(d[8 * c + 2], d[8 * c + 3]),
-                     pack_bf16(d[8 * c + 4], d[8 * c + 5]), pack_bf16(d[8 * c + 6], d[8 * c + 7]));
-#pragma unroll
-    for (int i = 0; i < GD_OUTP; ++i) st_bf16(szt + gd_cofs(i, tid, GD_TILE), d[i]);
     // dH3 = dO W4 ; dW4 += dO^T H3
     ok = run_mma(bm, phase, [&] {
       mma_gemm(tmem + GT_DB, a_a, b_w + GD_B_W4T, GD_OUTP, GD_H, false);
       mma_gemm(tmem + GT_DW4, a_zt, a_ht + 2 * GT_HT_BYTES, GD_TILE, GD_H, !first);
     });
     if (!ok) break;
-    backward_epilogue(trow + GT_DB, m3, sa, szt, tid);
+    if (half == 0) backward_epilogue_half<0>(trow + GT_DB, m3, sa, szt, row);
+    else backward_epilogue_half<32>(trow + GT_DB, m3, sa, szt, row);
     // dH2 = dZ3 W3 ; dW3 += dZ3^T H2
     ok = run_mma(bm, phase, [&] {
       mma_gemm(tmem + GT_DB, a_a, b_w + GD_B_W3T, GD_H, GD_H, false);
       mma_gemm(tmem + GT_DW3, a_zt, a_ht + GT_HT_BYTES, GD_TILE, GD_H, !first);
     });
     if (!ok) break;
-    backward_epilogue(trow + GT_DB, m2, sa, szt, tid);
+    if (half == 0) backward_epilogue_half<0>(trow + GT_DB, m2, sa, szt, row);
+    else backward_epilogue_half<32>(trow + GT_DB, m2, sa, szt, row);
     // dH1 = dZ2 W2 ; dW2 += dZ2^T H1
     ok = run_mma(bm, phase, [&] {
       mma_gemm(tmem + GT_DB, a_a, b_w + GD_B_W2T, GD_H, GD_H, false);
       mma_gemm(tmem + GT_DW2, a_zt, a_ht, GD_TILE, GD_H, !first);
     });
     if (!ok) break;
-    backward_epilogue(trow + GT_DB, m1, nullptr, szt, tid);
-    encode_col(sx, tid, u);  // X^T replaces X, whose last reader has completed
+    if (half == 0) backward_epilogue_half<0>(trow + GT_DB, m1, nullptr, szt, row);
+    else backward_epilogue_half<32>(trow + GT_DB, m1, nullptr, szt, row);
+    // X^T replaces X, whose last reader has completed
+    if (half == 0) encode_col_part<0, 4, false>(sx, row, u);
+    else encode_col_part<4, 7, true>(sx, row, u);
     // dW1 += dZ1^T X
     ok = run_mma(bm, phase, [&] { mma_gemm(tmem + GT_DW1, a_zt, a_x, GD_TILE, GD_IN, !first); });
     if (!ok) break;
@@ -642,29 +769,30 @@ __global__ void __launch_bounds__(128, 1) guide_train_kernel(const unsigned char
   // loss sum
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) lsum += __shfl_down_sync(0xFFFFFFFFu, lsum, off);
-  if ((tid & 31) == 0 && lsum != 0.0) atomicAdd(loss, lsum);
-  // weight gradients: lanes 0..63 (warps 0, 1) hold rows out = lane
-  if (ok && !first && warp < 2) {
-    const uint32_t row = tid;
+  if (lane == 0 && lsum != 0.0) atomicAdd(loss, lsum);
+  // weight gradients: TMEM lanes 0..63 (quads 0 and 1) hold rows out = row; the two
+  // warps of a quad split the columns; vector (float4) reductions into grad
+  if (ok && !first && quad < 2) {
     float v[16];
+    auto flush = [&](uint32_t tcol, float* dst) {
+      tmem_ld16(trow + tcol, v);
+#pragma unroll
+      for (int i = 0; i < 16; i += 4)
+        atomicAdd(reinterpret_cast<float4*>(dst + i), make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]));
+    };
+    const uint32_t c1a = half == 0 ? 0u : 6u, c1b = half == 0 ? 6u : GD_IN / 16;  // dW1: chunks 0-5 | 6-10
 #pragma unroll 1
-    for (uint32_t c = 0; c < GD_IN / 16; ++c) {
-      tmem_ld16(trow + GT_DW1 + 16u * c, v);
-#pragma unroll
-      for (int i = 0; i < 16; ++i) atomicAdd(grad + GD_P_W1 + row * GD_IN + 16u * c + i, v[i]);
-    }
+    for (uint32_t c = c1a; c < c1b; ++c) flush(GT_DW1 + 16u * c, grad + GD_P_W1 + row * GD_IN + 16u * c);
 #pragma unroll 1
-    for (uint32_t c = 0; c < GD_H / 16; ++c) {
-      tmem_ld16(trow + GT_DW2 + 16u * c, v);
-#pragma unroll
-      for (int i = 0; i < 16; ++i) atomicAdd(grad + GD_P_W2 + row * GD_H + 16u * c + i, v[i]);
-      tmem_ld16(trow + GT_DW3 + 16u * c, v);
-#pragma unroll
-      for (int i = 0; i < 16; ++i) atomicAdd(grad + GD_P_W3 + row * GD_H + 16u * c + i, v[i]);
-      tmem_ld16(trow + GT_DW4 + 16u * c, v);
+    for (uint32_t c = 2u * half; c < 2u * half + 2u; ++c) {
+      flush(GT_DW2 + 16u * c, grad + GD_P_W2 + row * GD_H + 16u * c);
+      flush(GT_DW3 + 16u * c, grad + GD_P_W3 + row * GD_H + 16u * c);
+      tmem_ld16(trow + GT_DW4 + 16u * c, v);  // every lane loads (the load is warp-wide); rows < 40 exist
       if (row < GD_OUT) {
 #pragma unroll
-        for (int i = 0; i < 16; ++i) atomicAdd(grad + GD_P_W4 + row * GD_H + 16u * c + i, v[i]);
+        for (int i = 0; i < 16; i += 4)
+          atomicAdd(reinterpret_cast<float4*>(grad + GD_P_W4 + row * GD_H + 16u * c + i),
+                    make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]));
       }
     }
   }
@@ -915,7 +1043,7 @@ void launch_train(clv_guide* g, const float4* rec, uint32_t n, cudaStream_t st) 
   const uint32_t tiles = (n + GD_TILE - 1) / GD_TILE;
   const uint32_t grid = std::min<uint32_t>(tiles, (uint32_t)sms());
   smem_attr(guide_train_kernel, GD_SMEM_TRAIN);
-  guide_train_kernel<<<grid, 128, GD_SMEM_TRAIN, st>>>(g->wblob, rec, n, g->grad, g->loss, g->err);
+  guide_train_kernel<<<grid, 256, GD_SMEM_TRAIN, st>>>(g->wblob, rec, n, g->grad, g->loss, g->err);
   clv_internal_count_launches(1);
 }
 
@@ -946,7 +1074,7 @@ void gd_prepare() {
 void gd_launch_queue(const GuideDev& G, const GdQueue& Q, uint32_t max_queries, cudaStream_t st) {
   const uint32_t tiles = (max_queries + GD_TILE - 1) / GD_TILE;
   const uint32_t grid = std::max<uint32_t>(1, std::min<uint32_t>(tiles, 2u * (uint32_t)sms()));
-  guide_infer_kernel<SRC_QUEUE><<<grid, 128, GD_SMEM_INFER, st>>>(G, Q, ArrayIO{nullptr, nullptr, 0u});
+  guide_infer_kernel<SRC_QUEUE><<<grid, 256, GD_SMEM_INFER, st>>>(G, Q, ArrayIO{nullptr, nullptr, 0u});
 }
 
 void gd_reset_records(clv_guide* g, cudaStream_t st) {
@@ -1050,7 +1178,7 @@ int clv_guide_forward(clv_guide* g, const float* queries, uint64_t n, float* out
     G.err = g->err;
     const uint32_t tiles = (uint32_t)((n + GD_TILE - 1) / GD_TILE);
     smem_attr(guide_infer_kernel<SRC_ARRAY>, GD_SMEM_INFER);
-    guide_infer_kernel<SRC_ARRAY><<<std::min<uint32_t>(tiles, 2u * sms()), 128, GD_SMEM_INFER>>>(G, GdQueue{}, A);
+    guide_infer_kernel<SRC_ARRAY><<<std::min<uint32_t>(tiles, 2u * sms()), 256, GD_SMEM_INFER>>>(G, GdQueue{}, A);
     clv_internal_count_launches(1);
     ckg(cudaGetLastError(), "guide forward launch");
     ckg(cudaMemcpy(out, A.out, bo, cudaMemcpyDeviceToHost), "cudaMemcpy D2H");

@@ -12,7 +12,10 @@ samples per pixel with seed 1, over two pixel sets of a workload image:
 These are the converged references that GPU renders are measured against
 (relMSE, GPU time to relMSE <= 1e-3).  GPU renders use other seeds.
 
-    python tests/golden/make_golden.py [name ...]     # names: box, prism, spheres, dense
+    python tests/golden/make_golden.py [name ...]     # names: box, prism, spheres, dense, batch
+
+``batch_ref.npz`` holds the same kind of subset reference for four scenes of the
+batched multi-scene workload (BATCH below).
 """
 
 import os
@@ -55,6 +58,13 @@ def scene_file(name, tmp):
     return scenes.write_scene(sc, os.path.join(tmp, name + ".json"))
 
 
+# Scenes of the batched multi-scene workload (clovers_gb300.scenes.batch_scene(index)) with a golden
+# reference over a stratified subset of their pixels: index -> subset stride.  Two without and two with
+# constant-density media, of four material kinds.
+BATCH = {3: 8, 23: 8, 31: 8, 40: 8}
+BATCH_DEPTH = 16
+
+
 def subset_pixels(width, height, stride):
     """Buffer indices of the centre pixel of every stride x stride cell of the image."""
     xs = np.arange(stride // 2, width, stride)
@@ -79,6 +89,26 @@ def make(name):
         name, el, os.cpu_count(), crop.mean(0), sub.mean(0), out), flush=True)
 
 
+def make_batch():
+    """tests/golden/batch_ref.npz: per scene of BATCH its subset's pixel indices and means."""
+    out = {}
+    with tempfile.TemporaryDirectory() as tmp:
+        for k, stride in sorted(BATCH.items()):
+            sc, w, h, _ = scenes.batch_scene(k, tmp)
+            path = scenes.write_scene(sc, os.path.join(tmp, "batch_%02d.json" % k))
+            o = oracle.Scene.from_json(path, w, h, precision=PRECISION)
+            px = subset_pixels(w, h, stride)
+            t0 = time.time()
+            sub = o.render_pixels(w, h, SPP, BATCH_DEPTH, SEED, px) / SPP
+            out["s%d_pixels" % k] = px
+            out["s%d_mean" % k] = sub
+            out["s%d_size" % k] = np.array([w, h])
+            print("batch scene %d: %dx%d, %d pixels, %.1f s, mean %s" % (k, w, h, px.size, time.time() - t0,
+                                                                        sub.mean(0)), flush=True)
+    np.savez_compressed(os.path.join(HERE, "batch_ref.npz"), scenes=np.array(sorted(BATCH)), spp=SPP, seed=SEED,
+                        depth=BATCH_DEPTH, precision=PRECISION, **out)
+
+
 if __name__ == "__main__":
-    for n in (sys.argv[1:] or list(WORKLOADS)):
-        make(n)
+    for n in (sys.argv[1:] or list(WORKLOADS) + ["batch"]):
+        make_batch() if n == "batch" else make(n)

@@ -90,3 +90,41 @@ def test_gpu_converges_to_golden(name):
         err = relmse(img[px], ref)
         print("%s %s: relMSE %.3g at %d spp (bound %s)" % (name, k, err, spp, bound))
         assert err < bound
+
+
+# batch scene -> relMSE bound of its subset at 256 spp (1.7x the f32 oracle's mean over three seeds:
+# 4.0e-4, 2.7e-3, 1.1e-4, 2.6e-3)
+BOUNDS_BATCH = {3: 6.8e-4, 23: 4.6e-3, 31: 1.9e-4, 40: 4.4e-3}
+
+
+def test_batch_golden_file_is_well_formed():
+    g = golden("batch")
+    assert sorted(int(k) for k in g["scenes"]) == sorted(make_golden.BATCH) == sorted(BOUNDS_BATCH)
+    assert int(g["spp"]) == 65536 and str(g["precision"]) == "f64"
+    for k, stride in make_golden.BATCH.items():
+        w, h = [int(v) for v in g["s%d_size" % k]]
+        assert np.array_equal(g["s%d_pixels" % k], make_golden.subset_pixels(w, h, stride))
+        m = g["s%d_mean" % k]
+        assert m.shape == (g["s%d_pixels" % k].size, 3) and np.all(np.isfinite(m)) and m.mean() > 0
+
+
+@pytest.mark.gpu
+def test_gpu_batch_converges_to_golden():
+    """The four golden scenes of the batched workload rendered together in one wavefront
+    (clv_render_batch) at 256 spp converge to the f64 references."""
+    from clovers_gb300 import scenes
+    g = golden("batch")
+    ids = [int(k) for k in g["scenes"]]
+    dev, opts = [], []
+    with tempfile.TemporaryDirectory() as tmp:
+        for k in ids:
+            sc, w, h, _ = scenes.batch_scene(k, tmp)
+            path = scenes.write_scene(sc, os.path.join(tmp, "batch_%02d.json" % k))
+            dev.append(cg.Scene.from_json(path, w, h).upload())
+            opts.append(cg.RenderOptions(width=w, height=h, samples=256, max_depth=int(g["depth"]), seed=4242))
+    imgs = cg.draw_batch(dev, opts)
+    for k, img, d in zip(ids, imgs, dev):
+        err = relmse(img.reshape(-1, 3).astype(np.float64)[g["s%d_pixels" % k]], g["s%d_mean" % k])
+        print("batch scene %d: relMSE %.3g at 256 spp (bound %g)" % (k, err, BOUNDS_BATCH[k]))
+        assert err < BOUNDS_BATCH[k]
+        assert d.status() == 0
