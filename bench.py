@@ -360,6 +360,43 @@ def batch_convergence(args, dev, tmp):
     for k in todo:
         res_batch[k] = {"gpu_ms": None, "spp": npass * chunk, "reached": False}
     t_batch_all = t
+    # (a') together, guided: one guide for all scenes, trained online on their records
+    res_gbatch, t_gbatch_all = {}, None
+    if args.guided:
+        for f in films.values():
+            f.zero_()
+        guide = cg.Guide(seed=args.guide_seed if args.guide_seed is not None else 7, learning_rate=args.guide_lr)
+        todo, t, npass, total = list(ids), 0.0, 0, 0
+        while todo and total < args.max_spp:
+            training = npass < args.guide_passes
+            nspp = args.guide_pass_spp if training else chunk
+            n = len(todo)
+            handles = (ctypes.c_void_p * n)(*[dev[k].handle.value for k in todo])
+            ol = []
+            for k in todo:
+                w, h = size[k]
+                o = cg.render_opts(cg.RenderOptions(width=w, height=h, samples=nspp, max_depth=DEPTH, seed=seed + k))
+                o.sample_offset = total
+                ol.append(o)
+            optarr = (_lib.RenderOptsC * n)(*ol)
+            ptrs = (ctypes.c_void_p * n)(*[films[k].data_ptr() for k in todo])
+            alpha = 0.0 if npass == 0 else args.guide_alpha
+
+            def gstep():
+                _lib.check(L.clv_render_batch_guided(handles, optarr, ptrs, n, guide.handle, alpha, sp))
+                if training:
+                    _lib.check(L.clv_guide_train(guide.handle, args.guide_steps, args.guide_batch, None, sp))
+            t += timed(gstep)
+            npass += 1
+            total += nspp
+            for k in list(todo):
+                e = relmse(k, total)
+                if e <= target:
+                    res_gbatch[k] = {"gpu_ms": round(t, 2), "spp": total, "relmse": e}
+                    todo.remove(k)
+        for k in todo:
+            res_gbatch[k] = {"gpu_ms": None, "spp": total, "reached": False}
+        t_gbatch_all = t
     # (b) alone, plain; (c) alone, guided
     res_alone, res_guided = {}, {}
     for k in ids:
@@ -405,6 +442,14 @@ def batch_convergence(args, dev, tmp):
     if res_guided:
         out["guided_alone"] = {str(k): v for k, v in res_guided.items()}
         out["guided_alone_total_ms"] = round(sum(v["gpu_ms"] for v in res_guided.values()), 2)
+    if res_gbatch:
+        out["guided_batched"] = {str(k): v for k, v in res_gbatch.items()}
+        out["guided_batched_total_ms"] = round(t_gbatch_all, 2)
+        out["guided_estimator"] = ("alpha %.2f of Lambertian bounces from one vMF-mixture MLP shared by the scenes "
+                                   "(positions normalised to each scene's box); %d training passes of %d spp, %d "
+                                   "Adam steps of %d records after each" % (args.guide_alpha, args.guide_passes,
+                                                                            args.guide_pass_spp, args.guide_steps,
+                                                                            args.guide_batch))
     return out
 
 

@@ -205,8 +205,9 @@ class DeviceBuffer:
             pass
 
 
-def draw_batch(scenes, options, stats=None):
-    """Renders several scenes in one wavefront (clv_render_batch): a list of (h*w, 3) XYZ(E) means."""
+def draw_batch(scenes, options, stats=None, guide=None, alpha=0.5):
+    """Renders several scenes in one wavefront (clv_render_batch, or clv_render_batch_guided with a
+    guide): a list of (h*w, 3) XYZ(E) means."""
     n = len(scenes)
     if n == 0 or n != len(options):
         raise ValueError("one RenderOptions per scene")
@@ -214,7 +215,10 @@ def draw_batch(scenes, options, stats=None):
     films = [DeviceBuffer(o.width * o.height * 3 * 8).zero() for o in options]
     handles = (ctypes.c_void_p * n)(*[s.handle.value for s in scenes])
     ptrs = (ctypes.c_void_p * n)(*[f.ptr.value for f in films])
-    check(lib().clv_render_batch(handles, opts, ptrs, n, None))
+    if guide is None:
+        check(lib().clv_render_batch(handles, opts, ptrs, n, None))
+    else:
+        check(lib().clv_render_batch_guided(handles, opts, ptrs, n, guide.handle, alpha, None))
     out = []
     for f, o in zip(films, options):
         out.append((f.to_numpy(np.float64, (o.width * o.height, 3)) / o.samples).astype(np.float32))

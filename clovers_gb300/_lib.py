@@ -89,6 +89,8 @@ SIGNATURES = {
     "clv_guide_set_params": (c_i32, [ctypes.c_void_p, ctypes.c_void_p]),
     "clv_render_guided": (c_i32, [ctypes.c_void_p, P(RenderOptsC), ctypes.c_void_p, c_f32, ctypes.c_void_p,
                                   ctypes.c_void_p]),
+    "clv_render_batch_guided": (c_i32, [ctypes.c_void_p, P(RenderOptsC), ctypes.c_void_p, c_u32, ctypes.c_void_p,
+                                        c_f32, ctypes.c_void_p]),
     "clv_guide_train": (c_i32, [ctypes.c_void_p, c_u32, c_u32, P(c_f64), ctypes.c_void_p]),
     "clv_guide_record_count": (c_i32, [ctypes.c_void_p, P(c_u64)]),
     "clv_guide_get_records": (c_i32, [ctypes.c_void_p, ctypes.c_void_p, c_u64]),

@@ -1338,9 +1338,9 @@ static int render_wavefront(clv_device_scene* d, const clv_render_opts* o, doubl
       wf_shade_specular<false><<<qgrid, block, 0, s>>>(d->view, P, W, C, d->err, WfBatch{});
       wf_shade_diffuse<false><<<qgrid, block, 0, s>>>(d->view, P, W, C, d->err, WfBatch{});
       if (guide) {
-        wf_guide_pre<<<qgrid, block, 0, s>>>(d->view, W, C, alpha);
+        wf_guide_pre<false><<<qgrid, block, 0, s>>>(d->view, W, C, alpha, WfBatch{});
         if (alpha > 0.0f) gd_launch_queue(G, GQ, (uint32_t)q, s);
-        wf_guide_post<<<qgrid, block, 0, s>>>(d->view, P, W, C, d->err, G);
+        wf_guide_post<false><<<qgrid, block, 0, s>>>(d->view, P, W, C, d->err, G, WfBatch{});
       }
       wf_finish<false><<<qgrid, block, 0, s>>>(d->view, P, W, C, film, WfBatch{});
       if (prof) cudaEventRecord(evs[4 * k + 3], s);
@@ -1398,8 +1398,11 @@ static int render_wavefront(clv_device_scene* d, const clv_render_opts* o, doubl
   }
 }
 
-int clv_render_batch(clv_device_scene* const* ds, const clv_render_opts* opts, double* const* films, uint32_t n,
-                     void* stream) {
+// The multi-scene wavefront; with `guide`, Lambertian bounces of every scene
+// go through the one guide (alpha as in clv_render_guided), positions
+// normalised to each scene's own box.
+static int render_batch(clv_device_scene* const* ds, const clv_render_opts* opts, double* const* films, uint32_t n,
+                        void* stream, clv_guide* guide, float alpha) {
   if (!ds || !opts || !films || n == 0) return fail(CLV_E_INVALID, "null argument or empty batch");
   if (n > (1u << 24)) return fail(CLV_E_INVALID, "too many scenes in one batch");
   for (uint32_t k = 0; k < n; ++k) {
@@ -1447,8 +1450,9 @@ int clv_render_batch(clv_device_scene* const* ds, const clv_render_opts* opts, d
     // one staging allocation for the batch tables
     const size_t b_views = n * sizeof(ClvDeviceScene), b_params = n * sizeof(WfParams);
     const size_t b_prefix = (n + 1) * sizeof(unsigned long long), b_films = n * sizeof(double*);
+    const size_t b_boxes = guide ? n * 6 * sizeof(float) : 0;
     auto up = [](size_t x) { return (x + 255) / 256 * 256; };
-    const size_t bytes = up(b_views) + up(b_params) + up(b_prefix) + up(b_films);
+    const size_t bytes = up(b_views) + up(b_params) + up(b_prefix) + up(b_films) + up(b_boxes);
     ck(cudaMalloc(&dmem, bytes), "cudaMalloc batch tables");
     char* c = static_cast<char*>(dmem);
     WfBatch B;
@@ -1463,6 +1467,16 @@ int clv_render_batch(clv_device_scene* const* ds, const clv_render_opts* opts, d
     c += up(b_prefix);
     B.films = reinterpret_cast<double* const*>(c);
     ck(cudaMemcpyAsync(c, fl.data(), b_films, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync");
+    c += up(b_films);
+    std::vector<float> boxes(guide ? n * 6 : 0);
+    for (uint32_t j = 0; guide && j < n; ++j)  // {bmin, 1 / extent} of each scene's box, batch order
+      for (int a = 0; a < 3; ++a) {
+        const float lo = views[j].root_box[2 * a], ext = views[j].root_box[2 * a + 1] - lo;
+        boxes[6 * j + a] = lo;
+        boxes[6 * j + 3 + a] = ext > 0.0f ? 1.0f / ext : 0.0f;
+      }
+    if (guide) ck(cudaMemcpyAsync(c, boxes.data(), b_boxes, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync");
+    const float* dboxes = guide ? reinterpret_cast<const float*>(c) : nullptr;
     B.n = n;
     B.total = total;
     clv_device_scene* d0 = ds[0];  // path state, counters and the error word come from the first scene
@@ -1485,6 +1499,19 @@ int clv_render_batch(clv_device_scene* const* ds, const clv_render_opts* opts, d
     WfCounters c0{std::min<unsigned long long>(q, total), 0u, {0u, 0u, 0u, 0u}};
     ck(cudaMemcpyAsync(d0->wf_counters, &c0, sizeof c0, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync");
     WfCounters* C = d0->wf_counters;
+    GuideDev G{};
+    GdQueue GQ{};
+    if (guide) {
+      W.gslot = guide->ensure_slots((uint32_t)q);
+      W.grec = guide->rec;
+      W.grec_count = guide->rec_count;
+      W.grec_cap = guide->rec_cap;
+      gd_reset_records(guide, st);
+      G = gd_view(guide, d0->view.root_box, alpha);
+      G.boxes = dboxes;
+      GQ = GdQueue{W.queue + (size_t)WF_Q_GUIDE * q, &C->queue[WF_Q_GUIDE], W.full, W.d_lambda, W.hit, W.meta, W.key};
+      gd_prepare();
+    }
     const int block = 128;
     const uint32_t grid = (uint32_t)((q + block - 1) / block);
     const uint32_t qgrid =
@@ -1514,6 +1541,11 @@ int clv_render_batch(clv_device_scene* const* ds, const clv_render_opts* opts, d
                                                                             only < 0 ? -1 : 2);
         wf_shade_specular<true><<<qgrid, block, 0, s>>>(S0, P0, W, C, d0->err, B);
         wf_shade_diffuse<true><<<qgrid, block, 0, s>>>(S0, P0, W, C, d0->err, B);
+        if (guide) {
+          wf_guide_pre<true><<<qgrid, block, 0, s>>>(S0, W, C, alpha, B);
+          if (alpha > 0.0f) gd_launch_queue(G, GQ, (uint32_t)q, s);
+          wf_guide_post<true><<<qgrid, block, 0, s>>>(S0, P0, W, C, d0->err, G, B);
+        }
         wf_finish<true><<<qgrid, block, 0, s>>>(S0, P0, W, C, nullptr, B);
       }
     };
@@ -1521,7 +1553,7 @@ int clv_render_batch(clv_device_scene* const* ds, const clv_render_opts* opts, d
     for (uint64_t it = 0;; it += batch) {
       if (graph.exec) ck(cudaGraphLaunch(graph.exec, st), "cudaGraphLaunch");
       else bounces(st);
-      g_launches += (3 + (spill_entries ? 1 : nlevels)) * batch;
+      g_launches += (3 + (spill_entries ? 1 : nlevels) + (guide ? (alpha > 0.0f ? 3 : 2) : 0)) * batch;
       ck(cudaGetLastError(), "wavefront launch");
       ck(cudaMemcpyAsync(d0->wf_live_host, &C->live, sizeof(unsigned int), cudaMemcpyDeviceToHost, st),
          "cudaMemcpyAsync");
@@ -1538,6 +1570,27 @@ int clv_render_batch(clv_device_scene* const* ds, const clv_render_opts* opts, d
     }
     return fail(CLV_E_CUDA, e.what());
   }
+}
+
+int clv_render_batch(clv_device_scene* const* ds, const clv_render_opts* opts, double* const* films, uint32_t n,
+                     void* stream) {
+  return render_batch(ds, opts, films, n, stream, nullptr, 0.0f);
+}
+
+int clv_render_batch_guided(clv_device_scene* const* ds, const clv_render_opts* opts, double* const* films,
+                            uint32_t n, clv_guide* g, float alpha, void* stream) {
+  if (!g) return fail(CLV_E_INVALID, "null guide");
+  if (!(alpha >= 0.0f && alpha <= 1.0f)) return fail(CLV_E_INVALID, "alpha must lie in [0, 1]");
+  const int rc = render_batch(ds, opts, films, n, stream, g, alpha);
+  if (rc) return rc;
+  uint32_t e = 0;
+  if (cudaMemcpy(&e, g->err, sizeof e, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return fail(CLV_E_CUDA, "cudaMemcpy D2H");
+  if (e) {
+    cudaMemset(g->err, 0, sizeof e);
+    return fail(CLV_E_DEVICE, "guide kernel timed out waiting for the tensor cores");
+  }
+  return CLV_OK;
 }
 
 int clv_render_guided(clv_device_scene* d, const clv_render_opts* o, clv_guide* g, float alpha, double* film_dev,

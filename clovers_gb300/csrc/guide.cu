@@ -513,9 +513,11 @@ __global__ void __launch_bounds__(256) guide_infer_kernel(GuideDev G, GdQueue Q,
         slot = Q.queue[qi];
         const float4 f0 = Q.full[3 * slot];
         const float4 dl = Q.d_lambda[slot];
-        u[0] = sat((f0.x - G.bmin[0]) * G.binv[0]);
-        u[1] = sat((f0.y - G.bmin[1]) * G.binv[1]);
-        u[2] = sat((f0.z - G.bmin[2]) * G.binv[2]);
+        float lo[3], inv[3];
+        gd_box(G, G.boxes ? Q.meta[slot].w : 0u, lo, inv);
+        u[0] = sat((f0.x - lo[0]) * inv[0]);
+        u[1] = sat((f0.y - lo[1]) * inv[1]);
+        u[2] = sat((f0.z - lo[2]) * inv[2]);
         u[3] = sat(0.5f - 0.5f * dl.x);  // outgoing direction = -ray direction
         u[4] = sat(0.5f - 0.5f * dl.y);
         u[5] = sat(0.5f - 0.5f * dl.z);
@@ -1093,6 +1095,7 @@ GuideDev gd_view(clv_guide* g, const float root_box[6], float alpha) {
     G.bmin[a] = lo;
     G.binv[a] = ext > 0.0f ? 1.0f / ext : 0.0f;
   }
+  G.boxes = nullptr;
   G.alpha = alpha;
   G.err = g->err;
   return G;

@@ -82,9 +82,28 @@ struct GuideDev {
   uint4* slot;                 // per path slot: record ids of its first two guided
                                // vertices and the hero throughput before each
   float bmin[3], binv[3];      // position normalisation (scene box)
+  const float* boxes;          // batches: per scene {bmin[3], binv[3]}, indexed by the slot's scene
+                               // (meta.w >> 8); null: bmin / binv
   float alpha;                 // share of guided samples in the blend
   uint32_t* err;
 };
+// Position normalisation of a slot's scene: {bmin, binv} of the batch table or the single scene.
+__device__ __forceinline__ void gd_box(const GuideDev& G, uint32_t meta_w, float lo[3], float inv[3]) {
+  if (G.boxes) {
+    const float* b = G.boxes + 6 * (size_t)(meta_w >> 8);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      lo[a] = b[a];
+      inv[a] = b[3 + a];
+    }
+  } else {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      lo[a] = G.bmin[a];
+      inv[a] = G.binv[a];
+    }
+  }
+}
 
 // The guided-vertex queue of one bounce and the path state it reads.
 struct GdQueue {

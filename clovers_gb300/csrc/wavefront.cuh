@@ -542,11 +542,16 @@ __device__ __forceinline__ void guide_pre_slot(const ClvDeviceScene& S, const Wf
   W.meta[i].z = p.rng.counter;
 }
 
-__global__ void __launch_bounds__(128, CLV_MINB_GUIDE) wf_guide_pre(ClvDeviceScene S, WfState W, WfCounters* C, float alpha) {
+template <bool BATCH>
+__global__ void __launch_bounds__(128, CLV_MINB_GUIDE) wf_guide_pre(ClvDeviceScene S, WfState W, WfCounters* C, float alpha,
+                                                    WfBatch B) {
   const uint32_t n = C->queue[WF_Q_GUIDE];
   const uint32_t stride = gridDim.x * blockDim.x;
-  for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += stride)
-    guide_pre_slot(S, W, alpha, W.queue[(size_t)WF_Q_GUIDE * W.Q + q]);
+  for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += stride) {
+    const uint32_t i = W.queue[(size_t)WF_Q_GUIDE * W.Q + q];
+    if constexpr (BATCH) guide_pre_slot(B.scenes[W.meta[i].w >> 8], W, alpha, i);
+    else guide_pre_slot(S, W, alpha, i);
+  }
 }
 
 // post: W.hit = {direction, guide density}.  One-sample MIS over the guide
@@ -592,9 +597,11 @@ __device__ __forceinline__ bool guide_post_slot(const ClvDeviceScene& S, const W
       if (r < W.grec_cap) {
         const float4 dl = W.d_lambda[i];
         float4* out = W.grec + GD_REC_F4 * (size_t)r;
-        out[0] = make_float4(fminf(1.0f, fmaxf(0.0f, (rec.p.x - G.bmin[0]) * G.binv[0])),
-                             fminf(1.0f, fmaxf(0.0f, (rec.p.y - G.bmin[1]) * G.binv[1])),
-                             fminf(1.0f, fmaxf(0.0f, (rec.p.z - G.bmin[2]) * G.binv[2])),
+        float lo[3], inv[3];
+        gd_box(G, p.meta.w, lo, inv);
+        out[0] = make_float4(fminf(1.0f, fmaxf(0.0f, (rec.p.x - lo[0]) * inv[0])),
+                             fminf(1.0f, fmaxf(0.0f, (rec.p.y - lo[1]) * inv[1])),
+                             fminf(1.0f, fmaxf(0.0f, (rec.p.z - lo[2]) * inv[2])),
                              fminf(1.0f, fmaxf(0.0f, 0.5f - 0.5f * dl.x)));
         out[1] = make_float4(fminf(1.0f, fmaxf(0.0f, 0.5f - 0.5f * dl.y)),
                              fminf(1.0f, fmaxf(0.0f, 0.5f - 0.5f * dl.z)),
@@ -623,8 +630,9 @@ __device__ __forceinline__ bool guide_post_slot(const ClvDeviceScene& S, const W
   return wf_advance(P, W, C, i, p, rec.p, nd);
 }
 
+template <bool BATCH>
 __global__ void __launch_bounds__(128, CLV_MINB_GUIDE) wf_guide_post(ClvDeviceScene S, WfParams P, WfState W, WfCounters* C,
-                                                     uint32_t* err, GuideDev G) {
+                                                     uint32_t* err, GuideDev G, WfBatch B) {
   const uint32_t n = C->queue[WF_Q_GUIDE];
   const uint32_t stride = gridDim.x * blockDim.x;
   const uint32_t first = blockIdx.x * blockDim.x + threadIdx.x;
@@ -634,7 +642,14 @@ __global__ void __launch_bounds__(128, CLV_MINB_GUIDE) wf_guide_post(ClvDeviceSc
     const uint32_t q = first + r * stride;
     bool live = false;
     const uint32_t i = q < n ? W.queue[(size_t)WF_Q_GUIDE * W.Q + q] : 0u;
-    if (q < n) live = guide_post_slot(S, P, W, C, err, G, i);
+    if (q < n) {
+      if constexpr (BATCH) {
+        const uint32_t sid = W.meta[i].w >> 8;
+        live = guide_post_slot(B.scenes[sid], B.params[sid], W, C, err, G, i);
+      } else {
+        live = guide_post_slot(S, P, W, C, err, G, i);
+      }
+    }
     wf_enqueue_block_one(W, C, WF_Q_FINISH, q < n && !live, i);
     nlive += live ? 1u : 0u;
   }

@@ -229,6 +229,14 @@ int clv_guide_set_params(clv_guide* guide, const float* params);
 int clv_render_guided(clv_device_scene* dscene, const clv_render_opts* opts, clv_guide* guide, float alpha,
                       double* film_dev, void* stream);
 
+/* clv_render_batch with the guide: the Lambertian bounces of every scene of
+ * the batch are drawn (share alpha) from the one guide, its inputs normalised
+ * to each scene's own box, and they leave training records for
+ * clv_guide_train, as clv_render_guided does for one scene.  No counterpart in
+ * the reference. */
+int clv_render_batch_guided(clv_device_scene* const* dscenes, const clv_render_opts* opts, double* const* films,
+                            uint32_t n, clv_guide* guide, float alpha, void* stream);
+
 /* `steps` Adam steps on consecutive batches of `batch` records (0 = 65536)
  * of the last guided render, taken from the records that carry light (f > 0;
  * the others add nothing to the gradient); mean_loss (optional) receives the

@@ -27,3 +27,25 @@ def test_batch_matches_individual_renders(tmp_path):
         single = cg.draw(cg.GlobalOptions(quiet=True), o, d)
         np.testing.assert_allclose(img, single, rtol=1e-6, atol=1e-9)
         assert d.status() == 0
+
+
+def test_guided_batch_matches_guided_single_renders(tmp_path):
+    """clv_render_batch_guided with one guide for every scene gives each scene the film that
+    clv_render_guided gives it alone with the same guide (same random streams; each query's network
+    output depends only on its own inputs, normalised to its own scene's box)."""
+    specs = [(scenes.enclosed_box(), 40, 32, 16, 10, 7), (scenes.random_spheres(1), 48, 27, 8, 12, 8)]
+    dev, opts = [], []
+    for k, (sc, w, h, spp, depth, seed) in enumerate(specs):
+        path = scenes.write_scene(sc, str(tmp_path / ("g%d.json" % k)))
+        dev.append(cg.Scene.from_json(path, w, h).upload())
+        opts.append(cg.RenderOptions(width=w, height=h, samples=spp, max_depth=depth, seed=seed))
+    guide = cg.Guide(seed=5)
+    for alpha in (0.0, 0.5):
+        batched = cg.draw_batch(dev, opts, guide=guide, alpha=alpha)
+        for d, o, img in zip(dev, opts, batched):
+            film = cg.DeviceBuffer(o.width * o.height * 24).zero()
+            cg.render_guided(d, o, guide, alpha, film)
+            single = film.to_numpy(np.float64, (o.width * o.height, 3)) / o.samples
+            np.testing.assert_allclose(img, single, rtol=1e-6, atol=1e-9)
+            assert d.status() == 0
+    assert guide.status() == 0
