@@ -289,6 +289,8 @@ __device__ __forceinline__ float mix_pdf(const Mix& m, float x, float y, float z
   }
   return q;
 }
+__device__ __forceinline__ void vmf_sample(float mx, float my, float mz, float kap, float u1, float u2, float& x,
+                                           float& y, float& z);
 // Lobe by u0, then the vMF sample of Jakob 2012 ("Numerically stable sampling
 // of the von Mises-Fisher distribution on S2") in the frame of Duff et al. 2017.
 __device__ __forceinline__ void mix_sample(const Mix& m, float u0, float u1, float u2, float& x, float& y, float& z) {
@@ -306,6 +308,11 @@ __device__ __forceinline__ void mix_sample(const Mix& m, float u0, float u1, flo
       kap = m.kap[k];
     }
   }
+  vmf_sample(mx, my, mz, kap, u1, u2, x, y, z);
+}
+// Jakob 2012's vMF sample around unit mean (mx, my, mz), concentration kap.
+__device__ __forceinline__ void vmf_sample(float mx, float my, float mz, float kap, float u1, float u2, float& x,
+                                           float& y, float& z) {
   float W = 1.0f + logf(u1 + (1.0f - u1) * expf(-2.0f * kap)) / kap;
   W = fminf(1.0f, fmaxf(-1.0f, W));
   const float sw = sqrtf(fmaxf(0.0f, 1.0f - W * W));
@@ -350,7 +357,8 @@ __device__ __forceinline__ float mix_grad(const Mix& m, float x, float y, float 
 namespace gd {
 
 // ------------------------------------------------------------- inference --
-#define GD_SMEM_INFER (GD_B_FWD + GD_TILE * GD_IN * 2 + GD_TILE * GD_H * 2 + 64)
+#define GI_XCH (GD_B_FWD + GD_TILE * GD_IN * 2 + GD_TILE * GD_H * 2)  // head exchange: 10 x 128 floats
+#define GD_SMEM_INFER (GI_XCH + 10 * GD_TILE * 4 + 64)
 enum { SRC_QUEUE = 0, SRC_ARRAY = 1 };
 struct ArrayIO {
   const float4* in;  // 2 per query: u0..u3 | u4..u6, -
@@ -467,6 +475,88 @@ __device__ __forceinline__ void backward_epilogue_half(uint32_t trow, uint32_t m
   }
 }
 
+// The vMF head split over the two threads of a row: each evaluates four
+// lobes (K0 = 0 or 4) and the two exchange the softmax maximum, the softmax
+// sum and the mixture density through shared memory (xch: 3 x 2 x 128
+// floats; every thread of the CTA calls these, so the barriers are uniform).
+struct Mix4 {
+  float mu[4][3], kap[4], w[4], nrm[4], mlen[4];
+  uint32_t kclamp;  // bit j: the concentration of lobe K0 + j was clamped
+};
+__device__ __forceinline__ float pair_exchange(float* xch, uint32_t row, uint32_t half, float v, bool take_max) {
+  xch[half * GD_TILE + row] = v;
+  __syncthreads();
+  const float a = xch[row], b = xch[GD_TILE + row];
+  return take_max ? fmaxf(a, b) : a + b;
+}
+// o[j] = output 5 K0 + j (j < 20).  Fills m (weights normalised over all 8 lobes).
+__device__ __forceinline__ void make_mix4(const float* o, Mix4& m, float* xch, uint32_t row, uint32_t half) {
+  float lmax = -3.0e38f;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) lmax = fmaxf(lmax, o[5 * k + 4]);
+  const float mx = pair_exchange(xch, row, half, lmax, true);
+  float sum = 0.0f;
+  m.kclamp = 0u;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const float x = o[5 * k], y = o[5 * k + 1], z = o[5 * k + 2];
+    const float l = sqrtf(x * x + y * y + z * z);
+    if (l > 1e-6f) {
+      m.mu[k][0] = x / l;
+      m.mu[k][1] = y / l;
+      m.mu[k][2] = z / l;
+      m.mlen[k] = l;
+    } else {
+      m.mu[k][0] = 0.0f;
+      m.mu[k][1] = 0.0f;
+      m.mu[k][2] = 1.0f;
+      m.mlen[k] = 1e-6f;
+    }
+    float lk = o[5 * k + 3];
+    if (!(lk >= GD_LOGK_MIN && lk <= GD_LOGK_MAX)) {
+      m.kclamp |= 1u << k;
+      lk = lk < GD_LOGK_MIN ? GD_LOGK_MIN : (lk > GD_LOGK_MAX ? GD_LOGK_MAX : GD_LOGK_MIN);
+    }
+    const float kap = expf(lk);
+    m.kap[k] = kap;
+    m.nrm[k] = kap / (6.283185307179586f * -expm1f(-2.0f * kap));
+    const float e = expf(o[5 * k + 4] - mx);
+    m.w[k] = e;
+    sum += e;
+  }
+  const float inv = 1.0f / pair_exchange(xch + 2 * GD_TILE, row, half, sum, false);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) m.w[k] *= inv;
+}
+// d[j] = d(-f log q(w)) / d output 5 K0 + j for the four lobes; returns -f log q
+// (the caller counts it once per row).
+__device__ __forceinline__ float mix_grad4(const Mix4& m, float x, float y, float z, float f, float* d, float* xch,
+                                           uint32_t row, uint32_t half) {
+  float v[4], c[4];
+  float qh = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    c[k] = m.mu[k][0] * x + m.mu[k][1] * y + m.mu[k][2] * z;
+    v[k] = m.nrm[k] * expf(m.kap[k] * (c[k] - 1.0f));
+    qh += m.w[k] * v[k];
+  }
+  const float q = fmaxf(pair_exchange(xch + 4 * GD_TILE, row, half, qh, false), 1e-30f);
+  const float g = -f / q;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const float kap = m.kap[k];
+    const float a = g * m.w[k] * v[k];
+    d[5 * k + 4] = a - g * m.w[k] * q;
+    const float dk = a * (1.0f / kap - 2.0f / expm1f(2.0f * kap) + c[k] - 1.0f);
+    d[5 * k + 3] = (m.kclamp >> k) & 1u ? 0.0f : dk * kap;
+    const float s = a * kap / m.mlen[k];
+    d[5 * k + 0] = s * (x - m.mu[k][0] * c[k]);
+    d[5 * k + 1] = s * (y - m.mu[k][1] * c[k]);
+    d[5 * k + 2] = s * (z - m.mu[k][2] * c[k]);
+  }
+  return f > 0.0f ? -f * logf(q) : 0.0f;
+}
+
 // Eight warps: warps w and w + 4 read the same TMEM lanes, so every query of
 // a tile has two threads, which split its encoding and its hidden-layer
 // epilogues; the first of the two evaluates the vMF head (and draws from it).
@@ -476,7 +566,8 @@ __global__ void __launch_bounds__(256) guide_infer_kernel(GuideDev G, GdQueue Q,
   unsigned char* sw = smem;
   unsigned char* sx = smem + GD_B_FWD;
   unsigned char* sh = sx + GD_TILE * GD_IN * 2;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(sh + GD_TILE * GD_H * 2);
+  float* xch = reinterpret_cast<float*>(smem + GI_XCH);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + GI_XCH + 10 * GD_TILE * 4);
   uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 2);
   const uint32_t tid = threadIdx.x, warp = tid >> 5;
   const uint32_t quad = warp & 3u, half = warp >> 2;
@@ -544,34 +635,87 @@ __global__ void __launch_bounds__(256) guide_infer_kernel(GuideDev G, GdQueue Q,
     else hidden_epilogue_half<32, false>(trow, sh, nullptr, row);
     ok = run_mma(bm, phase, [&] { mma_gemm(tmem, a_h, b_w + GD_B_W4, GD_H, GD_OUTP, false); });
     if (!ok) break;
-    if (half == 0) {
-      float o[GD_OUTP];
-      tmem_ld16(trow, o);
-      tmem_ld16(trow + 16u, o + 16);
-      tmem_ld16(trow + 32u, o + 32);
-      tc_fence_before();  // the next tile's MMAs overwrite these columns after a barrier
-      if (valid) {
-        if (SRC == SRC_ARRAY) {
+    if (SRC == SRC_ARRAY) {
+      if (half == 0) {
+        float o[GD_OUTP];
+        tmem_ld16(trow, o);
+        tmem_ld16(trow + 16u, o + 16);
+        tmem_ld16(trow + 32u, o + 32);
+        if (valid) {
 #pragma unroll
           for (int i = 0; i < GD_OUT; ++i) A.out[(size_t)GD_OUT * qi + i] = o[i];
-        } else {
-          Mix m;
-          make_mix(o, m);
-          const float4 hv = Q.hit[slot];
-          float x = hv.x, y = hv.y, z = hv.z;
-          if (hv.w != 0.0f) {  // this bounce samples the guide
-            const uint2 k = Q.key[slot];
-            clvd::Rng rng;
-            rng.key = (uint64_t)k.x | ((uint64_t)k.y << 32);
-            rng.counter = Q.meta[slot].z;
-            const float u0 = rng.f32(), u1 = rng.f32(), u2 = rng.f32();
-            mix_sample(m, u0, u1, u2, x, y, z);
-            Q.meta[slot].z = rng.counter;
-          }
-          float v[GD_LOBES];
-          const float q = mix_pdf(m, x, y, z, v);
-          Q.hit[slot] = make_float4(x, y, z, q);
         }
+      }
+      tc_fence_before();  // the next tile's MMAs overwrite these columns after a barrier
+    } else {
+      // the head: lobes 0-3 (half 0) or 4-7 (half 1); every thread takes part (uniform barriers)
+      float o32[32];
+      tmem_ld16(trow + 16u * half, o32);
+      tmem_ld16(trow + 16u * half + 16u, o32 + 16);
+      tc_fence_before();
+      Mix4 m;
+      make_mix4(o32 + 4 * half, m, xch, row, half);
+      const float4 hv = valid ? Q.hit[slot] : make_float4(0.0f, 0.0f, 1.0f, 0.0f);
+      const bool guided = valid && hv.w != 0.0f;  // this bounce samples the guide
+      clvd::Rng rng;
+      float u0 = 0.0f, u1 = 0.0f, u2 = 0.0f;
+      if (guided) {
+        const uint2 k = Q.key[slot];
+        rng.key = (uint64_t)k.x | ((uint64_t)k.y << 32);
+        rng.counter = Q.meta[slot].z;
+        u0 = rng.f32();
+        u1 = rng.f32();
+        u2 = rng.f32();
+      }
+      // lobe choice by u0 over the cumulative weights in lobe order (as mix_sample): the first
+      // half's running sum, or -1 if it already chose, goes to the second half
+      float acc = 0.0f;
+      int pick = -1;
+      float* xs = xch + 4 * GD_TILE;  // [row]: first half's sum or -1
+      if (half == 0) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          acc += m.w[k];
+          if (pick < 0 && u0 < acc) pick = k;
+        }
+        xs[row] = pick >= 0 ? -1.0f : acc;
+      }
+      __syncthreads();
+      if (half == 1) {
+        const float a0 = xs[row];
+        if (a0 >= 0.0f) {
+          acc = a0;
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {  // lobes 4..6; lobe 7 takes the rest
+            acc += m.w[k];
+            if (pick < 0 && u0 < acc) pick = k;
+          }
+          if (pick < 0) pick = 3;
+        }
+      }
+      float* xd = xch + 5 * GD_TILE;  // [3][row]: the sampled direction from the half that owns the lobe
+      if (guided && pick >= 0) {
+        float x, y, z;
+        vmf_sample(m.mu[pick][0], m.mu[pick][1], m.mu[pick][2], m.kap[pick], u1, u2, x, y, z);
+        xd[row] = x;
+        xd[GD_TILE + row] = y;
+        xd[2 * GD_TILE + row] = z;
+      }
+      __syncthreads();
+      float x = hv.x, y = hv.y, z = hv.z;
+      if (guided) {
+        x = xd[row];
+        y = xd[GD_TILE + row];
+        z = xd[2 * GD_TILE + row];
+      }
+      float qh = 0.0f;
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        qh += m.w[k] * (m.nrm[k] * expf(m.kap[k] * (m.mu[k][0] * x + m.mu[k][1] * y + m.mu[k][2] * z - 1.0f)));
+      const float q = pair_exchange(xch + 8 * GD_TILE, row, half, qh, false);
+      if (half == 0 && valid) {
+        Q.hit[slot] = make_float4(x, y, z, q);
+        if (guided) Q.meta[slot].z = rng.counter;
       }
     }
   }
@@ -600,7 +744,8 @@ namespace gd {
 #define GT_ZT (GT_A + GD_TILE * GD_H * 2)        // dZ^T (64 x 128); as an M = 128 operand its rows
                                                  // 64..127 read on into GT_HT (lanes never read back)
 #define GT_HT (GT_ZT + GD_H * GD_TILE * 2)       // H1^T, H2^T, H3^T (64 x 128 each)
-#define GT_BAR (GT_HT + 3 * GD_H * GD_TILE * 2)  // mbarriers, TMEM address
+#define GT_XCH (GT_HT + 3 * GD_H * GD_TILE * 2)  // head exchange of the two threads of a row: 3 x 256 floats
+#define GT_BAR (GT_XCH + 3 * 2 * GD_TILE * 4)    // mbarriers, TMEM address
 #define GD_SMEM_TRAIN (GT_BAR + 64)
 #define GT_HT_BYTES (GD_H * GD_TILE * 2)
 // TMEM columns of the training kernel (512 allocated)
@@ -641,8 +786,8 @@ __device__ __forceinline__ void backward_epilogue(uint32_t trow, uint64_t mask, 
 // grad (sums, fp32) and the loss sum into *loss.  Eight warps: warps w and
 // w + 4 read the same TMEM lanes (rows 32 (w mod 4) ..), so every row of a
 // tile has two threads, which split its encoding (inputs 0-3 | 4-6 and the
-// raw inputs) and its hidden-layer epilogues (units 0-31 | 32-63); the
-// first of the two evaluates the vMF head and its gradient.
+// raw inputs), its hidden-layer epilogues (units 0-31 | 32-63) and the vMF
+// head and its gradient (lobes 0-3 | 4-7).
 __global__ void __launch_bounds__(256, 1) guide_train_kernel(const unsigned char* __restrict__ wblob,
                                                              const float4* __restrict__ rec, uint32_t n,
                                                              float* __restrict__ grad, double* __restrict__ loss,
@@ -653,6 +798,7 @@ __global__ void __launch_bounds__(256, 1) guide_train_kernel(const unsigned char
   unsigned char* sa = smem + GT_A;
   unsigned char* szt = smem + GT_ZT;
   unsigned char* sht = smem + GT_HT;
+  float* xch = reinterpret_cast<float*>(smem + GT_XCH);
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + GT_BAR);
   uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 2);
   const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -690,11 +836,9 @@ __global__ void __launch_bounds__(256, 1) guide_train_kernel(const unsigned char
       const float4 a = rec[GD_REC_F4 * (size_t)r], b = rec[GD_REC_F4 * (size_t)r + 1];
       u[0] = a.x; u[1] = a.y; u[2] = a.z; u[3] = a.w;
       u[4] = b.x; u[5] = b.y; u[6] = b.z;
-      if (half == 0) {
-        const float4 c = rec[GD_REC_F4 * (size_t)r + 2];
-        wx = c.x; wy = c.y; wz = c.z;
-        f = (c.w > 0.0f && c.w < 3.0e38f) ? c.w : 0.0f;
-      }
+      const float4 c = rec[GD_REC_F4 * (size_t)r + 2];
+      wx = c.x; wy = c.y; wz = c.z;
+      f = (c.w > 0.0f && c.w < 3.0e38f) ? c.w : 0.0f;
     }
     // forward
     if (half == 0) encode_row_part<0, 4, false>(sx, row, u);
@@ -714,27 +858,48 @@ __global__ void __launch_bounds__(256, 1) guide_train_kernel(const unsigned char
     else m3 = hidden_epilogue_half<32>(trow + GT_DF, sa, sht + 2 * GT_HT_BYTES, row);
     ok = run_mma(bm, phase, [&] { mma_gemm(tmem + GT_DF, a_a, b_w + GD_B_W4, GD_H, GD_OUTP, false); });
     if (!ok) break;
-    if (half == 0) {
-      float o[GD_OUTP];
-      tmem_ld16(trow + GT_DF, o);
-      tmem_ld16(trow + GT_DF + 16u, o + 16);
-      tmem_ld16(trow + GT_DF + 32u, o + 32);
-      // loss gradient of the head
-      float d[GD_OUTP];
+    {  // the head: lobes 0-3 (half 0) or 4-7 (half 1), outputs 20 half .. 20 half + 19
+      float o32[32];
+      tmem_ld16(trow + GT_DF + 16u * half, o32);
+      tmem_ld16(trow + GT_DF + 16u * half + 16u, o32 + 16);
+      const float* o = o32 + 4 * half;  // output 20 half + j at o[j]
+      float d[20];
 #pragma unroll
-      for (int i = 0; i < GD_OUTP; ++i) d[i] = 0.0f;
+      for (int i = 0; i < 20; ++i) d[i] = 0.0f;
+      Mix4 m;
+      make_mix4(o, m, xch, row, half);
+      const float l = mix_grad4(m, wx, wy, wz, f, d, xch, row, half);
       if (f > 0.0f) {
-        Mix m;
-        make_mix(o, m);
-        lsum += (double)mix_grad(m, wx, wy, wz, f, d);
+        if (half == 0) lsum += (double)l;
+      } else {
+#pragma unroll
+        for (int i = 0; i < 20; ++i) d[i] = 0.0f;
       }
+      // dO row (K = 48, chunks of 8 outputs) and column `row` of dO^T; outputs 40..47 are zero
+      if (half == 0) {
 #pragma unroll
-      for (int c = 0; c < GD_OUTP / 8; ++c)
-        *reinterpret_cast<uint4*>(sa + gd_cofs(row, 8 * c, GD_OUTP)) =
-            make_uint4(pack_bf16(d[8 * c], d[8 * c + 1]), pack_bf16(d[8 * c + 2], d[8 * c + 3]),
-                       pack_bf16(d[8 * c + 4], d[8 * c + 5]), pack_bf16(d[8 * c + 6], d[8 * c + 7]));
+        for (int c = 0; c < 2; ++c)
+          *reinterpret_cast<uint4*>(sa + gd_cofs(row, 8 * c, GD_OUTP)) =
+              make_uint4(pack_bf16(d[8 * c], d[8 * c + 1]), pack_bf16(d[8 * c + 2], d[8 * c + 3]),
+                         pack_bf16(d[8 * c + 4], d[8 * c + 5]), pack_bf16(d[8 * c + 6], d[8 * c + 7]));
 #pragma unroll
-      for (int i = 0; i < GD_OUTP; ++i) st_bf16(szt + gd_cofs(i, row, GD_TILE), d[i]);
+        for (int i = 16; i < 20; ++i) st_bf16(sa + gd_cofs(row, i, GD_OUTP), d[i]);
+#pragma unroll
+        for (int i = 0; i < 20; ++i) st_bf16(szt + gd_cofs(i, row, GD_TILE), d[i]);
+      } else {
+        float e[28];  // outputs 20..47
+#pragma unroll
+        for (int i = 0; i < 28; ++i) e[i] = i < 20 ? d[i] : 0.0f;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) st_bf16(sa + gd_cofs(row, 20 + i, GD_OUTP), e[i]);
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+          *reinterpret_cast<uint4*>(sa + gd_cofs(row, 24 + 8 * c, GD_OUTP)) =
+              make_uint4(pack_bf16(e[4 + 8 * c], e[5 + 8 * c]), pack_bf16(e[6 + 8 * c], e[7 + 8 * c]),
+                         pack_bf16(e[8 + 8 * c], e[9 + 8 * c]), pack_bf16(e[10 + 8 * c], e[11 + 8 * c]));
+#pragma unroll
+        for (int i = 0; i < 28; ++i) st_bf16(szt + gd_cofs(20 + i, row, GD_TILE), e[i]);
+      }
     }
     // dH3 = dO W4 ; dW4 += dO^T H3
     ok = run_mma(bm, phase, [&] {
