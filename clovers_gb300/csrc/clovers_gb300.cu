@@ -1429,8 +1429,10 @@ static int render_batch(clv_device_scene* const* ds, const clv_render_opts* opts
     std::vector<unsigned long long> prefix(n + 1, 0ull);
     std::vector<double*> fl(n);
     uint32_t levels = 0;  // bit L: some scene needs traversal level L
+    bool any_wt = false;  // some scene uses the watertight triangle test
     for (uint32_t j = 0; j < n; ++j) {
       const uint32_t k = order[j];
+      any_wt = any_wt || ds[k]->view.watertight != 0;
       views[j] = ds[k]->view;
       fl[j] = films[k];
       const clv_render_opts& o = opts[k];
@@ -1529,16 +1531,25 @@ static int render_batch(clv_device_scene* const* ds, const clv_render_opts* opts
         // one intersect launch per traversal level present, each over its own scenes' slots
         // (a batch with a tree deeper than CLV_STACK levels: one generic launch with a spilling stack)
         const int only = nlevels > 1 ? 0 : -1;
-        if (spill_entries)
+        // triangle test fixed at compile time when no scene of the batch is watertight (the common case)
+#define CLV_BISECT(L, WTM, O) wf_intersect<L, false, true, WTM><<<grid, block, 0, s>>>(S0, W, C, d0->err, nullptr, B, O)
+        if (spill_entries) {
           wf_intersect<2, false, true, CLV_WT_SCENE, true><<<grid, block, 0, s>>>(S0, W, C, d0->err, nullptr, B, -1);
-        else if (levels & 1u)
-          wf_intersect<0, false, true, CLV_WT_SCENE><<<grid, block, 0, s>>>(S0, W, C, d0->err, nullptr, B, only);
-        if (!spill_entries && (levels & 2u))
-          wf_intersect<1, false, true, CLV_WT_SCENE><<<grid, block, 0, s>>>(S0, W, C, d0->err, nullptr, B,
-                                                                            only < 0 ? -1 : 1);
-        if (!spill_entries && (levels & 4u))
-          wf_intersect<2, false, true, CLV_WT_SCENE><<<grid, block, 0, s>>>(S0, W, C, d0->err, nullptr, B,
-                                                                            only < 0 ? -1 : 2);
+        } else {
+          if (levels & 1u) {
+            if (any_wt) CLV_BISECT(0, CLV_WT_SCENE, only);
+            else CLV_BISECT(0, CLV_WT_OFF, only);
+          }
+          if (levels & 2u) {
+            if (any_wt) CLV_BISECT(1, CLV_WT_SCENE, only < 0 ? -1 : 1);
+            else CLV_BISECT(1, CLV_WT_OFF, only < 0 ? -1 : 1);
+          }
+          if (levels & 4u) {
+            if (any_wt) CLV_BISECT(2, CLV_WT_SCENE, only < 0 ? -1 : 2);
+            else CLV_BISECT(2, CLV_WT_OFF, only < 0 ? -1 : 2);
+          }
+        }
+#undef CLV_BISECT
         wf_shade_specular<true><<<qgrid, block, 0, s>>>(S0, P0, W, C, d0->err, B);
         wf_shade_diffuse<true><<<qgrid, block, 0, s>>>(S0, P0, W, C, d0->err, B);
         if (guide) {

@@ -193,15 +193,18 @@ __device__ __forceinline__ void encode_col(unsigned char* tile, uint32_t col, co
   st_bf16(tile + gd_cofs(175, col, GD_TILE), 1.0f);
 }
 
-// Part of a row of the encoded-input tile: the features of inputs [J0, J1)
-// and, with RAW, the raw inputs and the constant 1 (columns 168..175).  Two
-// threads share a row in the training kernel, one part each.
-template <int J0, int J1, bool RAW>
-__device__ __forceinline__ void encode_row_part(unsigned char* tile, uint32_t row, const float u[7]) {
-#pragma unroll
-  for (int j = J0; j < J1; ++j) {
+// Half of a row of the encoded-input tile (two threads share a row): half 0
+// the features of inputs 0-3, half 1 those of inputs 4-6 and the raw inputs
+// with the constant 1 (columns 168..175).  Both halves run the same code.
+__device__ __forceinline__ float input_j(const float u[7], int j) {
+  return j == 0 ? u[0] : j == 1 ? u[1] : j == 2 ? u[2] : j == 3 ? u[3] : j == 4 ? u[4] : j == 5 ? u[5] : u[6];
+}
+__device__ __forceinline__ void encode_row_half(unsigned char* tile, uint32_t row, const float u[7], uint32_t half) {
+  const int j0 = half ? 4 : 0, j1 = half ? 7 : 4;
+#pragma unroll 1
+  for (int j = j0; j < j1; ++j) {
     float v[24];
-    freq_row(u[j], v);
+    freq_row(input_j(u, j), v);
 #pragma unroll
     for (int ch = 0; ch < 3; ++ch) {
       const uint4 w = make_uint4(pack_bf16(v[8 * ch], v[8 * ch + 1]), pack_bf16(v[8 * ch + 2], v[8 * ch + 3]),
@@ -209,23 +212,23 @@ __device__ __forceinline__ void encode_row_part(unsigned char* tile, uint32_t ro
       *reinterpret_cast<uint4*>(tile + gd_cofs(row, 24 * j + 8 * ch, GD_IN)) = w;
     }
   }
-  if (RAW) {
+  if (half) {
     const uint4 w = make_uint4(pack_bf16(u[0], u[1]), pack_bf16(u[2], u[3]), pack_bf16(u[4], u[5]),
                                pack_bf16(u[6], 1.0f));
     *reinterpret_cast<uint4*>(tile + gd_cofs(row, 168, GD_IN)) = w;
   }
 }
-// The same part of column `col` of the transposed tile.
-template <int J0, int J1, bool RAW>
-__device__ __forceinline__ void encode_col_part(unsigned char* tile, uint32_t col, const float u[7]) {
-#pragma unroll
-  for (int j = J0; j < J1; ++j) {
+// The same half of column `col` of the transposed tile.
+__device__ __forceinline__ void encode_col_half(unsigned char* tile, uint32_t col, const float u[7], uint32_t half) {
+  const int j0 = half ? 4 : 0, j1 = half ? 7 : 4;
+#pragma unroll 1
+  for (int j = j0; j < j1; ++j) {
     float v[24];
-    freq_row(u[j], v);
+    freq_row(input_j(u, j), v);
 #pragma unroll
     for (int e = 0; e < 24; ++e) st_bf16(tile + gd_cofs(24 * j + e, col, GD_TILE), v[e]);
   }
-  if (RAW) {
+  if (half) {
 #pragma unroll
     for (int j = 0; j < 7; ++j) st_bf16(tile + gd_cofs(168 + j, col, GD_TILE), u[j]);
     st_bf16(tile + gd_cofs(175, col, GD_TILE), 1.0f);
@@ -417,15 +420,16 @@ __device__ __forceinline__ uint64_t hidden_epilogue(uint32_t trow, unsigned char
   return mask;
 }
 
-// Half of hidden_epilogue: columns [C0, C0 + 32) of this thread's row; the
-// returned mask holds bit u - C0 for each unit u > 0.
-template <int C0, bool TT = true>
-__device__ __forceinline__ uint32_t hidden_epilogue_half(uint32_t trow, unsigned char* a_tile, unsigned char* t_tile,
-                                                         uint32_t row) {
+// Half of hidden_epilogue: columns [c0, c0 + 32) of this thread's row (c0 =
+// 0 or 32), out of line so that the three layers and both halves share one
+// copy of the code; t_tile (optional) receives the transposed copy.  The
+// returned mask holds bit u - c0 for each unit u > 0.
+__device__ __noinline__ uint32_t hidden_epilogue_half(uint32_t trow, unsigned char* a_tile, unsigned char* t_tile,
+                                                      uint32_t row, uint32_t c0) {
   uint32_t mask = 0;
 #pragma unroll
-  for (int cc = 0; cc < 2; ++cc) {
-    const int c = C0 / 16 + cc;
+  for (uint32_t cc = 0; cc < 2; ++cc) {
+    const uint32_t c = c0 / 16 + cc;
     float v[16];
     tmem_ld16(trow + 16u * c, v);
 #pragma unroll
@@ -441,7 +445,7 @@ __device__ __forceinline__ uint32_t hidden_epilogue_half(uint32_t trow, unsigned
       *reinterpret_cast<uint4*>(a_tile + gd_cofs(row, 16 * c + 8 * hh, GD_H)) =
           make_uint4(pack_bf16(p[0], p[1]), pack_bf16(p[2], p[3]), pack_bf16(p[4], p[5]), pack_bf16(p[6], p[7]));
     }
-    if (TT) {
+    if (t_tile) {
 #pragma unroll
       for (int i = 0; i < 16; ++i) st_bf16(t_tile + gd_cofs(16 * c + i, row, GD_TILE), v[i]);
     }
@@ -449,17 +453,16 @@ __device__ __forceinline__ uint32_t hidden_epilogue_half(uint32_t trow, unsigned
   return mask;
 }
 // Half of backward_epilogue over the same columns (mask from hidden_epilogue_half).
-template <int C0>
-__device__ __forceinline__ void backward_epilogue_half(uint32_t trow, uint32_t mask, unsigned char* a_tile,
-                                                       unsigned char* t_tile, uint32_t row) {
+__device__ __noinline__ void backward_epilogue_half(uint32_t trow, uint32_t mask, unsigned char* a_tile,
+                                                    unsigned char* t_tile, uint32_t row, uint32_t c0) {
 #pragma unroll
-  for (int cc = 0; cc < 2; ++cc) {
-    const int c = C0 / 16 + cc;
+  for (uint32_t cc = 0; cc < 2; ++cc) {
+    const uint32_t c = c0 / 16 + cc;
     float v[16];
     tmem_ld16(trow + 16u * c, v);
 #pragma unroll
     for (int i = 0; i < 16; ++i) {
-      const int unit = 16 * c + i;
+      const uint32_t unit = 16 * c + i;
       v[i] = (unit != GD_H - 1 && ((mask >> (16 * cc + i)) & 1u)) ? v[i] : 0.0f;
     }
     if (a_tile) {
@@ -594,45 +597,73 @@ __global__ void __launch_bounds__(256) guide_infer_kernel(GuideDev G, GdQueue Q,
   bool ok = __syncthreads_and(mbar_wait(bw, 0)) != 0;
   uint32_t phase = 0;
   const uint32_t a_x = smem_u32(sx), a_h = smem_u32(sh), b_w = smem_u32(sw);
+  // The inputs of a tile (and, for queued queries, the slot's direction record, key and
+  // random-stream position), loaded one tile ahead so that their latency overlaps the
+  // current tile's MMAs and epilogues.
+  struct In {
+    float u[7];
+    uint32_t slot, ctr;
+    bool valid;
+    float4 hv;
+    uint2 key;
+  };
+  auto load = [&](uint32_t tile, In& x) {
+    const uint32_t qi = tile * GD_TILE + row;
+    x.valid = tile < ntiles && qi < n;
+#pragma unroll
+    for (int j = 0; j < 7; ++j) x.u[j] = 0.0f;
+    x.slot = 0;
+    x.ctr = 0;
+    x.hv = make_float4(0.0f, 0.0f, 1.0f, 0.0f);
+    x.key = make_uint2(0u, 0u);
+    if (!x.valid) return;
+    if (SRC == SRC_QUEUE) {
+      const uint32_t slot = Q.queue[qi];
+      x.slot = slot;
+      const float4 f0 = Q.full[3 * slot];
+      const float4 dl = Q.d_lambda[slot];
+      const uint4 mt = Q.meta[slot];
+      x.ctr = mt.z;
+      x.hv = Q.hit[slot];
+      x.key = Q.key[slot];
+      float lo[3], inv[3];
+      gd_box(G, mt.w, lo, inv);
+      x.u[0] = sat((f0.x - lo[0]) * inv[0]);
+      x.u[1] = sat((f0.y - lo[1]) * inv[1]);
+      x.u[2] = sat((f0.z - lo[2]) * inv[2]);
+      x.u[3] = sat(0.5f - 0.5f * dl.x);  // outgoing direction = -ray direction
+      x.u[4] = sat(0.5f - 0.5f * dl.y);
+      x.u[5] = sat(0.5f - 0.5f * dl.z);
+      x.u[6] = ((float)__float_as_int(dl.w) - 380.0f) * 0.0025f;
+    } else {
+      const float4 a = A.in[2 * qi], b = A.in[2 * qi + 1];
+      x.u[0] = a.x; x.u[1] = a.y; x.u[2] = a.z; x.u[3] = a.w;
+      x.u[4] = b.x; x.u[5] = b.y; x.u[6] = b.z;
+    }
+  };
+  In cur;
+  load(blockIdx.x, cur);
   for (uint32_t tile = blockIdx.x; ok && tile < ntiles; tile += gridDim.x) {
     const uint32_t qi = tile * GD_TILE + row;
-    const bool valid = qi < n;
-    float u[7] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-    uint32_t slot = 0;
-    if (valid) {
-      if (SRC == SRC_QUEUE) {
-        slot = Q.queue[qi];
-        const float4 f0 = Q.full[3 * slot];
-        const float4 dl = Q.d_lambda[slot];
-        float lo[3], inv[3];
-        gd_box(G, G.boxes ? Q.meta[slot].w : 0u, lo, inv);
-        u[0] = sat((f0.x - lo[0]) * inv[0]);
-        u[1] = sat((f0.y - lo[1]) * inv[1]);
-        u[2] = sat((f0.z - lo[2]) * inv[2]);
-        u[3] = sat(0.5f - 0.5f * dl.x);  // outgoing direction = -ray direction
-        u[4] = sat(0.5f - 0.5f * dl.y);
-        u[5] = sat(0.5f - 0.5f * dl.z);
-        u[6] = ((float)__float_as_int(dl.w) - 380.0f) * 0.0025f;
-      } else {
-        const float4 a = A.in[2 * qi], b = A.in[2 * qi + 1];
-        u[0] = a.x; u[1] = a.y; u[2] = a.z; u[3] = a.w;
-        u[4] = b.x; u[5] = b.y; u[6] = b.z;
-      }
-    }
-    if (half == 0) encode_row_part<0, 4, false>(sx, row, u);
-    else encode_row_part<4, 7, true>(sx, row, u);
+    const bool valid = cur.valid;
+    const uint32_t slot = cur.slot;
+    float u[7];
+#pragma unroll
+    for (int j = 0; j < 7; ++j) u[j] = cur.u[j];
+    const float4 hv_cur = cur.hv;
+    const uint2 key_cur = cur.key;
+    const uint32_t ctr_cur = cur.ctr;
+    load(tile + gridDim.x, cur);  // next tile, in flight during this one
+    encode_row_half(sx, row, u, half);
     ok = run_mma(bm, phase, [&] { mma_gemm(tmem, a_x, b_w + GD_B_W1, GD_IN, GD_H, false); });
     if (!ok) break;
-    if (half == 0) hidden_epilogue_half<0, false>(trow, sh, nullptr, row);
-    else hidden_epilogue_half<32, false>(trow, sh, nullptr, row);
+    hidden_epilogue_half(trow, sh, nullptr, row, 32u * half);
     ok = run_mma(bm, phase, [&] { mma_gemm(tmem, a_h, b_w + GD_B_W2, GD_H, GD_H, false); });
     if (!ok) break;
-    if (half == 0) hidden_epilogue_half<0, false>(trow, sh, nullptr, row);
-    else hidden_epilogue_half<32, false>(trow, sh, nullptr, row);
+    hidden_epilogue_half(trow, sh, nullptr, row, 32u * half);
     ok = run_mma(bm, phase, [&] { mma_gemm(tmem, a_h, b_w + GD_B_W3, GD_H, GD_H, false); });
     if (!ok) break;
-    if (half == 0) hidden_epilogue_half<0, false>(trow, sh, nullptr, row);
-    else hidden_epilogue_half<32, false>(trow, sh, nullptr, row);
+    hidden_epilogue_half(trow, sh, nullptr, row, 32u * half);
     ok = run_mma(bm, phase, [&] { mma_gemm(tmem, a_h, b_w + GD_B_W4, GD_H, GD_OUTP, false); });
     if (!ok) break;
     if (SRC == SRC_ARRAY) {
@@ -655,14 +686,13 @@ __global__ void __launch_bounds__(256) guide_infer_kernel(GuideDev G, GdQueue Q,
       tc_fence_before();
       Mix4 m;
       make_mix4(o32 + 4 * half, m, xch, row, half);
-      const float4 hv = valid ? Q.hit[slot] : make_float4(0.0f, 0.0f, 1.0f, 0.0f);
+      const float4 hv = hv_cur;
       const bool guided = valid && hv.w != 0.0f;  // this bounce samples the guide
       clvd::Rng rng;
       float u0 = 0.0f, u1 = 0.0f, u2 = 0.0f;
       if (guided) {
-        const uint2 k = Q.key[slot];
-        rng.key = (uint64_t)k.x | ((uint64_t)k.y << 32);
-        rng.counter = Q.meta[slot].z;
+        rng.key = (uint64_t)key_cur.x | ((uint64_t)key_cur.y << 32);
+        rng.counter = ctr_cur;
         u0 = rng.f32();
         u1 = rng.f32();
         u2 = rng.f32();
@@ -841,21 +871,17 @@ __global__ void __launch_bounds__(256, 1) guide_train_kernel(const unsigned char
       f = (c.w > 0.0f && c.w < 3.0e38f) ? c.w : 0.0f;
     }
     // forward
-    if (half == 0) encode_row_part<0, 4, false>(sx, row, u);
-    else encode_row_part<4, 7, true>(sx, row, u);
+    encode_row_half(sx, row, u, half);
     ok = run_mma(bm, phase, [&] { mma_gemm(tmem + GT_DF, a_x, b_w + GD_B_W1, GD_IN, GD_H, false); });
     if (!ok) break;
     uint32_t m1, m2, m3;
-    if (half == 0) m1 = hidden_epilogue_half<0>(trow + GT_DF, sa, sht, row);
-    else m1 = hidden_epilogue_half<32>(trow + GT_DF, sa, sht, row);
+    m1 = hidden_epilogue_half(trow + GT_DF, sa, sht, row, 32u * half);
     ok = run_mma(bm, phase, [&] { mma_gemm(tmem + GT_DF, a_a, b_w + GD_B_W2, GD_H, GD_H, false); });
     if (!ok) break;
-    if (half == 0) m2 = hidden_epilogue_half<0>(trow + GT_DF, sa, sht + GT_HT_BYTES, row);
-    else m2 = hidden_epilogue_half<32>(trow + GT_DF, sa, sht + GT_HT_BYTES, row);
+    m2 = hidden_epilogue_half(trow + GT_DF, sa, sht + GT_HT_BYTES, row, 32u * half);
     ok = run_mma(bm, phase, [&] { mma_gemm(tmem + GT_DF, a_a, b_w + GD_B_W3, GD_H, GD_H, false); });
     if (!ok) break;
-    if (half == 0) m3 = hidden_epilogue_half<0>(trow + GT_DF, sa, sht + 2 * GT_HT_BYTES, row);
-    else m3 = hidden_epilogue_half<32>(trow + GT_DF, sa, sht + 2 * GT_HT_BYTES, row);
+    m3 = hidden_epilogue_half(trow + GT_DF, sa, sht + 2 * GT_HT_BYTES, row, 32u * half);
     ok = run_mma(bm, phase, [&] { mma_gemm(tmem + GT_DF, a_a, b_w + GD_B_W4, GD_H, GD_OUTP, false); });
     if (!ok) break;
     {  // the head: lobes 0-3 (half 0) or 4-7 (half 1), outputs 20 half .. 20 half + 19
@@ -907,27 +933,23 @@ __global__ void __launch_bounds__(256, 1) guide_train_kernel(const unsigned char
       mma_gemm(tmem + GT_DW4, a_zt, a_ht + 2 * GT_HT_BYTES, GD_TILE, GD_H, !first);
     });
     if (!ok) break;
-    if (half == 0) backward_epilogue_half<0>(trow + GT_DB, m3, sa, szt, row);
-    else backward_epilogue_half<32>(trow + GT_DB, m3, sa, szt, row);
+    backward_epilogue_half(trow + GT_DB, m3, sa, szt, row, 32u * half);
     // dH2 = dZ3 W3 ; dW3 += dZ3^T H2
     ok = run_mma(bm, phase, [&] {
       mma_gemm(tmem + GT_DB, a_a, b_w + GD_B_W3T, GD_H, GD_H, false);
       mma_gemm(tmem + GT_DW3, a_zt, a_ht + GT_HT_BYTES, GD_TILE, GD_H, !first);
     });
     if (!ok) break;
-    if (half == 0) backward_epilogue_half<0>(trow + GT_DB, m2, sa, szt, row);
-    else backward_epilogue_half<32>(trow + GT_DB, m2, sa, szt, row);
+    backward_epilogue_half(trow + GT_DB, m2, sa, szt, row, 32u * half);
     // dH1 = dZ2 W2 ; dW2 += dZ2^T H1
     ok = run_mma(bm, phase, [&] {
       mma_gemm(tmem + GT_DB, a_a, b_w + GD_B_W2T, GD_H, GD_H, false);
       mma_gemm(tmem + GT_DW2, a_zt, a_ht, GD_TILE, GD_H, !first);
     });
     if (!ok) break;
-    if (half == 0) backward_epilogue_half<0>(trow + GT_DB, m1, nullptr, szt, row);
-    else backward_epilogue_half<32>(trow + GT_DB, m1, nullptr, szt, row);
+    backward_epilogue_half(trow + GT_DB, m1, nullptr, szt, row, 32u * half);
     // X^T replaces X, whose last reader has completed
-    if (half == 0) encode_col_part<0, 4, false>(sx, row, u);
-    else encode_col_part<4, 7, true>(sx, row, u);
+    encode_col_half(sx, row, u, half);
     // dW1 += dZ1^T X
     ok = run_mma(bm, phase, [&] { mma_gemm(tmem + GT_DW1, a_zt, a_x, GD_TILE, GD_IN, !first); });
     if (!ok) break;
