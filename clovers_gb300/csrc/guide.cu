@@ -360,6 +360,9 @@ __device__ __forceinline__ float mix_grad(const Mix& m, float x, float y, float 
 namespace gd {
 
 // ------------------------------------------------------------- inference --
+#ifndef GD_PREFETCH
+#define GD_PREFETCH 1  // inference loads the next tile's inputs during the current tile
+#endif
 #define GI_XCH (GD_B_FWD + GD_TILE * GD_IN * 2 + GD_TILE * GD_H * 2)  // head exchange: 10 x 128 floats
 #define GD_SMEM_INFER (GI_XCH + 10 * GD_TILE * 4 + 64)
 enum { SRC_QUEUE = 0, SRC_ARRAY = 1 };
@@ -642,8 +645,13 @@ __global__ void __launch_bounds__(256) guide_infer_kernel(GuideDev G, GdQueue Q,
     }
   };
   In cur;
+#if GD_PREFETCH
   load(blockIdx.x, cur);
+#endif
   for (uint32_t tile = blockIdx.x; ok && tile < ntiles; tile += gridDim.x) {
+#if !GD_PREFETCH
+    load(tile, cur);
+#endif
     const uint32_t qi = tile * GD_TILE + row;
     const bool valid = cur.valid;
     const uint32_t slot = cur.slot;
@@ -653,7 +661,9 @@ __global__ void __launch_bounds__(256) guide_infer_kernel(GuideDev G, GdQueue Q,
     const float4 hv_cur = cur.hv;
     const uint2 key_cur = cur.key;
     const uint32_t ctr_cur = cur.ctr;
+#if GD_PREFETCH
     load(tile + gridDim.x, cur);  // next tile, in flight during this one
+#endif
     encode_row_half(sx, row, u, half);
     ok = run_mma(bm, phase, [&] { mma_gemm(tmem, a_x, b_w + GD_B_W1, GD_IN, GD_H, false); });
     if (!ok) break;
@@ -684,8 +694,11 @@ __global__ void __launch_bounds__(256) guide_infer_kernel(GuideDev G, GdQueue Q,
       tmem_ld16(trow + 16u * half, o32);
       tmem_ld16(trow + 16u * half + 16u, o32 + 16);
       tc_fence_before();
+      float o[20];  // output 20 half + j (selected, not indexed: o32 stays in registers)
+#pragma unroll
+      for (int j = 0; j < 20; ++j) o[j] = half ? o32[j + 4] : o32[j];
       Mix4 m;
-      make_mix4(o32 + 4 * half, m, xch, row, half);
+      make_mix4(o, m, xch, row, half);
       const float4 hv = hv_cur;
       const bool guided = valid && hv.w != 0.0f;  // this bounce samples the guide
       clvd::Rng rng;
@@ -725,8 +738,17 @@ __global__ void __launch_bounds__(256) guide_infer_kernel(GuideDev G, GdQueue Q,
       }
       float* xd = xch + 5 * GD_TILE;  // [3][row]: the sampled direction from the half that owns the lobe
       if (guided && pick >= 0) {
+        float mx = 0.0f, my = 0.0f, mz = 1.0f, kp = 1.0f;  // the picked lobe, selected without indexing
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+          if (k == pick) {
+            mx = m.mu[k][0];
+            my = m.mu[k][1];
+            mz = m.mu[k][2];
+            kp = m.kap[k];
+          }
         float x, y, z;
-        vmf_sample(m.mu[pick][0], m.mu[pick][1], m.mu[pick][2], m.kap[pick], u1, u2, x, y, z);
+        vmf_sample(mx, my, mz, kp, u1, u2, x, y, z);
         xd[row] = x;
         xd[GD_TILE + row] = y;
         xd[2 * GD_TILE + row] = z;
@@ -888,7 +910,9 @@ __global__ void __launch_bounds__(256, 1) guide_train_kernel(const unsigned char
       float o32[32];
       tmem_ld16(trow + GT_DF + 16u * half, o32);
       tmem_ld16(trow + GT_DF + 16u * half + 16u, o32 + 16);
-      const float* o = o32 + 4 * half;  // output 20 half + j at o[j]
+      float o[20];  // output 20 half + j (selected, not indexed: o32 stays in registers)
+#pragma unroll
+      for (int j = 0; j < 20; ++j) o[j] = half ? o32[j + 4] : o32[j];
       float d[20];
 #pragma unroll
       for (int i = 0; i < 20; ++i) d[i] = 0.0f;
