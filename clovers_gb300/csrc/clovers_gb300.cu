@@ -1528,21 +1528,20 @@ static int render_batch(clv_device_scene* const* ds, const clv_render_opts* opts
         cudaMemsetAsync(&C->live, 0, 5 * sizeof(unsigned int), s);
         // one intersect launch per traversal level present, each over its own scenes' slots
         // (a batch with a tree deeper than CLV_STACK levels: one generic launch with a spilling stack)
+        // one intersect launch per traversal level present, each over its own scenes' slots
+        // (a batch with a tree deeper than CLV_STACK levels: one generic launch with a spilling stack)
+        const int only = nlevels > 1 ? 0 : -1;
         if (spill_entries) {
           wf_intersect<2, false, true, CLV_WT_SCENE, true><<<grid, block, 0, s>>>(S0, W, C, d0->err, nullptr, B, -1);
-        } else if (nlevels > 1) {  // one launch; each warp takes the variant of its highest level
-          switch (levels) {
-            case 3: wf_intersect_mixed<3><<<grid, block, 0, s>>>(W, C, d0->err, B); break;
-            case 5: wf_intersect_mixed<5><<<grid, block, 0, s>>>(W, C, d0->err, B); break;
-            case 6: wf_intersect_mixed<6><<<grid, block, 0, s>>>(W, C, d0->err, B); break;
-            default: wf_intersect_mixed<7><<<grid, block, 0, s>>>(W, C, d0->err, B); break;
-          }
-        } else if (levels & 1u) {
-          wf_intersect<0, false, true, CLV_WT_SCENE><<<grid, block, 0, s>>>(S0, W, C, d0->err, nullptr, B, -1);
-        } else if (levels & 2u) {
-          wf_intersect<1, false, true, CLV_WT_SCENE><<<grid, block, 0, s>>>(S0, W, C, d0->err, nullptr, B, -1);
         } else {
-          wf_intersect<2, false, true, CLV_WT_SCENE><<<grid, block, 0, s>>>(S0, W, C, d0->err, nullptr, B, -1);
+          if (levels & 1u)
+            wf_intersect<0, false, true, CLV_WT_SCENE><<<grid, block, 0, s>>>(S0, W, C, d0->err, nullptr, B, only);
+          if (levels & 2u)
+            wf_intersect<1, false, true, CLV_WT_SCENE><<<grid, block, 0, s>>>(S0, W, C, d0->err, nullptr, B,
+                                                                              only < 0 ? -1 : 1);
+          if (levels & 4u)
+            wf_intersect<2, false, true, CLV_WT_SCENE><<<grid, block, 0, s>>>(S0, W, C, d0->err, nullptr, B,
+                                                                              only < 0 ? -1 : 2);
         }
         wf_shade_specular<true><<<qgrid, block, 0, s>>>(S0, P0, W, C, d0->err, B);
         wf_shade_diffuse<true><<<qgrid, block, 0, s>>>(S0, P0, W, C, d0->err, B);
@@ -1558,7 +1557,7 @@ static int render_batch(clv_device_scene* const* ds, const clv_render_opts* opts
     for (uint64_t it = 0;; it += batch) {
       if (graph.exec) ck(cudaGraphLaunch(graph.exec, st), "cudaGraphLaunch");
       else bounces(st);
-      g_launches += (4 + (guide ? (alpha > 0.0f ? 3 : 2) : 0)) * batch;
+      g_launches += (3 + (spill_entries ? 1 : nlevels) + (guide ? (alpha > 0.0f ? 3 : 2) : 0)) * batch;
       ck(cudaGetLastError(), "wavefront launch");
       ck(cudaMemcpyAsync(d0->wf_live_host, &C->live, sizeof(unsigned int), cudaMemcpyDeviceToHost, st),
          "cudaMemcpyAsync");

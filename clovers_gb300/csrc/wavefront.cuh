@@ -298,28 +298,6 @@ __global__ void __launch_bounds__(128, CPLX == 1 ? CLV_MINB_CHAIN : CLV_MINB) wf
   if (COUNT) warp_add_counts(cnt, live, c.nodes, c.prims);
 }
 
-// Batches whose scenes need different traversal levels (MASK: bit L = some
-// scene at level L): one launch over all slots, in which each warp runs the
-// variant of the highest level among its lanes' scenes.  A higher variant
-// handles every object of the lower levels with the same arithmetic, so the
-// results are those of the per-level variants; no launch runs empty and no
-// slot is read by launches of other levels.
-template <int MASK>
-__global__ void __launch_bounds__(128, (MASK & 2) ? CLV_MINB_CHAIN : CLV_MINB)
-    wf_intersect_mixed(WfState W, WfCounters* C, uint32_t* err, WfBatch B) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  Counters c{0u, 0u};
-  const uint4 m = i < W.Q ? W.meta[i] : make_uint4(0u, 0u, 0u, 0u);
-  const bool go = (m.w & 1u) != 0u;
-  const ClvDeviceScene& S = B.scenes[go ? m.w >> 8 : 0u];
-  const uint32_t level = __reduce_max_sync(0xFFFFFFFFu, go ? S.compound_level : 0u);  // uniform over the warp
-  int cls;
-  if ((MASK & 4) && level == 2) cls = intersect_slot<2, false, CLV_WT_SCENE>(S, W, err, i, m, go, c);
-  else if ((MASK & 2) && level == 1) cls = intersect_slot<1, false, CLV_WT_SCENE>(S, W, err, i, m, go, c);
-  else cls = intersect_slot<0, false, CLV_WT_SCENE>(S, W, err, i, m, go, c);
-  wf_enqueue_block(W, C, cls, i);
-}
-
 __device__ __forceinline__ bool wf_is_normal_pos(float v) {
   const float a = fabsf(v);
   return v > 0.0f && a >= 1.17549435e-38f && a <= 3.40282347e+38f;
