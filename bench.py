@@ -178,6 +178,12 @@ def run_reference(args, world, rank):
     samples = W_IMG * H_IMG * spp_sample
     value = samples * len(times) / sum(times) / 1e6
     sample = "%dx%d image at %d spp per step (of the workload's %d spp)" % (W_IMG, H_IMG, spp_sample, SPP)
+    rows, spp1 = 16, 16  # one core, beside the all-threads figure: a band of the image
+    t0 = time.perf_counter()
+    sc.render(W_IMG, H_IMG, spp1, DEPTH, SEED, window=(0, H_IMG // 2, W_IMG, H_IMG // 2 + rows), threads=1)
+    el1 = time.perf_counter() - t0
+    one_core = {"value": round(W_IMG * rows * spp1 / el1 / 1e6, 4), "unit": "Msamples/s",
+                "sample": "%d middle rows of %d pixels at %d spp (%.2f s)" % (rows, W_IMG, spp1, el1)}
     line = {
         "impl": "reference", "metric": "Msamples/s", "value": round(value, 4), "unit": "Msamples/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -186,7 +192,7 @@ def run_reference(args, world, rank):
         "config": {"workload": "enclosed box %dx%d, %d spp, depth %d" % (W_IMG, H_IMG, SPP, DEPTH), "sample": sample,
                    "parallelism": "host threads"},
         "cpu_baseline": {"value": round(value, 4), "unit": "Msamples/s", "cores": threads, "kind": "port",
-                         "sample": sample},
+                         "sample": sample, "one_core": one_core},
         "e2e": {"value": round(value, 4), "unit": "Msamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference is Rust and cannot be built here (no rustc/cargo); its algorithm runs as the "
                 "C++ restatement in oracle/, row-parallel over all host threads",
