@@ -476,6 +476,14 @@ def run_config(args):
     build_s = time.perf_counter() - t0
     d = host.upload()
     film = torch.zeros(w * h * 3, dtype=torch.float64, device="cuda")
+    tune = None
+    if not args.no_autotune:  # wavefront shape search on a sixteenth of the samples, before any timing
+        t0 = time.perf_counter()
+        res = d.autotune(cg.RenderOptions(width=w, height=h, samples=max(1, spp // 16), max_depth=depth,
+                                          seed=SEED + 7), stream=sp)
+        best = min(res, key=lambda r: r[3])
+        tune = {"path_slots": best[0], "shade_blocks_per_sm": best[1], "warp_appends": best[2],
+                "candidates": len(res), "tuning_s": round(time.perf_counter() - t0, 3)}
 
     def render(n_spp, offset, seed=SEED):
         o = cg.render_opts(cg.RenderOptions(width=w, height=h, samples=n_spp, max_depth=depth, seed=seed))
@@ -499,7 +507,8 @@ def run_config(args):
             "unit": "Msamples/s",
             "n_gpus": 1, "steps": len(ms), "warmup": args.warmup, "ms_per_step": round(ms_step, 3) if ms else None,
             "higher_is_better": True, "dtype": "f32", "data": "synthetic (seeded generator, reference scene format)",
-            "config": {"workload": desc, "scene_load_and_bvh_s": round(build_s, 3), "objects": host.info()["objects"]}}
+            "config": {"workload": desc, "scene_load_and_bvh_s": round(build_s, 3), "objects": host.info()["objects"],
+                       "autotune": tune}}
     gold = GOLDEN.get(args.config)
     if gold:
         plain, guided = time_to_relmse(args, gold, d, w, h, depth, film, stream, render, args.guided)
@@ -757,9 +766,9 @@ def main():
             t0 = time.perf_counter()
             res = dscene.autotune(cg.RenderOptions(width=W_IMG, height=H_IMG, samples=max(1, SPP // 4),
                                                    max_depth=DEPTH, seed=SEED + 7), stream=sp)
-            best = min(res, key=lambda r: r[2])
-            tune = {"path_slots": best[0], "shade_blocks_per_sm": best[1], "candidates": len(res),
-                    "tuning_s": round(time.perf_counter() - t0, 3)}
+            best = min(res, key=lambda r: r[3])
+            tune = {"path_slots": best[0], "shade_blocks_per_sm": best[1], "warp_appends": best[2],
+                    "candidates": len(res), "tuning_s": round(time.perf_counter() - t0, 3)}
         for w in range(args.warmup):
             film.zero_()
             _lib.check(L.clv_render_device(dscene.handle, ctypes.byref(opts_for(10**6 + w)), film.data_ptr(), sp))

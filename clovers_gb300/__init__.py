@@ -144,12 +144,12 @@ class DeviceScene:
 
     def autotune(self, render_options, stream=None):
         """clv_autotune on a short render: the chosen shape is kept for later
-        renders of this scene; returns [(path_slots, shade_blocks_per_sm, ms)]."""
+        renders of this scene; returns [(path_slots, shade_blocks_per_sm, warp_appends, ms)]."""
         o = render_opts(render_options)
-        res = (_lib.TuneResultC * 32)()
+        res = (_lib.TuneResultC * 64)()
         n = ctypes.c_uint32()
-        check(lib().clv_autotune(self._h, ctypes.byref(o), res, 32, ctypes.byref(n), stream))
-        return [(r.path_slots, r.shade_blocks_per_sm, r.ms) for r in res[:n.value]]
+        check(lib().clv_autotune(self._h, ctypes.byref(o), res, 64, ctypes.byref(n), stream))
+        return [(r.path_slots, r.shade_blocks_per_sm, r.warp_appends, r.ms) for r in res[:n.value]]
 
 
 def render_opts(opts: RenderOptions, sample_offset=0, path_slots=0):

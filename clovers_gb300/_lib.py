@@ -41,7 +41,7 @@ class GuideOptsC(ctypes.Structure):
 
 
 class TuneResultC(ctypes.Structure):
-    _fields_ = [("path_slots", c_u32), ("shade_blocks_per_sm", c_u32), ("ms", c_f32)]
+    _fields_ = [("path_slots", c_u32), ("shade_blocks_per_sm", c_u32), ("warp_appends", c_u32), ("ms", c_f32)]
 
 
 class RenderProfileC(ctypes.Structure):

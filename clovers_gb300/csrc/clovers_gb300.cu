@@ -623,6 +623,7 @@ struct clv_device_scene {
   // wavefront shape chosen by clv_autotune (0: the built-in defaults)
   uint32_t tuned_slots = 0;      // paths in flight
   uint32_t tuned_shade = 0;      // shading-kernel blocks per SM
+  uint32_t tuned_append = 0;     // intersect queue appends per warp (1) or per block (0)
   unsigned long long* ray_next = nullptr;  // work counter of the persistent ray casts
   uint32_t* ray_sort = nullptr;            // ray order: histogram, keys, permutation
   uint64_t ray_sort_cap = 0;               // rays the sort scratch holds
@@ -697,6 +698,7 @@ struct clv_device_scene {
     W.grec_cap = 0;
     W.spill = nullptr;
     W.stack_cap = CLV_STACK;
+    W.warp_append = 0;
     return W;
   }
   static constexpr size_t kWfSlotBytes = 16 * 5 + 48 + 8 + 16;
@@ -847,8 +849,9 @@ int clv_render_profile_run(clv_device_scene* d, const clv_render_opts* o, double
 }
 
 // Times the wavefront render `o` (a short one: a few samples per pixel) for
-// every candidate shape -- paths in flight SMs x {1, 2, 4, 8, 16} x 1024 and
-// shading grids of {8, 16, 32} blocks per SM, the minimum of two runs each --
+// every candidate shape -- paths in flight SMs x {1, 2, 4, 8, 16} x 1024,
+// shading grids of {8, 16, 32} blocks per SM and intersect queue appends per
+// block or per warp, the minimum of two runs each --
 // and keeps the fastest in the scene for later renders that leave path_slots
 // at 0 (clv_render, clv_render_device, clv_render_guided, clv_render_batch
 // with this scene first).
@@ -861,7 +864,7 @@ int clv_autotune(clv_device_scene* d, const clv_render_opts* o, clv_tune_result*
   cudaStream_t st = (cudaStream_t)stream;
   double* film = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
-  const uint32_t old_slots = d->tuned_slots, old_shade = d->tuned_shade;
+  const uint32_t old_slots = d->tuned_slots, old_shade = d->tuned_shade, old_append = d->tuned_append;
   auto cleanup = [&]() {
     if (film) cudaFree(film);
     if (e0) cudaEventDestroy(e0);
@@ -878,11 +881,13 @@ int clv_autotune(clv_device_scene* d, const clv_render_opts* o, clv_tune_result*
     clv_render_opts t = *o;
     t.path_slots = 0;
     float best = 3.0e38f;
-    uint32_t best_slots = 0, best_shade = 0, n = 0;
+    uint32_t best_slots = 0, best_shade = 0, best_append = 0, n = 0;
     for (uint32_t a = 0; a < 5; ++a)
-      for (uint32_t b = 0; b < 3; ++b) {
+      for (uint32_t b = 0; b < 3; ++b)
+        for (uint32_t ap = 0; ap < 2; ++ap) {
         d->tuned_slots = sms * slot_mult[a] * 1024u;
         d->tuned_shade = shade[b];
+        d->tuned_append = ap;
         float ms = 3.0e38f;
         for (int rep = 0; rep < 2; ++rep) {
           ck(cudaMemsetAsync(film, 0, fb, st), "cudaMemsetAsync");
@@ -895,22 +900,25 @@ int clv_autotune(clv_device_scene* d, const clv_render_opts* o, clv_tune_result*
           ck(cudaEventElapsedTime(&m, e0, e1), "cudaEventElapsedTime");
           ms = std::min(ms, m);
         }
-        if (results && n < max_results) results[n] = clv_tune_result{d->tuned_slots, d->tuned_shade, ms};
+        if (results && n < max_results) results[n] = clv_tune_result{d->tuned_slots, d->tuned_shade, ap, ms};
         ++n;
         if (ms < best) {
           best = ms;
           best_slots = d->tuned_slots;
           best_shade = d->tuned_shade;
+          best_append = ap;
         }
       }
     d->tuned_slots = best_slots;
     d->tuned_shade = best_shade;
+    d->tuned_append = best_append;
     if (n_results) *n_results = n;
     cleanup();
     return CLV_OK;
   } catch (std::exception& ex) {
     d->tuned_slots = old_slots;
     d->tuned_shade = old_shade;
+    d->tuned_append = old_append;
     cleanup();
     return fail(CLV_E_CUDA, ex.what());
   }
@@ -1267,6 +1275,7 @@ static int render_wavefront(clv_device_scene* d, const clv_render_opts* o, doubl
       W.spill = d->spill_region((size_t)q * spill_entries * sizeof(float4));
       W.stack_cap = d->view.max_depth_tree;
     }
+    W.warp_append = d->tuned_append;
     WfCounters c0{std::min<uint64_t>(q, P.total), 0u, {0u, 0u, 0u, 0u}};
     ck(cudaMemcpyAsync(d->wf_counters, &c0, sizeof c0, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync");
     GuideDev G{};
@@ -1833,6 +1842,7 @@ extern "C" int clv_render_device_noalloc(clv_device_scene* d, const clv_render_o
   W.grec_cap = 0;
   W.spill = nullptr;
   W.stack_cap = CLV_STACK;
+  W.warp_append = 0;
   const int block = 128;
   const uint32_t grid = (uint32_t)((q + block - 1) / block);
   const uint32_t qgrid =

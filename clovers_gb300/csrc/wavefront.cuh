@@ -40,6 +40,9 @@ struct WfState {
   // beyond CLV_STACK of slot i at spill[(k - CLV_STACK) * Q + i], stack_cap in all
   float4* spill;
   uint32_t stack_cap;
+  // intersect queue appends: 0 one atomic per class and block (two block barriers),
+  // 1 one atomic per class and warp (no barrier); chosen per scene by clv_autotune
+  uint32_t warp_append;
 };
 
 #define WF_Q_FINISH 0  // misses, emitters and paths ended in the shade kernels
@@ -187,6 +190,23 @@ __device__ __forceinline__ void wf_enqueue_block(const WfState& W, WfCounters* C
     W.queue[(size_t)cls * W.Q + pos] = i;
   }
 }
+// Appends each thread's slot i to queue `cls` (cls < 0: nothing) with one
+// atomic per class for the warp and no block barrier; every lane of the warp
+// calls it.  Faster than wf_enqueue_block where traversal lengths within a
+// block vary widely (warps that finish early do not wait at the barrier).
+__device__ __forceinline__ void wf_enqueue_warp(const WfState& W, WfCounters* C, int cls, uint32_t i) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    const unsigned m = __ballot_sync(0xFFFFFFFFu, cls == c);
+    if (!m) continue;
+    const int leader = __ffs(m) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(&C->queue[c], (uint32_t)__popc(m));
+    base = __shfl_sync(0xFFFFFFFFu, base, leader);
+    if (cls == c) W.queue[(size_t)c * W.Q + base + __popc(m & ((1u << lane) - 1u))] = i;
+  }
+}
 // Appends the slots of the threads with `want` to queue `cls`, one atomic for
 // the block; every thread of the 128-thread block calls it, in every round.
 __device__ __forceinline__ void wf_enqueue_block_one(const WfState& W, WfCounters* C, int cls, bool want, uint32_t i) {
@@ -294,7 +314,8 @@ __global__ void __launch_bounds__(128, CPLX == 1 ? CLV_MINB_CHAIN : CLV_MINB) wf
   int cls;
   if constexpr (BATCH) cls = intersect_slot<CPLX, COUNT, WT, DEEP>(B.scenes[go ? m.w >> 8 : 0u], W, err, i, m, go, c);
   else cls = intersect_slot<CPLX, COUNT, WT, DEEP>(S, W, err, i, m, go, c);
-  wf_enqueue_block(W, C, cls, i);
+  if (W.warp_append) wf_enqueue_warp(W, C, cls, i);  // uniform over the launch
+  else wf_enqueue_block(W, C, cls, i);
   if (COUNT) warp_add_counts(cnt, live, c.nodes, c.prims);
 }
 

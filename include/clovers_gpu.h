@@ -163,14 +163,18 @@ int clv_resolve_srgb(const float* xyz, uint32_t width, uint32_t height, uint8_t*
 /* Wavefront shape tuning (no counterpart in the reference; part of the
  * batching and autotuning layer).  Renders `opts` -- pass a short render, a few samples per
  * pixel of the workload to tune for -- twice for each candidate shape: paths
- * in flight (path_slots) SMs x {1, 2, 4, 8, 16} x 1024 and shading grids of
- * {8, 16, 32} blocks per SM, and keeps the fastest in the scene: later
- * wavefront renders of this scene with opts->path_slots = 0 use it.  results
- * (optional) receives up to max_results timings, n_results their count (15).
- * Allocates a film and the largest path state it tries. */
+ * in flight (path_slots) SMs x {1, 2, 4, 8, 16} x 1024, shading grids of
+ * {8, 16, 32} blocks per SM, and the intersect's queue appends per block (one
+ * atomic per class and block, behind two block barriers) or per warp (no
+ * barrier: better where traversal lengths vary widely within a block), and
+ * keeps the fastest in the scene: later wavefront renders of this scene with
+ * opts->path_slots = 0 use it.  results (optional) receives up to max_results
+ * timings, n_results their count (30).  Allocates a film and the largest path
+ * state it tries. */
 typedef struct clv_tune_result {
   uint32_t path_slots;
   uint32_t shade_blocks_per_sm;
+  uint32_t warp_appends;  /* 1: the intersect appends its queues per warp, 0: per block */
   float ms;
 } clv_tune_result;
 int clv_autotune(clv_device_scene* dscene, const clv_render_opts* opts, clv_tune_result* results,

@@ -133,8 +133,9 @@ def test_autotune_keeps_the_image(box_scene_path):
     opts = cg.RenderOptions(width=128, height=128, samples=8, max_depth=8, seed=3)
     before = cg.draw(cg.GlobalOptions(quiet=True), opts, d)
     res = d.autotune(cg.RenderOptions(width=128, height=128, samples=4, max_depth=8, seed=1))
-    assert len(res) == 15 and all(ms > 0 for _, _, ms in res)
-    best = min(res, key=lambda r: r[2])
+    assert len(res) == 30 and all(ms > 0 for _, _, _, ms in res)
+    assert sorted(set(r[2] for r in res)) == [0, 1]
+    best = min(res, key=lambda r: r[3])
     print("autotune: best %s of %d candidates" % (best, len(res)))
     after = cg.draw(cg.GlobalOptions(quiet=True), opts, d)
     # the same random streams give the same paths; only the f64 deposit order may move the last bits
