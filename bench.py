@@ -477,13 +477,16 @@ def run_config(args):
     d = host.upload()
     film = torch.zeros(w * h * 3, dtype=torch.float64, device="cuda")
     tune = None
-    if not args.no_autotune:  # wavefront shape search on a sixteenth of the samples, before any timing
+    if not args.no_autotune:
+        # wavefront shape search before any timing, on a quarter of the samples (a short render is mostly
+        # wavefront tail and favours small shapes), at most 2^27 samples per candidate
         t0 = time.perf_counter()
-        res = d.autotune(cg.RenderOptions(width=w, height=h, samples=max(1, spp // 16), max_depth=depth,
-                                          seed=SEED + 7), stream=sp)
+        tune_spp = max(1, min(spp // 4, (1 << 27) // (w * h)))
+        res = d.autotune(cg.RenderOptions(width=w, height=h, samples=tune_spp, max_depth=depth, seed=SEED + 7),
+                         stream=sp)
         best = min(res, key=lambda r: r[3])
         tune = {"path_slots": best[0], "shade_blocks_per_sm": best[1], "warp_appends": best[2],
-                "candidates": len(res), "tuning_s": round(time.perf_counter() - t0, 3)}
+                "candidates": len(res), "tuning_spp": tune_spp, "tuning_s": round(time.perf_counter() - t0, 3)}
 
     def render(n_spp, offset, seed=SEED):
         o = cg.render_opts(cg.RenderOptions(width=w, height=h, samples=n_spp, max_depth=depth, seed=seed))

@@ -142,6 +142,10 @@ class DeviceScene:
         check(lib().clv_device_status(self._h, ctypes.byref(f)))
         return f.value
 
+    def set_shape(self, path_slots=0, shade_blocks_per_sm=0, warp_appends=0):
+        """clv_device_scene_set_shape: the wavefront shape of later renders (0 = built-in defaults)."""
+        check(lib().clv_device_scene_set_shape(self._h, path_slots, shade_blocks_per_sm, warp_appends))
+
     def autotune(self, render_options, stream=None):
         """clv_autotune on a short render: the chosen shape is kept for later
         renders of this scene; returns [(path_slots, shade_blocks_per_sm, warp_appends, ms)]."""

@@ -66,6 +66,7 @@ SIGNATURES = {
     "clv_render_batch": (c_i32, [ctypes.c_void_p, P(RenderOptsC), ctypes.c_void_p, c_u32, ctypes.c_void_p]),
     "clv_render_device_noalloc": (c_i32, [ctypes.c_void_p, P(RenderOptsC), ctypes.c_void_p, ctypes.c_void_p]),
     "clv_autotune": (c_i32, [ctypes.c_void_p, P(RenderOptsC), ctypes.c_void_p, c_u32, P(c_u32), ctypes.c_void_p]),
+    "clv_device_scene_set_shape": (c_i32, [ctypes.c_void_p, c_u32, c_u32, c_u32]),
     "clv_resolve_device": (c_i32, [ctypes.c_void_p, c_u32, c_u32, c_u32, ctypes.c_void_p, ctypes.c_void_p,
                                    ctypes.c_void_p]),
     "clv_resolve_srgb": (c_i32, [ctypes.c_void_p, c_u32, c_u32, ctypes.c_void_p]),

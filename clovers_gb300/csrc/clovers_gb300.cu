@@ -623,7 +623,7 @@ struct clv_device_scene {
   // wavefront shape chosen by clv_autotune (0: the built-in defaults)
   uint32_t tuned_slots = 0;      // paths in flight
   uint32_t tuned_shade = 0;      // shading-kernel blocks per SM
-  uint32_t tuned_append = 0;     // intersect queue appends per warp (1) or per block (0)
+  uint32_t tuned_append = 0;     // intersect queue appends per warp (1) or per block (0), primitive-level scenes
   unsigned long long* ray_next = nullptr;  // work counter of the persistent ray casts
   uint32_t* ray_sort = nullptr;            // ray order: histogram, keys, permutation
   uint64_t ray_sort_cap = 0;               // rays the sort scratch holds
@@ -698,7 +698,6 @@ struct clv_device_scene {
     W.grec_cap = 0;
     W.spill = nullptr;
     W.stack_cap = CLV_STACK;
-    W.warp_append = 0;
     return W;
   }
   static constexpr size_t kWfSlotBytes = 16 * 5 + 48 + 8 + 16;
@@ -884,7 +883,7 @@ int clv_autotune(clv_device_scene* d, const clv_render_opts* o, clv_tune_result*
     uint32_t best_slots = 0, best_shade = 0, best_append = 0, n = 0;
     for (uint32_t a = 0; a < 5; ++a)
       for (uint32_t b = 0; b < 3; ++b)
-        for (uint32_t ap = 0; ap < 2; ++ap) {
+        for (uint32_t ap = 0; ap < (d->view.compound_level == 0 && !d->deep() ? 2u : 1u); ++ap) {
         d->tuned_slots = sms * slot_mult[a] * 1024u;
         d->tuned_shade = shade[b];
         d->tuned_append = ap;
@@ -922,6 +921,19 @@ int clv_autotune(clv_device_scene* d, const clv_render_opts* o, clv_tune_result*
     cleanup();
     return fail(CLV_E_CUDA, ex.what());
   }
+}
+
+int clv_device_scene_set_shape(clv_device_scene* d, uint32_t path_slots, uint32_t shade_blocks_per_sm,
+                               uint32_t warp_appends) {
+  if (!d) return fail(CLV_E_INVALID, "null argument");
+  if (warp_appends > 1) return fail(CLV_E_INVALID, "warp_appends takes 0 or 1");
+  if (warp_appends && (d->view.compound_level != 0 || d->deep()))
+    return fail(CLV_E_INVALID, "per-warp appends exist for primitive-level scenes of at most 64 BVH levels");
+  if (shade_blocks_per_sm > 64) return fail(CLV_E_INVALID, "shade_blocks_per_sm above 64");
+  d->tuned_slots = path_slots;
+  d->tuned_shade = shade_blocks_per_sm;
+  d->tuned_append = warp_appends;
+  return CLV_OK;
 }
 
 int clv_selftest_division(uint64_t n, uint64_t seed, uint64_t* mismatches) {
@@ -1275,7 +1287,6 @@ static int render_wavefront(clv_device_scene* d, const clv_render_opts* o, doubl
       W.spill = d->spill_region((size_t)q * spill_entries * sizeof(float4));
       W.stack_cap = d->view.max_depth_tree;
     }
-    W.warp_append = d->tuned_append;
     WfCounters c0{std::min<uint64_t>(q, P.total), 0u, {0u, 0u, 0u, 0u}};
     ck(cudaMemcpyAsync(d->wf_counters, &c0, sizeof c0, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync");
     GuideDev G{};
@@ -1321,7 +1332,20 @@ static int render_wavefront(clv_device_scene* d, const clv_render_opts* o, doubl
       if (prof) cudaEventRecord(evs[4 * k], s);
 #define CLV_ISECT(L, N, T) \
   wf_intersect<L, N, false, T><<<grid, block, 0, s>>>(d->view, W, C, d->err, N ? dcnt : nullptr, WfBatch{}, -1)
-      if (spill_entries && prof && count)
+      // per-warp appends (primitive-level scenes only, as tuned)
+      const bool wapp = level == 0 && d->tuned_append && !spill_entries;
+#define CLV_ISECT_W(N, T) \
+  wf_intersect<0, N, false, T, false, true><<<grid, block, 0, s>>>(d->view, W, C, d->err, N ? dcnt : nullptr, WfBatch{}, -1)
+      if (wapp) {
+        const bool cnt = prof && count;
+        if (d->view.watertight) {
+          if (cnt) CLV_ISECT_W(true, CLV_WT_ON);
+          else CLV_ISECT_W(false, CLV_WT_ON);
+        } else {
+          if (cnt) CLV_ISECT_W(true, CLV_WT_OFF);
+          else CLV_ISECT_W(false, CLV_WT_OFF);
+        }
+      } else if (spill_entries && prof && count)
         wf_intersect<2, true, false, CLV_WT_SCENE, true><<<grid, block, 0, s>>>(d->view, W, C, d->err, dcnt,
                                                                                 WfBatch{}, -1);
       else if (spill_entries)
@@ -1342,6 +1366,7 @@ static int render_wavefront(clv_device_scene* d, const clv_render_opts* o, doubl
         default: CLV_ISECT(2, true, CLV_WT_ON); break;
       }
 #undef CLV_ISECT
+#undef CLV_ISECT_W
       if (prof) cudaEventRecord(evs[4 * k + 1], s);
       if (prof) cudaEventRecord(evs[4 * k + 2], s);
       wf_shade_specular<false><<<qgrid, block, 0, s>>>(d->view, P, W, C, d->err, WfBatch{});
@@ -1842,7 +1867,6 @@ extern "C" int clv_render_device_noalloc(clv_device_scene* d, const clv_render_o
   W.grec_cap = 0;
   W.spill = nullptr;
   W.stack_cap = CLV_STACK;
-  W.warp_append = 0;
   const int block = 128;
   const uint32_t grid = (uint32_t)((q + block - 1) / block);
   const uint32_t qgrid =

@@ -40,9 +40,6 @@ struct WfState {
   // beyond CLV_STACK of slot i at spill[(k - CLV_STACK) * Q + i], stack_cap in all
   float4* spill;
   uint32_t stack_cap;
-  // intersect queue appends: 0 one atomic per class and block (two block barriers),
-  // 1 one atomic per class and warp (no barrier); chosen per scene by clv_autotune
-  uint32_t warp_append;
 };
 
 #define WF_Q_FINISH 0  // misses, emitters and paths ended in the shade kernels
@@ -301,7 +298,10 @@ __device__ __forceinline__ int intersect_slot(const ClvDeviceScene& S, const WfS
 // only_level >= 0 (batches): only the slots of scenes at that traversal level,
 // so that a batch runs each scene with the variant its objects need.
 // DEEP: trees deeper than CLV_STACK levels (CPLX 2 only), stack entries spilled to W.spill.
-template <int CPLX, bool COUNT, bool BATCH, int WT, bool DEEP = false>
+// WAPP: queue appends per warp instead of per block (primitive-level scenes that
+// clv_autotune finds faster so; a separate instantiation, because even an unused
+// run-time branch to the warp form slowed the wrapper-chain variant by 11 %).
+template <int CPLX, bool COUNT, bool BATCH, int WT, bool DEEP = false, bool WAPP = false>
 __global__ void __launch_bounds__(128, CPLX == 1 ? CLV_MINB_CHAIN : CLV_MINB) wf_intersect(ClvDeviceScene S, WfState W, WfCounters* C, uint32_t* err,
                                                               unsigned long long* cnt, WfBatch B, int only_level) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -314,7 +314,7 @@ __global__ void __launch_bounds__(128, CPLX == 1 ? CLV_MINB_CHAIN : CLV_MINB) wf
   int cls;
   if constexpr (BATCH) cls = intersect_slot<CPLX, COUNT, WT, DEEP>(B.scenes[go ? m.w >> 8 : 0u], W, err, i, m, go, c);
   else cls = intersect_slot<CPLX, COUNT, WT, DEEP>(S, W, err, i, m, go, c);
-  if (W.warp_append) wf_enqueue_warp(W, C, cls, i);  // uniform over the launch
+  if constexpr (WAPP) wf_enqueue_warp(W, C, cls, i);
   else wf_enqueue_block(W, C, cls, i);
   if (COUNT) warp_add_counts(cnt, live, c.nodes, c.prims);
 }

@@ -180,6 +180,13 @@ typedef struct clv_tune_result {
 int clv_autotune(clv_device_scene* dscene, const clv_render_opts* opts, clv_tune_result* results,
                  uint32_t max_results, uint32_t* n_results, void* stream);
 
+/* Sets the wavefront shape clv_autotune would keep (0 = the built-in default
+ * for path_slots and shade_blocks_per_sm), e.g. to reuse a shape tuned in an
+ * earlier run.  warp_appends = 1 is valid for primitive-level scenes only
+ * (clv_scene_info.traversal_level 0, BVH of at most 64 levels). */
+int clv_device_scene_set_shape(clv_device_scene* dscene, uint32_t path_slots, uint32_t shade_blocks_per_sm,
+                               uint32_t warp_appends);
+
 /* ---- ray casts --------------------------------------------------------- */
 
 /* Closest hit of each ray with BVHNode::hit's exact decision order
