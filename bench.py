@@ -478,10 +478,11 @@ def run_config(args):
     film = torch.zeros(w * h * 3, dtype=torch.float64, device="cuda")
     tune = None
     if not args.no_autotune:
-        # wavefront shape search before any timing, on a quarter of the samples (a short render is mostly
-        # wavefront tail and favours small shapes), at most 2^27 samples per candidate
+        # wavefront shape search before any timing, on the workload's own samples per pixel where that is
+        # at most 2^27 samples per candidate (a shorter render is mostly wavefront tail and favours small
+        # shapes), else on 2^27 samples' worth
         t0 = time.perf_counter()
-        tune_spp = max(1, min(spp // 4, (1 << 27) // (w * h)))
+        tune_spp = max(1, min(spp, (1 << 27) // (w * h)))
         res = d.autotune(cg.RenderOptions(width=w, height=h, samples=tune_spp, max_depth=depth, seed=SEED + 7),
                          stream=sp)
         best = min(res, key=lambda r: r[3])
