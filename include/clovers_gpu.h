@@ -164,13 +164,14 @@ int clv_resolve_srgb(const float* xyz, uint32_t width, uint32_t height, uint8_t*
  * batching and autotuning layer).  Renders `opts` -- pass a short render, a few samples per
  * pixel of the workload to tune for -- twice for each candidate shape: paths
  * in flight (path_slots) SMs x {1, 2, 4, 8, 16} x 1024, shading grids of
- * {8, 16, 32} blocks per SM, and the intersect's queue appends per block (one
+ * {8, 16, 32} blocks per SM, and, for primitive-level scenes (traversal level
+ * 0, BVH of at most 64 levels), the intersect's queue appends per block (one
  * atomic per class and block, behind two block barriers) or per warp (no
  * barrier: better where traversal lengths vary widely within a block), and
  * keeps the fastest in the scene: later wavefront renders of this scene with
  * opts->path_slots = 0 use it.  results (optional) receives up to max_results
- * timings, n_results their count (30).  Allocates a film and the largest path
- * state it tries. */
+ * timings, n_results their count (30 for primitive-level scenes, else 15).
+ * Allocates a film and the largest path state it tries. */
 typedef struct clv_tune_result {
   uint32_t path_slots;
   uint32_t shade_blocks_per_sm;
