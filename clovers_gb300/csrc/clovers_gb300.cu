@@ -1435,17 +1435,12 @@ static int render_wavefront(clv_device_scene* d, const clv_render_opts* o, doubl
 // The multi-scene wavefront; with `guide`, Lambertian bounces of every scene
 // go through the one guide (alpha as in clv_render_guided), positions
 // normalised to each scene's own box.
-static int render_batch(clv_device_scene* const* ds, const clv_render_opts* opts, double* const* films, uint32_t n,
-                        void* stream, clv_guide* guide, float alpha) {
-  if (!ds || !opts || !films || n == 0) return fail(CLV_E_INVALID, "null argument or empty batch");
-  if (n > (1u << 24)) return fail(CLV_E_INVALID, "too many scenes in one batch");
-  for (uint32_t k = 0; k < n; ++k) {
-    const int rc = check_opts(ds[k], &opts[k]);
-    if (rc) return rc;
-    if (!films[k]) return fail(CLV_E_INVALID, "null film");
-    if (opts[k].mode != CLV_MODE_PATH_TRACING) return fail(CLV_E_INVALID, "batches render path tracing only");
-  }
-  cudaStream_t st = (cudaStream_t)stream;
+// One wavefront over at most CLV_BATCH_MAX scenes (arguments checked by the caller).
+// Holds the constant-memory scene tables until its last launch has finished.
+static int render_batch_part(clv_device_scene* const* ds, const clv_render_opts* opts, double* const* films,
+                             uint32_t n, cudaStream_t st, clv_guide* guide, float alpha, bool reset_records) {
+  static std::mutex tables_mu;
+  std::lock_guard<std::mutex> lock(tables_mu);
   void* dmem = nullptr;
   try {
     // The work items are laid out scene after scene, the scenes ordered by the
@@ -1482,20 +1477,17 @@ static int render_batch(clv_device_scene* const* ds, const clv_render_opts* opts
     const int nlevels = __builtin_popcount(levels);
     const unsigned long long total = prefix[n];
     // one staging allocation for the batch tables
-    const size_t b_views = n * sizeof(ClvDeviceScene), b_params = n * sizeof(WfParams);
+    ck(cudaMemcpyToSymbolAsync(wf_bscene, views.data(), n * sizeof(ClvDeviceScene), 0, cudaMemcpyHostToDevice, st),
+       "cudaMemcpyToSymbolAsync");
+    ck(cudaMemcpyToSymbolAsync(wf_bparam, params.data(), n * sizeof(WfParams), 0, cudaMemcpyHostToDevice, st),
+       "cudaMemcpyToSymbolAsync");
     const size_t b_prefix = (n + 1) * sizeof(unsigned long long), b_films = n * sizeof(double*);
     const size_t b_boxes = guide ? n * 6 * sizeof(float) : 0;
     auto up = [](size_t x) { return (x + 255) / 256 * 256; };
-    const size_t bytes = up(b_views) + up(b_params) + up(b_prefix) + up(b_films) + up(b_boxes);
+    const size_t bytes = up(b_prefix) + up(b_films) + up(b_boxes);
     ck(cudaMalloc(&dmem, bytes), "cudaMalloc batch tables");
     char* c = static_cast<char*>(dmem);
     WfBatch B;
-    B.scenes = reinterpret_cast<const ClvDeviceScene*>(c);
-    ck(cudaMemcpyAsync(c, views.data(), b_views, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync");
-    c += up(b_views);
-    B.params = reinterpret_cast<const WfParams*>(c);
-    ck(cudaMemcpyAsync(c, params.data(), b_params, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync");
-    c += up(b_params);
     B.prefix = reinterpret_cast<const unsigned long long*>(c);
     ck(cudaMemcpyAsync(c, prefix.data(), b_prefix, cudaMemcpyHostToDevice, st), "cudaMemcpyAsync");
     c += up(b_prefix);
@@ -1540,7 +1532,7 @@ static int render_batch(clv_device_scene* const* ds, const clv_render_opts* opts
       W.grec = guide->rec;
       W.grec_count = guide->rec_count;
       W.grec_cap = guide->rec_cap;
-      gd_reset_records(guide, st);
+      if (reset_records) gd_reset_records(guide, st);
       G = gd_view(guide, d0->view.root_box, alpha);
       G.boxes = dboxes;
       GQ = GdQueue{W.queue + (size_t)WF_Q_GUIDE * q, &C->queue[WF_Q_GUIDE], W.full, W.d_lambda, W.hit, W.meta, W.key};
@@ -1560,8 +1552,6 @@ static int render_batch(clv_device_scene* const* ds, const clv_render_opts* opts
     auto bounces = [&](cudaStream_t s) {
       for (int k = 0; k < batch; ++k) {
         cudaMemsetAsync(&C->live, 0, 5 * sizeof(unsigned int), s);
-        // one intersect launch per traversal level present, each over its own scenes' slots
-        // (a batch with a tree deeper than CLV_STACK levels: one generic launch with a spilling stack)
         // one intersect launch per traversal level present, each over its own scenes' slots
         // (a batch with a tree deeper than CLV_STACK levels: one generic launch with a spilling stack)
         const int only = nlevels > 1 ? 0 : -1;
@@ -1608,6 +1598,26 @@ static int render_batch(clv_device_scene* const* ds, const clv_render_opts* opts
     }
     return fail(CLV_E_CUDA, e.what());
   }
+}
+
+// A batch of more than CLV_BATCH_MAX scenes renders as consecutive wavefronts of
+// CLV_BATCH_MAX scenes; a guided batch collects the training records of all of them.
+static int render_batch(clv_device_scene* const* ds, const clv_render_opts* opts, double* const* films, uint32_t n,
+                        void* stream, clv_guide* guide, float alpha) {
+  if (!ds || !opts || !films || n == 0) return fail(CLV_E_INVALID, "null argument or empty batch");
+  if (n > (1u << 24)) return fail(CLV_E_INVALID, "too many scenes in one batch");
+  for (uint32_t k = 0; k < n; ++k) {
+    const int rc = check_opts(ds[k], &opts[k]);
+    if (rc) return rc;
+    if (!films[k]) return fail(CLV_E_INVALID, "null film");
+    if (opts[k].mode != CLV_MODE_PATH_TRACING) return fail(CLV_E_INVALID, "batches render path tracing only");
+  }
+  for (uint32_t k0 = 0; k0 < n; k0 += CLV_BATCH_MAX) {
+    const uint32_t m = std::min<uint32_t>(CLV_BATCH_MAX, n - k0);
+    const int rc = render_batch_part(ds + k0, opts + k0, films + k0, m, (cudaStream_t)stream, guide, alpha, k0 == 0);
+    if (rc) return rc;
+  }
+  return CLV_OK;
 }
 
 int clv_render_batch(clv_device_scene* const* ds, const clv_render_opts* opts, double* const* films, uint32_t n,

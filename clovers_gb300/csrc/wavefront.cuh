@@ -60,9 +60,15 @@ struct WfParams {
 
 // Several scenes rendered by one wavefront: the work items of scene s are
 // [prefix[s], prefix[s+1]); a path slot records its scene in meta.w >> 8.
+// The scene views and render parameters of a batch sit in constant memory
+// (wf_bscene / wf_bparam, at most CLV_BATCH_MAX scenes), so that the kernels
+// read them through the constant cache, as a single-scene kernel reads its
+// scene from the kernel parameters; the host writes the tables before the
+// batch's launches and holds them until its last launch has finished.
+#define CLV_BATCH_MAX 128
+__constant__ ClvDeviceScene wf_bscene[CLV_BATCH_MAX];
+__constant__ WfParams wf_bparam[CLV_BATCH_MAX];
 struct WfBatch {
-  const ClvDeviceScene* scenes;
-  const WfParams* params;
   const unsigned long long* prefix;  // n + 1 entries
   double* const* films;
   uint32_t n;
@@ -126,7 +132,7 @@ __global__ void wf_init(ClvDeviceScene S, WfParams P, WfState W, WfBatch B) {
   if constexpr (BATCH) {
     if ((unsigned long long)i < B.total) {
       const uint32_t sid = wf_scene_of(B, i);
-      wf_start_path(B.scenes[sid], B.params[sid], W, i, i - B.prefix[sid], sid);
+      wf_start_path(wf_bscene[sid], wf_bparam[sid], W, i, i - B.prefix[sid], sid);
       return;
     }
   } else {
@@ -309,10 +315,10 @@ __global__ void __launch_bounds__(128, CPLX == 1 ? CLV_MINB_CHAIN : CLV_MINB) wf
   uint32_t live = 0;
   const uint4 m = i < W.Q ? W.meta[i] : make_uint4(0u, 0u, 0u, 0u);
   bool go = (m.w & 1u) != 0u;
-  if (BATCH && go && only_level >= 0) go = B.scenes[m.w >> 8].compound_level == (uint32_t)only_level;
+  if (BATCH && go && only_level >= 0) go = wf_bscene[m.w >> 8].compound_level == (uint32_t)only_level;
   live = go ? 1u : 0u;
   int cls;
-  if constexpr (BATCH) cls = intersect_slot<CPLX, COUNT, WT, DEEP>(B.scenes[go ? m.w >> 8 : 0u], W, err, i, m, go, c);
+  if constexpr (BATCH) cls = intersect_slot<CPLX, COUNT, WT, DEEP>(wf_bscene[go ? m.w >> 8 : 0u], W, err, i, m, go, c);
   else cls = intersect_slot<CPLX, COUNT, WT, DEEP>(S, W, err, i, m, go, c);
   if constexpr (WAPP) wf_enqueue_warp(W, C, cls, i);
   else wf_enqueue_block(W, C, cls, i);
@@ -436,7 +442,7 @@ __global__ void __launch_bounds__(128, CLV_MINB_SHADE) wf_shade_specular(ClvDevi
       i = W.queue[(size_t)WF_Q_SPEC * W.Q + q];
       if constexpr (BATCH) {
         const uint32_t sid = W.meta[i].w >> 8;
-        live = specular_slot(B.scenes[sid], B.params[sid], W, C, i);
+        live = specular_slot(wf_bscene[sid], wf_bparam[sid], W, C, i);
       } else {
         live = specular_slot(S, P, W, C, i);
       }
@@ -516,7 +522,7 @@ __global__ void __launch_bounds__(128, CLV_MINB_SHADE) wf_shade_diffuse(ClvDevic
       i = W.queue[(size_t)WF_Q_DIFF * W.Q + q];
       if constexpr (BATCH) {
         const uint32_t sid = W.meta[i].w >> 8;
-        live = diffuse_slot(B.scenes[sid], B.params[sid], W, C, err, i);
+        live = diffuse_slot(wf_bscene[sid], wf_bparam[sid], W, C, err, i);
       } else {
         live = diffuse_slot(S, P, W, C, err, i);
       }
@@ -570,7 +576,7 @@ __global__ void __launch_bounds__(128, CLV_MINB_GUIDE) wf_guide_pre(ClvDeviceSce
   const uint32_t stride = gridDim.x * blockDim.x;
   for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += stride) {
     const uint32_t i = W.queue[(size_t)WF_Q_GUIDE * W.Q + q];
-    if constexpr (BATCH) guide_pre_slot(B.scenes[W.meta[i].w >> 8], W, alpha, i);
+    if constexpr (BATCH) guide_pre_slot(wf_bscene[W.meta[i].w >> 8], W, alpha, i);
     else guide_pre_slot(S, W, alpha, i);
   }
 }
@@ -666,7 +672,7 @@ __global__ void __launch_bounds__(128, CLV_MINB_GUIDE) wf_guide_post(ClvDeviceSc
     if (q < n) {
       if constexpr (BATCH) {
         const uint32_t sid = W.meta[i].w >> 8;
-        live = guide_post_slot(B.scenes[sid], B.params[sid], W, C, err, G, i);
+        live = guide_post_slot(wf_bscene[sid], wf_bparam[sid], W, C, err, G, i);
       } else {
         live = guide_post_slot(S, P, W, C, err, G, i);
       }
@@ -759,7 +765,7 @@ __global__ void __launch_bounds__(128, CLV_MINB_SHADE) wf_finish(ClvDeviceScene 
       i = W.queue[(size_t)WF_Q_FINISH * W.Q + q];
       if constexpr (BATCH) {
         const uint32_t sid = W.meta[i].w >> 8;
-        finish_slot(B.scenes[sid], W, B.films[sid], i);
+        finish_slot(wf_bscene[sid], W, B.films[sid], i);
       } else {
         finish_slot(S, W, film, i);
       }
@@ -792,7 +798,7 @@ __global__ void __launch_bounds__(128, CLV_MINB_SHADE) wf_finish(ClvDeviceScene 
         if constexpr (BATCH) {
           if (w < B.total) {
             const uint32_t sid = wf_scene_of(B, w);
-            wf_start_path(B.scenes[sid], B.params[sid], W, i, w - B.prefix[sid], sid);
+            wf_start_path(wf_bscene[sid], wf_bparam[sid], W, i, w - B.prefix[sid], sid);
             live = true;
           } else {
             W.meta[i].w = 0u;

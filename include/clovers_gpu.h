@@ -131,8 +131,11 @@ int clv_render_device(clv_device_scene* dscene, const clv_render_opts* opts, dou
  * so scenes of uneven size keep the GPU full.  Each scene adds its film sums
  * into films[k] (width*height*3 doubles, caller-zeroed), exactly as n calls of
  * clv_render_device with the same options would (same random streams).  The
- * path state of the batch lives in dscenes[0].  No counterpart in the
- * reference, which renders one scene per process. */
+ * path state of the batch lives in dscenes[0].  Up to 128 scenes share one
+ * wavefront (their views sit in constant memory, so concurrent batch calls
+ * run one after another); larger batches render as consecutive wavefronts of
+ * 128 scenes.  No counterpart in the reference, which renders one scene per
+ * process. */
 int clv_render_batch(clv_device_scene* const* dscenes, const clv_render_opts* opts, double* const* films, uint32_t n,
                      void* stream);
 

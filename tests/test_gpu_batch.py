@@ -27,6 +27,15 @@ def test_batch_matches_individual_renders(tmp_path):
         single = cg.draw(cg.GlobalOptions(quiet=True), o, d)
         np.testing.assert_allclose(img, single, rtol=1e-6, atol=1e-9)
         assert d.status() == 0
+    # a batch with a watertight scene runs the variants that choose the triangle test per scene
+    path = scenes.write_scene(specs[2][0], str(tmp_path / "wt.json"))
+    wt = cg.Scene.from_json(path, 40, 30).set_watertight().upload()
+    wt_opts = cg.RenderOptions(width=40, height=30, samples=16, max_depth=10, seed=9)
+    batched = cg.draw_batch(dev + [wt], opts + [wt_opts])
+    for d, o, img in zip(dev + [wt], opts + [wt_opts], batched):
+        single = cg.draw(cg.GlobalOptions(quiet=True), o, d)
+        np.testing.assert_allclose(img, single, rtol=1e-6, atol=1e-9)
+        assert d.status() == 0
 
 
 def test_guided_batch_matches_guided_single_renders(tmp_path):
@@ -49,3 +58,23 @@ def test_guided_batch_matches_guided_single_renders(tmp_path):
             np.testing.assert_allclose(img, single, rtol=1e-6, atol=1e-9)
             assert d.status() == 0
     assert guide.status() == 0
+
+
+def test_batch_larger_than_one_wavefront(tmp_path):
+    """A batch of more than 128 scenes (the size of the constant-memory scene tables) renders as
+    consecutive wavefronts; every scene still gets its own render's film."""
+    specs = [scenes.enclosed_box(), scenes.random_spheres(1), scenes.batch_scene(1, str(tmp_path))[0]]
+    dev = []
+    for k, sc in enumerate(specs):
+        path = scenes.write_scene(sc, str(tmp_path / ("m%d.json" % k)))
+        dev.append(cg.Scene.from_json(path, 16, 12).upload())
+    ds, opts = [], []
+    for k in range(131):
+        ds.append(dev[k % 3])
+        opts.append(cg.RenderOptions(width=16, height=12, samples=1 + k % 3, max_depth=4 + k % 5, seed=100 + k))
+    batched = cg.draw_batch(ds, opts)
+    assert len(batched) == 131
+    for k in (0, 1, 2, 64, 127, 128, 129, 130):
+        single = cg.draw(cg.GlobalOptions(quiet=True), opts[k], ds[k])
+        np.testing.assert_allclose(batched[k], single, rtol=1e-6, atol=1e-9)
+    assert all(d.status() == 0 for d in dev)
