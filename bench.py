@@ -297,10 +297,45 @@ def run_batch(args):
                                    "0-3 smoke boxes, 128^2-1024^2, 16-512 spp, depth %d" % (n, DEPTH),
                        "samples_per_step": samples, "triangles": tris, "scene_load_s": round(load_s, 2)},
             "one_by_one": {"ms": round(t_seq, 3), "value": round(samples / (t_seq / 1e3) / 1e6, 3)}}
-    conv = batch_convergence(args, dev, tmp)
+    line["small_scenes"] = batch_small(args, L, sp, tmp, n, timed)
+    conv = None if args.no_convergence else batch_convergence(args, dev, tmp)
     if conv:
         line["time_to_relmse"] = conv
     print(json.dumps(line), flush=True)
+
+
+def batch_small(args, L, sp, tmp, n, timed, side=128, spp=16):
+    """The same scenes at side x side pixels and spp samples per pixel: renders too small to fill the GPU
+    alone (side^2 * spp work items against about 1.2 M path slots), batched vs one by one."""
+    import torch
+    import clovers_gb300 as cg
+    from clovers_gb300 import _lib
+    dev, opts, films = [], [], []
+    for k in range(n):
+        dev.append(cg.Scene.from_json(os.path.join(tmp, "batch_%02d.json" % k), side, side).upload())
+        opts.append(cg.render_opts(cg.RenderOptions(width=side, height=side, samples=spp, max_depth=DEPTH,
+                                                    seed=100 + k)))
+        films.append(torch.zeros(side * side * 3, dtype=torch.float64, device="cuda"))
+    handles = (ctypes.c_void_p * n)(*[d.handle.value for d in dev])
+    optarr = (_lib.RenderOptsC * n)(*opts)
+    ptrs = (ctypes.c_void_p * n)(*[f.data_ptr() for f in films])
+
+    def batched():
+        _lib.check(L.clv_render_batch(handles, optarr, ptrs, n, sp))
+
+    def one_by_one():
+        for k in range(n):
+            _lib.check(L.clv_render_device(dev[k].handle, ctypes.byref(optarr[k]), films[k].data_ptr(), sp))
+
+    for _ in range(args.warmup):
+        batched()
+        one_by_one()
+    t_batch = min(timed(batched) for _ in range(args.steps))
+    t_seq = min(timed(one_by_one) for _ in range(args.steps))
+    samples = n * side * side * spp
+    return {"workload": "the same %d scenes at %dx%d, %d spp" % (n, side, side, spp), "samples_per_step": samples,
+            "batched": {"ms": round(t_batch, 3), "value": round(samples / (t_batch / 1e3) / 1e6, 3)},
+            "one_by_one": {"ms": round(t_seq, 3), "value": round(samples / (t_seq / 1e3) / 1e6, 3)}}
 
 
 def batch_convergence(args, dev, tmp):
@@ -704,6 +739,8 @@ def main():
     ap.add_argument("--max-spp", type=int, default=8192, help="cap of the progressive relMSE measurement")
     ap.add_argument("--batch", action="store_true", help="measure the batched multi-scene workload")
     ap.add_argument("--batch-scenes", type=int, default=64)
+    ap.add_argument("--no-convergence", action="store_true",
+                    help="with --batch: skip the per-scene time to relMSE 1e-3 (launch lists of the timed renders)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline legs")
     ap.add_argument("--no-parity", action="store_true",
                     help="skip the check of every timed ray cast against the oracle (untimed, about 40 s of CPU)")

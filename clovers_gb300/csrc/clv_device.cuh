@@ -39,6 +39,9 @@ namespace clvd {
 #ifndef CLV_MINB
 #define CLV_MINB 8         // resident blocks per SM asked of the wavefront intersect (64 registers)
 #endif
+#ifndef CLV_MINB_MEDIUM
+#define CLV_MINB_MEDIUM CLV_MINB  // the same for its variant with media and object lists
+#endif
 #ifndef CLV_MINB_CHAIN
 #define CLV_MINB_CHAIN 7   // the same for its wrapper-chain variant (72 registers; 6 and 8 slower on the box)
 #endif

@@ -308,7 +308,7 @@ __device__ __forceinline__ int intersect_slot(const ClvDeviceScene& S, const WfS
 // clv_autotune finds faster so; a separate instantiation, because even an unused
 // run-time branch to the warp form slowed the wrapper-chain variant by 11 %).
 template <int CPLX, bool COUNT, bool BATCH, int WT, bool DEEP = false, bool WAPP = false>
-__global__ void __launch_bounds__(128, CPLX == 1 ? CLV_MINB_CHAIN : CLV_MINB) wf_intersect(ClvDeviceScene S, WfState W, WfCounters* C, uint32_t* err,
+__global__ void __launch_bounds__(128, CPLX == 1 ? CLV_MINB_CHAIN : CPLX == 2 ? CLV_MINB_MEDIUM : CLV_MINB) wf_intersect(ClvDeviceScene S, WfState W, WfCounters* C, uint32_t* err,
                                                               unsigned long long* cnt, WfBatch B, int only_level) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   Counters c{0u, 0u};
