@@ -534,6 +534,14 @@ int sm_count() {
   return n;
 }
 
+// Grid of a shading kernel with `minb` resident blocks per SM (wf_shade_diffuse,
+// wf_guide_post): the shading grid (tuned or default blocks per SM) scaled by
+// minb over the other shading kernels' resident blocks.
+uint32_t scaled_grid(uint32_t grid, uint32_t tuned_shade, uint32_t minb) {
+  const uint64_t per_sm = (uint64_t)(tuned_shade ? tuned_shade : CLV_SHADE_BLOCKS) * minb / CLV_MINB_SHADE;
+  return (uint32_t)std::min<uint64_t>(grid, (uint64_t)sm_count() * std::max<uint64_t>(1, per_sm));
+}
+
 }  // namespace
 
 int clv_internal_fail(int code, const char* msg) { return fail(code, msg); }
@@ -1309,6 +1317,8 @@ static int render_wavefront(clv_device_scene* d, const clv_render_opts* o, doubl
     // shading kernels walk their queues with a grid-stride loop over a fixed grid
     const uint32_t qgrid =
         std::min<uint32_t>(grid, (uint32_t)sm_count() * (d->tuned_shade ? d->tuned_shade : CLV_SHADE_BLOCKS));
+    const uint32_t dgrid = scaled_grid(grid, d->tuned_shade, CLV_MINB_DIFFUSE);
+    const uint32_t pgrid = scaled_grid(grid, d->tuned_shade, CLV_MINB_GUIDE_POST);
     if (prof) {
       std::memset(prof, 0, sizeof *prof);
       ck(cudaMalloc(&dcnt, 3 * sizeof(unsigned long long)), "cudaMalloc");
@@ -1370,11 +1380,11 @@ static int render_wavefront(clv_device_scene* d, const clv_render_opts* o, doubl
       if (prof) cudaEventRecord(evs[4 * k + 1], s);
       if (prof) cudaEventRecord(evs[4 * k + 2], s);
       wf_shade_specular<false><<<qgrid, block, 0, s>>>(d->view, P, W, C, d->err, WfBatch{});
-      wf_shade_diffuse<false><<<qgrid, block, 0, s>>>(d->view, P, W, C, d->err, WfBatch{});
+      wf_shade_diffuse<false><<<dgrid, block, 0, s>>>(d->view, P, W, C, d->err, WfBatch{});
       if (guide) {
         wf_guide_pre<false><<<qgrid, block, 0, s>>>(d->view, W, C, alpha, WfBatch{});
         if (alpha > 0.0f) gd_launch_queue(G, GQ, (uint32_t)q, s);
-        wf_guide_post<false><<<qgrid, block, 0, s>>>(d->view, P, W, C, d->err, G, WfBatch{});
+        wf_guide_post<false><<<pgrid, block, 0, s>>>(d->view, P, W, C, d->err, G, WfBatch{});
       }
       wf_finish<false><<<qgrid, block, 0, s>>>(d->view, P, W, C, film, WfBatch{});
       if (prof) cudaEventRecord(evs[4 * k + 3], s);
@@ -1542,6 +1552,8 @@ static int render_batch_part(clv_device_scene* const* ds, const clv_render_opts*
     const uint32_t grid = (uint32_t)((q + block - 1) / block);
     const uint32_t qgrid =
         std::min<uint32_t>(grid, (uint32_t)sm_count() * (d0->tuned_shade ? d0->tuned_shade : CLV_SHADE_BLOCKS));
+    const uint32_t dgrid = scaled_grid(grid, d0->tuned_shade, CLV_MINB_DIFFUSE);
+    const uint32_t pgrid = scaled_grid(grid, d0->tuned_shade, CLV_MINB_GUIDE_POST);
     const ClvDeviceScene& S0 = d0->view;
     const WfParams P0 = params[0];
     wf_init<true><<<grid, block, 0, st>>>(S0, P0, W, B);
@@ -1568,11 +1580,11 @@ static int render_batch_part(clv_device_scene* const* ds, const clv_render_opts*
                                                                               only < 0 ? -1 : 2);
         }
         wf_shade_specular<true><<<qgrid, block, 0, s>>>(S0, P0, W, C, d0->err, B);
-        wf_shade_diffuse<true><<<qgrid, block, 0, s>>>(S0, P0, W, C, d0->err, B);
+        wf_shade_diffuse<true><<<dgrid, block, 0, s>>>(S0, P0, W, C, d0->err, B);
         if (guide) {
           wf_guide_pre<true><<<qgrid, block, 0, s>>>(S0, W, C, alpha, B);
           if (alpha > 0.0f) gd_launch_queue(G, GQ, (uint32_t)q, s);
-          wf_guide_post<true><<<qgrid, block, 0, s>>>(S0, P0, W, C, d0->err, G, B);
+          wf_guide_post<true><<<pgrid, block, 0, s>>>(S0, P0, W, C, d0->err, G, B);
         }
         wf_finish<true><<<qgrid, block, 0, s>>>(S0, P0, W, C, nullptr, B);
       }
@@ -1881,6 +1893,7 @@ extern "C" int clv_render_device_noalloc(clv_device_scene* d, const clv_render_o
   const uint32_t grid = (uint32_t)((q + block - 1) / block);
   const uint32_t qgrid =
       std::min<uint32_t>(grid, (uint32_t)sm_count() * (d->tuned_shade ? d->tuned_shade : CLV_SHADE_BLOCKS));
+  const uint32_t dgrid = scaled_grid(grid, d->tuned_shade, CLV_MINB_DIFFUSE);
   // the array keeps the previous call's contents: counters are reset here and
   // wf_init rewrites every path slot
   noalloc_counters_init<<<1, 1, 0, st>>>(C, std::min<uint64_t>(q, P.total));
@@ -1900,7 +1913,7 @@ extern "C" int clv_render_device_noalloc(clv_device_scene* d, const clv_render_o
         default: wf_intersect<2, false, false, CLV_WT_ON><<<grid, block, 0, st>>>(d->view, W, C, d->err, nullptr, WfBatch{}, -1); break;
       }
       wf_shade_specular<false><<<qgrid, block, 0, st>>>(d->view, P, W, C, d->err, WfBatch{});
-      wf_shade_diffuse<false><<<qgrid, block, 0, st>>>(d->view, P, W, C, d->err, WfBatch{});
+      wf_shade_diffuse<false><<<dgrid, block, 0, st>>>(d->view, P, W, C, d->err, WfBatch{});
       wf_finish<false><<<qgrid, block, 0, st>>>(d->view, P, W, C, film_dev, WfBatch{});
     }
     g_launches += 4 * batch;

@@ -163,8 +163,16 @@ __device__ __forceinline__ void warp_add_counts(unsigned long long* cnt, uint32_
 #ifndef CLV_MINB_SHADE
 #define CLV_MINB_SHADE 8  // resident blocks per SM asked of the shading kernels (64 registers)
 #endif
+#ifndef CLV_MINB_DIFFUSE
+// the same for wf_shade_diffuse, whose grid scales with it: 5 blocks (96 registers, 28 bytes of spills
+// against 232 at 64) measured best of 4..8 (enclosed box 682.7 against 675.5 Msamples/s at 8)
+#define CLV_MINB_DIFFUSE 5
+#endif
 #ifndef CLV_MINB_GUIDE
-#define CLV_MINB_GUIDE CLV_MINB_SHADE  // the same for the guided bounce kernels
+#define CLV_MINB_GUIDE CLV_MINB_SHADE  // the same for wf_guide_pre
+#endif
+#ifndef CLV_MINB_GUIDE_POST
+#define CLV_MINB_GUIDE_POST CLV_MINB_SHADE  // the same for wf_guide_post (its grid scales with it)
 #endif
 // Appends each thread's slot i to queue `cls` (cls < 0: nothing) with one
 // atomic per class for the whole block; every thread of the 128-thread block
@@ -507,7 +515,7 @@ __device__ __forceinline__ bool diffuse_slot(const ClvDeviceScene& S, const WfPa
 }
 
 template <bool BATCH>
-__global__ void __launch_bounds__(128, CLV_MINB_SHADE) wf_shade_diffuse(ClvDeviceScene S, WfParams P, WfState W, WfCounters* C,
+__global__ void __launch_bounds__(128, CLV_MINB_DIFFUSE) wf_shade_diffuse(ClvDeviceScene S, WfParams P, WfState W, WfCounters* C,
                                                         uint32_t* err, WfBatch B) {
   const uint32_t n = C->queue[WF_Q_DIFF];
   const uint32_t stride = gridDim.x * blockDim.x;
@@ -658,7 +666,7 @@ __device__ __forceinline__ bool guide_post_slot(const ClvDeviceScene& S, const W
 }
 
 template <bool BATCH>
-__global__ void __launch_bounds__(128, CLV_MINB_GUIDE) wf_guide_post(ClvDeviceScene S, WfParams P, WfState W, WfCounters* C,
+__global__ void __launch_bounds__(128, CLV_MINB_GUIDE_POST) wf_guide_post(ClvDeviceScene S, WfParams P, WfState W, WfCounters* C,
                                                      uint32_t* err, GuideDev G, WfBatch B) {
   const uint32_t n = C->queue[WF_Q_GUIDE];
   const uint32_t stride = gridDim.x * blockDim.x;
