@@ -520,9 +520,10 @@ def run_config(args):
         tune_spp = max(1, min(spp, (1 << 27) // (w * h)))
         res = d.autotune(cg.RenderOptions(width=w, height=h, samples=tune_spp, max_depth=depth, seed=SEED + 7),
                          stream=sp)
-        best = min(res, key=lambda r: r[3])
+        best = min(res, key=lambda r: r[4])
         tune = {"path_slots": best[0], "shade_blocks_per_sm": best[1], "warp_appends": best[2],
-                "candidates": len(res), "tuning_spp": tune_spp, "tuning_s": round(time.perf_counter() - t0, 3)}
+                "diffuse_blocks_per_sm": best[3], "candidates": len(res), "tuning_spp": tune_spp,
+                "tuning_s": round(time.perf_counter() - t0, 3)}
 
     def render(n_spp, offset, seed=SEED):
         o = cg.render_opts(cg.RenderOptions(width=w, height=h, samples=n_spp, max_depth=depth, seed=seed))
@@ -807,9 +808,10 @@ def main():
             t0 = time.perf_counter()
             res = dscene.autotune(cg.RenderOptions(width=W_IMG, height=H_IMG, samples=max(1, SPP // 4),
                                                    max_depth=DEPTH, seed=SEED + 7), stream=sp)
-            best = min(res, key=lambda r: r[3])
+            best = min(res, key=lambda r: r[4])
             tune = {"path_slots": best[0], "shade_blocks_per_sm": best[1], "warp_appends": best[2],
-                    "candidates": len(res), "tuning_s": round(time.perf_counter() - t0, 3)}
+                    "diffuse_blocks_per_sm": best[3], "candidates": len(res),
+                    "tuning_s": round(time.perf_counter() - t0, 3)}
         for w in range(args.warmup):
             film.zero_()
             _lib.check(L.clv_render_device(dscene.handle, ctypes.byref(opts_for(10**6 + w)), film.data_ptr(), sp))

@@ -142,18 +142,21 @@ class DeviceScene:
         check(lib().clv_device_status(self._h, ctypes.byref(f)))
         return f.value
 
-    def set_shape(self, path_slots=0, shade_blocks_per_sm=0, warp_appends=0):
+    def set_shape(self, path_slots=0, shade_blocks_per_sm=0, warp_appends=0, diffuse_blocks_per_sm=0):
         """clv_device_scene_set_shape: the wavefront shape of later renders (0 = built-in defaults)."""
-        check(lib().clv_device_scene_set_shape(self._h, path_slots, shade_blocks_per_sm, warp_appends))
+        check(lib().clv_device_scene_set_shape(self._h, path_slots, shade_blocks_per_sm, warp_appends,
+                                               diffuse_blocks_per_sm))
 
     def autotune(self, render_options, stream=None):
         """clv_autotune on a short render: the chosen shape is kept for later
-        renders of this scene; returns [(path_slots, shade_blocks_per_sm, warp_appends, ms)]."""
+        renders of this scene; returns [(path_slots, shade_blocks_per_sm, warp_appends,
+        diffuse_blocks_per_sm, ms)]."""
         o = render_opts(render_options)
         res = (_lib.TuneResultC * 64)()
         n = ctypes.c_uint32()
         check(lib().clv_autotune(self._h, ctypes.byref(o), res, 64, ctypes.byref(n), stream))
-        return [(r.path_slots, r.shade_blocks_per_sm, r.warp_appends, r.ms) for r in res[:n.value]]
+        return [(r.path_slots, r.shade_blocks_per_sm, r.warp_appends, r.diffuse_blocks_per_sm, r.ms)
+                for r in res[:n.value]]
 
 
 def render_opts(opts: RenderOptions, sample_offset=0, path_slots=0):

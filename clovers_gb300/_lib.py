@@ -41,7 +41,8 @@ class GuideOptsC(ctypes.Structure):
 
 
 class TuneResultC(ctypes.Structure):
-    _fields_ = [("path_slots", c_u32), ("shade_blocks_per_sm", c_u32), ("warp_appends", c_u32), ("ms", c_f32)]
+    _fields_ = [("path_slots", c_u32), ("shade_blocks_per_sm", c_u32), ("warp_appends", c_u32),
+                ("diffuse_blocks_per_sm", c_u32), ("ms", c_f32)]
 
 
 class RenderProfileC(ctypes.Structure):
@@ -66,7 +67,7 @@ SIGNATURES = {
     "clv_render_batch": (c_i32, [ctypes.c_void_p, P(RenderOptsC), ctypes.c_void_p, c_u32, ctypes.c_void_p]),
     "clv_render_device_noalloc": (c_i32, [ctypes.c_void_p, P(RenderOptsC), ctypes.c_void_p, ctypes.c_void_p]),
     "clv_autotune": (c_i32, [ctypes.c_void_p, P(RenderOptsC), ctypes.c_void_p, c_u32, P(c_u32), ctypes.c_void_p]),
-    "clv_device_scene_set_shape": (c_i32, [ctypes.c_void_p, c_u32, c_u32, c_u32]),
+    "clv_device_scene_set_shape": (c_i32, [ctypes.c_void_p, c_u32, c_u32, c_u32, c_u32]),
     "clv_resolve_device": (c_i32, [ctypes.c_void_p, c_u32, c_u32, c_u32, ctypes.c_void_p, ctypes.c_void_p,
                                    ctypes.c_void_p]),
     "clv_resolve_srgb": (c_i32, [ctypes.c_void_p, c_u32, c_u32, ctypes.c_void_p]),

@@ -542,6 +542,19 @@ uint32_t scaled_grid(uint32_t grid, uint32_t tuned_shade, uint32_t minb) {
   return (uint32_t)std::min<uint64_t>(grid, (uint64_t)sm_count() * std::max<uint64_t>(1, per_sm));
 }
 
+// wf_shade_diffuse in the variant `blocks` (resident blocks per SM; 0 = the default).
+template <bool BATCH>
+void launch_shade_diffuse(uint32_t blocks, uint32_t grid, uint32_t tuned_shade, cudaStream_t s,
+                          const ClvDeviceScene& S, const WfParams& P, const WfState& W, WfCounters* C, uint32_t* err,
+                          const WfBatch& B) {
+  if (blocks == CLV_MINB_DIFFUSE_ALT)
+    wf_shade_diffuse<BATCH, CLV_MINB_DIFFUSE_ALT>
+        <<<scaled_grid(grid, tuned_shade, CLV_MINB_DIFFUSE_ALT), 128, 0, s>>>(S, P, W, C, err, B);
+  else
+    wf_shade_diffuse<BATCH, CLV_MINB_DIFFUSE>
+        <<<scaled_grid(grid, tuned_shade, CLV_MINB_DIFFUSE), 128, 0, s>>>(S, P, W, C, err, B);
+}
+
 }  // namespace
 
 int clv_internal_fail(int code, const char* msg) { return fail(code, msg); }
@@ -632,6 +645,7 @@ struct clv_device_scene {
   uint32_t tuned_slots = 0;      // paths in flight
   uint32_t tuned_shade = 0;      // shading-kernel blocks per SM
   uint32_t tuned_append = 0;     // intersect queue appends per warp (1) or per block (0), primitive-level scenes
+  uint32_t tuned_diffuse = 0;    // wf_shade_diffuse variant: resident blocks per SM (0: CLV_MINB_DIFFUSE)
   unsigned long long* ray_next = nullptr;  // work counter of the persistent ray casts
   uint32_t* ray_sort = nullptr;            // ray order: histogram, keys, permutation
   uint64_t ray_sort_cap = 0;               // rays the sort scratch holds
@@ -871,7 +885,8 @@ int clv_autotune(clv_device_scene* d, const clv_render_opts* o, clv_tune_result*
   cudaStream_t st = (cudaStream_t)stream;
   double* film = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
-  const uint32_t old_slots = d->tuned_slots, old_shade = d->tuned_shade, old_append = d->tuned_append;
+  const uint32_t old_slots = d->tuned_slots, old_shade = d->tuned_shade, old_append = d->tuned_append,
+                 old_diffuse = d->tuned_diffuse;
   auto cleanup = [&]() {
     if (film) cudaFree(film);
     if (e0) cudaEventDestroy(e0);
@@ -889,36 +904,46 @@ int clv_autotune(clv_device_scene* d, const clv_render_opts* o, clv_tune_result*
     t.path_slots = 0;
     float best = 3.0e38f;
     uint32_t best_slots = 0, best_shade = 0, best_append = 0, n = 0;
+    auto time_shape = [&]() {  // best of two renders of the current shape
+      float ms = 3.0e38f;
+      for (int rep = 0; rep < 2; ++rep) {
+        ck(cudaMemsetAsync(film, 0, fb, st), "cudaMemsetAsync");
+        ck(cudaEventRecord(e0, st), "cudaEventRecord");
+        rc = render_wavefront(d, &t, film, st, nullptr);
+        if (rc) throw std::runtime_error(g_error);
+        ck(cudaEventRecord(e1, st), "cudaEventRecord");
+        ck(cudaEventSynchronize(e1), "cudaEventSynchronize");
+        float m = 0.0f;
+        ck(cudaEventElapsedTime(&m, e0, e1), "cudaEventElapsedTime");
+        ms = std::min(ms, m);
+      }
+      const uint32_t db = d->tuned_diffuse ? d->tuned_diffuse : CLV_MINB_DIFFUSE;
+      if (results && n < max_results)
+        results[n] = clv_tune_result{d->tuned_slots, d->tuned_shade, d->tuned_append, db, ms};
+      ++n;
+      return ms;
+    };
+    d->tuned_diffuse = 0;
     for (uint32_t a = 0; a < 5; ++a)
       for (uint32_t b = 0; b < 3; ++b)
         for (uint32_t ap = 0; ap < (d->view.compound_level == 0 && !d->deep() ? 2u : 1u); ++ap) {
-        d->tuned_slots = sms * slot_mult[a] * 1024u;
-        d->tuned_shade = shade[b];
-        d->tuned_append = ap;
-        float ms = 3.0e38f;
-        for (int rep = 0; rep < 2; ++rep) {
-          ck(cudaMemsetAsync(film, 0, fb, st), "cudaMemsetAsync");
-          ck(cudaEventRecord(e0, st), "cudaEventRecord");
-          rc = render_wavefront(d, &t, film, st, nullptr);
-          if (rc) throw std::runtime_error(g_error);
-          ck(cudaEventRecord(e1, st), "cudaEventRecord");
-          ck(cudaEventSynchronize(e1), "cudaEventSynchronize");
-          float m = 0.0f;
-          ck(cudaEventElapsedTime(&m, e0, e1), "cudaEventElapsedTime");
-          ms = std::min(ms, m);
+          d->tuned_slots = sms * slot_mult[a] * 1024u;
+          d->tuned_shade = shade[b];
+          d->tuned_append = ap;
+          const float ms = time_shape();
+          if (ms < best) {
+            best = ms;
+            best_slots = d->tuned_slots;
+            best_shade = d->tuned_shade;
+            best_append = ap;
+          }
         }
-        if (results && n < max_results) results[n] = clv_tune_result{d->tuned_slots, d->tuned_shade, ap, ms};
-        ++n;
-        if (ms < best) {
-          best = ms;
-          best_slots = d->tuned_slots;
-          best_shade = d->tuned_shade;
-          best_append = ap;
-        }
-      }
     d->tuned_slots = best_slots;
     d->tuned_shade = best_shade;
     d->tuned_append = best_append;
+    // the other wf_shade_diffuse variant at the chosen shape
+    d->tuned_diffuse = CLV_MINB_DIFFUSE_ALT;
+    if (!(time_shape() < best)) d->tuned_diffuse = 0;
     if (n_results) *n_results = n;
     cleanup();
     return CLV_OK;
@@ -926,21 +951,26 @@ int clv_autotune(clv_device_scene* d, const clv_render_opts* o, clv_tune_result*
     d->tuned_slots = old_slots;
     d->tuned_shade = old_shade;
     d->tuned_append = old_append;
+    d->tuned_diffuse = old_diffuse;
     cleanup();
     return fail(CLV_E_CUDA, ex.what());
   }
 }
 
 int clv_device_scene_set_shape(clv_device_scene* d, uint32_t path_slots, uint32_t shade_blocks_per_sm,
-                               uint32_t warp_appends) {
+                               uint32_t warp_appends, uint32_t diffuse_blocks_per_sm) {
   if (!d) return fail(CLV_E_INVALID, "null argument");
   if (warp_appends > 1) return fail(CLV_E_INVALID, "warp_appends takes 0 or 1");
   if (warp_appends && (d->view.compound_level != 0 || d->deep()))
     return fail(CLV_E_INVALID, "per-warp appends exist for primitive-level scenes of at most 64 BVH levels");
   if (shade_blocks_per_sm > 64) return fail(CLV_E_INVALID, "shade_blocks_per_sm above 64");
+  if (diffuse_blocks_per_sm && diffuse_blocks_per_sm != CLV_MINB_DIFFUSE && diffuse_blocks_per_sm != CLV_MINB_DIFFUSE_ALT)
+    return fail(CLV_E_INVALID, "diffuse_blocks_per_sm takes 0, " + std::to_string(CLV_MINB_DIFFUSE) + " or " +
+                                   std::to_string(CLV_MINB_DIFFUSE_ALT));
   d->tuned_slots = path_slots;
   d->tuned_shade = shade_blocks_per_sm;
   d->tuned_append = warp_appends;
+  d->tuned_diffuse = diffuse_blocks_per_sm == CLV_MINB_DIFFUSE ? 0u : diffuse_blocks_per_sm;
   return CLV_OK;
 }
 
@@ -1317,7 +1347,6 @@ static int render_wavefront(clv_device_scene* d, const clv_render_opts* o, doubl
     // shading kernels walk their queues with a grid-stride loop over a fixed grid
     const uint32_t qgrid =
         std::min<uint32_t>(grid, (uint32_t)sm_count() * (d->tuned_shade ? d->tuned_shade : CLV_SHADE_BLOCKS));
-    const uint32_t dgrid = scaled_grid(grid, d->tuned_shade, CLV_MINB_DIFFUSE);
     const uint32_t pgrid = scaled_grid(grid, d->tuned_shade, CLV_MINB_GUIDE_POST);
     if (prof) {
       std::memset(prof, 0, sizeof *prof);
@@ -1380,7 +1409,7 @@ static int render_wavefront(clv_device_scene* d, const clv_render_opts* o, doubl
       if (prof) cudaEventRecord(evs[4 * k + 1], s);
       if (prof) cudaEventRecord(evs[4 * k + 2], s);
       wf_shade_specular<false><<<qgrid, block, 0, s>>>(d->view, P, W, C, d->err, WfBatch{});
-      wf_shade_diffuse<false><<<dgrid, block, 0, s>>>(d->view, P, W, C, d->err, WfBatch{});
+      launch_shade_diffuse<false>(d->tuned_diffuse, grid, d->tuned_shade, s, d->view, P, W, C, d->err, WfBatch{});
       if (guide) {
         wf_guide_pre<false><<<qgrid, block, 0, s>>>(d->view, W, C, alpha, WfBatch{});
         if (alpha > 0.0f) gd_launch_queue(G, GQ, (uint32_t)q, s);
@@ -1552,7 +1581,6 @@ static int render_batch_part(clv_device_scene* const* ds, const clv_render_opts*
     const uint32_t grid = (uint32_t)((q + block - 1) / block);
     const uint32_t qgrid =
         std::min<uint32_t>(grid, (uint32_t)sm_count() * (d0->tuned_shade ? d0->tuned_shade : CLV_SHADE_BLOCKS));
-    const uint32_t dgrid = scaled_grid(grid, d0->tuned_shade, CLV_MINB_DIFFUSE);
     const uint32_t pgrid = scaled_grid(grid, d0->tuned_shade, CLV_MINB_GUIDE_POST);
     const ClvDeviceScene& S0 = d0->view;
     const WfParams P0 = params[0];
@@ -1580,7 +1608,7 @@ static int render_batch_part(clv_device_scene* const* ds, const clv_render_opts*
                                                                               only < 0 ? -1 : 2);
         }
         wf_shade_specular<true><<<qgrid, block, 0, s>>>(S0, P0, W, C, d0->err, B);
-        wf_shade_diffuse<true><<<dgrid, block, 0, s>>>(S0, P0, W, C, d0->err, B);
+        launch_shade_diffuse<true>(d0->tuned_diffuse, grid, d0->tuned_shade, s, S0, P0, W, C, d0->err, B);
         if (guide) {
           wf_guide_pre<true><<<qgrid, block, 0, s>>>(S0, W, C, alpha, B);
           if (alpha > 0.0f) gd_launch_queue(G, GQ, (uint32_t)q, s);
@@ -1893,7 +1921,6 @@ extern "C" int clv_render_device_noalloc(clv_device_scene* d, const clv_render_o
   const uint32_t grid = (uint32_t)((q + block - 1) / block);
   const uint32_t qgrid =
       std::min<uint32_t>(grid, (uint32_t)sm_count() * (d->tuned_shade ? d->tuned_shade : CLV_SHADE_BLOCKS));
-  const uint32_t dgrid = scaled_grid(grid, d->tuned_shade, CLV_MINB_DIFFUSE);
   // the array keeps the previous call's contents: counters are reset here and
   // wf_init rewrites every path slot
   noalloc_counters_init<<<1, 1, 0, st>>>(C, std::min<uint64_t>(q, P.total));
@@ -1913,7 +1940,7 @@ extern "C" int clv_render_device_noalloc(clv_device_scene* d, const clv_render_o
         default: wf_intersect<2, false, false, CLV_WT_ON><<<grid, block, 0, st>>>(d->view, W, C, d->err, nullptr, WfBatch{}, -1); break;
       }
       wf_shade_specular<false><<<qgrid, block, 0, st>>>(d->view, P, W, C, d->err, WfBatch{});
-      wf_shade_diffuse<false><<<dgrid, block, 0, st>>>(d->view, P, W, C, d->err, WfBatch{});
+      launch_shade_diffuse<false>(d->tuned_diffuse, grid, d->tuned_shade, st, d->view, P, W, C, d->err, WfBatch{});
       wf_finish<false><<<qgrid, block, 0, st>>>(d->view, P, W, C, film_dev, WfBatch{});
     }
     g_launches += 4 * batch;

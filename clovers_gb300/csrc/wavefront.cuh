@@ -163,11 +163,12 @@ __device__ __forceinline__ void warp_add_counts(unsigned long long* cnt, uint32_
 #ifndef CLV_MINB_SHADE
 #define CLV_MINB_SHADE 8  // resident blocks per SM asked of the shading kernels (64 registers)
 #endif
-#ifndef CLV_MINB_DIFFUSE
-// the same for wf_shade_diffuse, whose grid scales with it: 5 blocks (96 registers, 28 bytes of spills
-// against 232 at 64) measured best of 4..8 (enclosed box 682.7 against 675.5 Msamples/s at 8)
+// wf_shade_diffuse comes in two variants, its grid scaled to its resident blocks:
+// 5 blocks per SM (96 registers, 28 bytes of spills; the default: enclosed box
+// 686 against 679 Msamples/s) and 8 (64 registers, 232 bytes of spills; the
+// caustic prism 1380 against 1360).  clv_autotune picks one per scene.
 #define CLV_MINB_DIFFUSE 5
-#endif
+#define CLV_MINB_DIFFUSE_ALT 8
 #ifndef CLV_MINB_GUIDE
 #define CLV_MINB_GUIDE CLV_MINB_SHADE  // the same for wf_guide_pre
 #endif
@@ -514,8 +515,8 @@ __device__ __forceinline__ bool diffuse_slot(const ClvDeviceScene& S, const WfPa
   return wf_advance(P, W, C, i, p, rec.p, nd);
 }
 
-template <bool BATCH>
-__global__ void __launch_bounds__(128, CLV_MINB_DIFFUSE) wf_shade_diffuse(ClvDeviceScene S, WfParams P, WfState W, WfCounters* C,
+template <bool BATCH, int MINB>
+__global__ void __launch_bounds__(128, MINB) wf_shade_diffuse(ClvDeviceScene S, WfParams P, WfState W, WfCounters* C,
                                                         uint32_t* err, WfBatch B) {
   const uint32_t n = C->queue[WF_Q_DIFF];
   const uint32_t stride = gridDim.x * blockDim.x;
@@ -721,6 +722,26 @@ __device__ __forceinline__ void film_deposit(const ClvDeviceScene& S, double* fi
 
 // Background on a miss (trace.rs:42-48) or emission of a light (trace.rs:51-58), then the film deposit.
 __device__ __forceinline__ void finish_slot(const ClvDeviceScene& S, const WfState& W, double* film, uint32_t i) {
+  {  // a path that ends on a surface that does not emit adds nothing: skip its hit record
+    const uint32_t ref = __float_as_uint(W.hit[i].y);
+    if (ref != CLV_REF_EMPTY) {
+      const uint32_t kind = CLV_REF_KIND(ref), idx = CLV_REF_INDEX(ref);
+      uint32_t mat;
+      if (kind == CLV_REF_TRI) mat = S.tri_mat[idx];
+      else if (kind == CLV_REF_QUAD) mat = S.quad_mat[idx];
+      else if (kind == CLV_REF_SPHERE) mat = S.sphere_mat[idx];
+      else mat = __float_as_uint(W.full[3 * i + 2].y);
+      const uint32_t k = S.materials[mat].kind;
+      if (k != CLV_MAT_DIFFUSELIGHT && k != CLV_MAT_CONELIGHT) {
+        if (W.gslot) {  // the path's recorded vertices carry zero radiance
+          const uint4 gs = W.gslot[i];
+          if (gs.x != 0xFFFFFFFFu) reinterpret_cast<float*>(W.grec + GD_REC_F4 * (size_t)gs.x + 2)[3] = 0.0f;
+          if (gs.y != 0xFFFFFFFFu) reinterpret_cast<float*>(W.grec + GD_REC_F4 * (size_t)gs.y + 2)[3] = 0.0f;
+        }
+        return;
+      }
+    }
+  }
   const float4 a = W.o_time[i], b = W.d_lambda[i];
   const Ray ray{mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, __float_as_int(b.w)};
   const float4 bv = W.beta[i];

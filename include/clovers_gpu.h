@@ -170,26 +170,30 @@ int clv_resolve_srgb(const float* xyz, uint32_t width, uint32_t height, uint8_t*
  * {8, 16, 32} blocks per SM, and, for primitive-level scenes (traversal level
  * 0, BVH of at most 64 levels), the intersect's queue appends per block (one
  * atomic per class and block, behind two block barriers) or per warp (no
- * barrier: better where traversal lengths vary widely within a block), and
- * keeps the fastest in the scene: later wavefront renders of this scene with
+ * barrier: better where traversal lengths vary widely within a block); then,
+ * at the fastest of those, the diffuse shading kernel at 8 instead of 5
+ * resident blocks per SM (64 instead of 96 registers).  It keeps the fastest
+ * in the scene: later wavefront renders of this scene with
  * opts->path_slots = 0 use it.  results (optional) receives up to max_results
- * timings, n_results their count (30 for primitive-level scenes, else 15).
+ * timings, n_results their count (31 for primitive-level scenes, else 16).
  * Allocates a film and the largest path state it tries. */
 typedef struct clv_tune_result {
   uint32_t path_slots;
   uint32_t shade_blocks_per_sm;
-  uint32_t warp_appends;  /* 1: the intersect appends its queues per warp, 0: per block */
+  uint32_t warp_appends;          /* 1: the intersect appends its queues per warp, 0: per block */
+  uint32_t diffuse_blocks_per_sm; /* resident blocks per SM of the diffuse shading kernel (5 or 8) */
   float ms;
 } clv_tune_result;
 int clv_autotune(clv_device_scene* dscene, const clv_render_opts* opts, clv_tune_result* results,
                  uint32_t max_results, uint32_t* n_results, void* stream);
 
 /* Sets the wavefront shape clv_autotune would keep (0 = the built-in default
- * for path_slots and shade_blocks_per_sm), e.g. to reuse a shape tuned in an
- * earlier run.  warp_appends = 1 is valid for primitive-level scenes only
- * (clv_scene_info.traversal_level 0, BVH of at most 64 levels). */
+ * for path_slots, shade_blocks_per_sm and diffuse_blocks_per_sm), e.g. to
+ * reuse a shape tuned in an earlier run.  warp_appends = 1 is valid for
+ * primitive-level scenes only (clv_scene_info.traversal_level 0, BVH of at
+ * most 64 levels); diffuse_blocks_per_sm takes 0, 5 or 8. */
 int clv_device_scene_set_shape(clv_device_scene* dscene, uint32_t path_slots, uint32_t shade_blocks_per_sm,
-                               uint32_t warp_appends);
+                               uint32_t warp_appends, uint32_t diffuse_blocks_per_sm);
 
 /* ---- ray casts --------------------------------------------------------- */
 

@@ -128,31 +128,37 @@ def test_render_rejects_mismatched_size(box_scene_path):
         cg.draw(cg.GlobalOptions(), cg.RenderOptions(width=32, height=16, samples=1), d)
 
 
-@pytest.mark.parametrize("which,candidates", [("box", 15), ("spheres", 30)])
+@pytest.mark.parametrize("which,candidates", [("box", 16), ("spheres", 31)])
 def test_autotune_keeps_the_image(request, which, candidates):
-    """clv_autotune tries paths in flight x shading grids, and for primitive-level
-    scenes (the random spheres) also per-warp intersect appends; whatever it picks,
-    the image is the same."""
+    """clv_autotune tries paths in flight x shading grids, for primitive-level
+    scenes (the random spheres) also per-warp intersect appends, and at the best
+    of those the other diffuse-shading variant; whatever it picks, the image is
+    the same."""
     path = request.getfixturevalue(which + "_scene_path")
     w, h = (128, 128) if which == "box" else (160, 90)
     d = cg.Scene.from_json(path, w, h).upload()
     opts = cg.RenderOptions(width=w, height=h, samples=8, max_depth=8, seed=3)
     before = cg.draw(cg.GlobalOptions(quiet=True), opts, d)
     res = d.autotune(cg.RenderOptions(width=w, height=h, samples=4, max_depth=8, seed=1))
-    assert len(res) == candidates and all(ms > 0 for _, _, _, ms in res)
-    assert sorted(set(r[2] for r in res)) == ([0] if candidates == 15 else [0, 1])
-    best = min(res, key=lambda r: r[3])
+    assert len(res) == candidates and all(r[4] > 0 for r in res)
+    appends = [0] if candidates == 16 else [0, 1]
+    assert sorted(set(r[2] for r in res)) == appends
+    assert [r[3] for r in res] == [5] * (candidates - 1) + [8]
+    best = min(res, key=lambda r: r[4])
     print("autotune: best %s of %d candidates" % (best, len(res)))
     after = cg.draw(cg.GlobalOptions(quiet=True), opts, d)
     # the same random streams give the same paths; only the f64 deposit order may move the last bits
     assert np.allclose(before, after, rtol=1e-5, atol=1e-9)
-    for appends in ([0] if candidates == 15 else [0, 1]):  # each queue-append form renders the same image
-        d.set_shape(0, 0, appends)
-        img = cg.draw(cg.GlobalOptions(quiet=True), opts, d)
-        assert np.allclose(before, img, rtol=1e-5, atol=1e-9), appends
-    if candidates == 15:
+    for ap in appends:  # each queue-append form and diffuse variant renders the same image
+        for db in (5, 8):
+            d.set_shape(0, 0, ap, db)
+            img = cg.draw(cg.GlobalOptions(quiet=True), opts, d)
+            assert np.allclose(before, img, rtol=1e-5, atol=1e-9), (ap, db)
+    if candidates == 16:
         with pytest.raises(cg.ClvError):
             d.set_shape(0, 0, 1)  # per-warp appends exist for primitive-level scenes only
+    with pytest.raises(cg.ClvError):
+        d.set_shape(0, 0, 0, 6)  # the diffuse kernel exists at 5 and 8 blocks per SM
     assert d.status() == 0
 
 
