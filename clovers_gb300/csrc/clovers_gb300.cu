@@ -680,9 +680,30 @@ struct clv_device_scene {
     if (!cap_stream) cap_stream = pool::stream();
     return cap_stream;
   }
+  // A second stream and a fork / join event pair: wf_shade_specular runs beside
+  // the diffuse and guided kernels of the same bounce (their queues hold
+  // disjoint slots), so that each fills the other's tail.  False if any of
+  // them cannot be created (the bounce then runs in one stream).
+  cudaStream_t side_stream = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  bool fork_streams() {
+    if (!side_stream) side_stream = pool::stream();
+    if (!ev_fork && cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming) != cudaSuccess) {
+      cudaGetLastError();
+      ev_fork = nullptr;
+    }
+    if (!ev_join && cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming) != cudaSuccess) {
+      cudaGetLastError();
+      ev_join = nullptr;
+    }
+    return side_stream && ev_fork && ev_join;
+  }
   size_t counters_bytes = 0;
   ~clv_device_scene() {
     pool::release_stream(cap_stream);
+    pool::release_stream(side_stream);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
     pool::release(ray_sort, ray_sort_bytes);
     pool::release(spill, spill_bytes);
     if (!owned.empty()) pool::release(owned[0], owned_bytes);  // scene arrays, error word and ray counter
@@ -1366,6 +1387,7 @@ static int render_wavefront(clv_device_scene* d, const clv_render_opts* o, doubl
       prof->ms_init = ms;
     }
     // one bounce: counters, closest hits, the shading passes, path ends
+    const bool fork = d->fork_streams();
     auto bounce = [&](cudaStream_t s, int k) {
       cudaMemsetAsync(&d->wf_counters->live, 0, 5 * sizeof(unsigned int), s);  // live + 4 queue lengths
       if (prof) cudaEventRecord(evs[4 * k], s);
@@ -1408,13 +1430,19 @@ static int render_wavefront(clv_device_scene* d, const clv_render_opts* o, doubl
 #undef CLV_ISECT_W
       if (prof) cudaEventRecord(evs[4 * k + 1], s);
       if (prof) cudaEventRecord(evs[4 * k + 2], s);
-      wf_shade_specular<false><<<qgrid, block, 0, s>>>(d->view, P, W, C, d->err, WfBatch{});
+      if (fork) {
+        cudaEventRecord(d->ev_fork, s);
+        cudaStreamWaitEvent(d->side_stream, d->ev_fork, 0);
+      }
+      wf_shade_specular<false><<<qgrid, block, 0, fork ? d->side_stream : s>>>(d->view, P, W, C, d->err, WfBatch{});
+      if (fork) cudaEventRecord(d->ev_join, d->side_stream);
       launch_shade_diffuse<false>(d->tuned_diffuse, grid, d->tuned_shade, s, d->view, P, W, C, d->err, WfBatch{});
       if (guide) {
         wf_guide_pre<false><<<qgrid, block, 0, s>>>(d->view, W, C, alpha, WfBatch{});
         if (alpha > 0.0f) gd_launch_queue(G, GQ, (uint32_t)q, s);
         wf_guide_post<false><<<pgrid, block, 0, s>>>(d->view, P, W, C, d->err, G, WfBatch{});
       }
+      if (fork) cudaStreamWaitEvent(s, d->ev_join, 0);
       wf_finish<false><<<qgrid, block, 0, s>>>(d->view, P, W, C, film, WfBatch{});
       if (prof) cudaEventRecord(evs[4 * k + 3], s);
     };
@@ -1589,6 +1617,7 @@ static int render_batch_part(clv_device_scene* const* ds, const clv_render_opts*
     uint32_t max_depth = 0;
     for (uint32_t k = 0; k < n; ++k) max_depth = std::max(max_depth, opts[k].max_depth);
     const int batch = 8;
+    const bool fork = d0->fork_streams();
     auto bounces = [&](cudaStream_t s) {
       for (int k = 0; k < batch; ++k) {
         cudaMemsetAsync(&C->live, 0, 5 * sizeof(unsigned int), s);
@@ -1607,13 +1636,19 @@ static int render_batch_part(clv_device_scene* const* ds, const clv_render_opts*
             wf_intersect<2, false, true, CLV_WT_SCENE><<<grid, block, 0, s>>>(S0, W, C, d0->err, nullptr, B,
                                                                               only < 0 ? -1 : 2);
         }
-        wf_shade_specular<true><<<qgrid, block, 0, s>>>(S0, P0, W, C, d0->err, B);
+        if (fork) {  // specular shading beside the diffuse and guided kernels
+          cudaEventRecord(d0->ev_fork, s);
+          cudaStreamWaitEvent(d0->side_stream, d0->ev_fork, 0);
+        }
+        wf_shade_specular<true><<<qgrid, block, 0, fork ? d0->side_stream : s>>>(S0, P0, W, C, d0->err, B);
+        if (fork) cudaEventRecord(d0->ev_join, d0->side_stream);
         launch_shade_diffuse<true>(d0->tuned_diffuse, grid, d0->tuned_shade, s, S0, P0, W, C, d0->err, B);
         if (guide) {
           wf_guide_pre<true><<<qgrid, block, 0, s>>>(S0, W, C, alpha, B);
           if (alpha > 0.0f) gd_launch_queue(G, GQ, (uint32_t)q, s);
           wf_guide_post<true><<<pgrid, block, 0, s>>>(S0, P0, W, C, d0->err, G, B);
         }
+        if (fork) cudaStreamWaitEvent(s, d0->ev_join, 0);
         wf_finish<true><<<qgrid, block, 0, s>>>(S0, P0, W, C, nullptr, B);
       }
     };
