@@ -1623,18 +1623,31 @@ static int render_batch_part(clv_device_scene* const* ds, const clv_render_opts*
         cudaMemsetAsync(&C->live, 0, 5 * sizeof(unsigned int), s);
         // one intersect launch per traversal level present, each over its own scenes' slots
         // (a batch with a tree deeper than CLV_STACK levels: one generic launch with a spilling stack)
+        // (several levels: the lowest level's launch runs on the second stream,
+        // beside the others; their slots are disjoint)
         const int only = nlevels > 1 ? 0 : -1;
         if (spill_entries) {
           wf_intersect<2, false, true, CLV_WT_SCENE, true><<<grid, block, 0, s>>>(S0, W, C, d0->err, nullptr, B, -1);
         } else {
+          const bool split = fork && nlevels > 1;
+          if (split) {
+            cudaEventRecord(d0->ev_fork, s);
+            cudaStreamWaitEvent(d0->side_stream, d0->ev_fork, 0);
+          }
+          const uint32_t lowest = levels & (0u - levels);
+          auto sl = [&](uint32_t bit) { return split && bit == lowest ? d0->side_stream : s; };
           if (levels & 1u)
-            wf_intersect<0, false, true, CLV_WT_SCENE><<<grid, block, 0, s>>>(S0, W, C, d0->err, nullptr, B, only);
+            wf_intersect<0, false, true, CLV_WT_SCENE><<<grid, block, 0, sl(1u)>>>(S0, W, C, d0->err, nullptr, B, only);
           if (levels & 2u)
-            wf_intersect<1, false, true, CLV_WT_SCENE><<<grid, block, 0, s>>>(S0, W, C, d0->err, nullptr, B,
-                                                                              only < 0 ? -1 : 1);
+            wf_intersect<1, false, true, CLV_WT_SCENE><<<grid, block, 0, sl(2u)>>>(S0, W, C, d0->err, nullptr, B,
+                                                                                  only < 0 ? -1 : 1);
           if (levels & 4u)
-            wf_intersect<2, false, true, CLV_WT_SCENE><<<grid, block, 0, s>>>(S0, W, C, d0->err, nullptr, B,
-                                                                              only < 0 ? -1 : 2);
+            wf_intersect<2, false, true, CLV_WT_SCENE><<<grid, block, 0, sl(4u)>>>(S0, W, C, d0->err, nullptr, B,
+                                                                                  only < 0 ? -1 : 2);
+          if (split) {
+            cudaEventRecord(d0->ev_join, d0->side_stream);
+            cudaStreamWaitEvent(s, d0->ev_join, 0);
+          }
         }
         if (fork) {  // specular shading beside the diffuse and guided kernels
           cudaEventRecord(d0->ev_fork, s);
