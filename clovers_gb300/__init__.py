@@ -371,6 +371,24 @@ def render(global_options: GlobalOptions, render_options: RenderOptions):
     from .imageio import format_duration, write_png, write_exr
     import time
 
+    o = render_options
+    if not global_options.quiet:  # render.rs:112-125
+        print("clovers \U0001F340 path tracing renderer")
+        print()
+        print("%dx%d resolution" % (o.width, o.height))
+        if o.mode == "normal-map":
+            print("rendering a normalmap")
+        else:
+            print("%d samples per pixel" % o.samples)
+            print("using the %s sampler" % o.sampler)
+            print("%d max bounce depth" % o.max_depth)
+        print()
+    if o.sampler == "blue":
+        if o.samples not in (1, 2, 4, 8, 16, 32, 64, 128, 256):  # render.rs:127-129
+            raise ClvError(_lib.CLV_E_INVALID, "the blue sampler only supports the following sample-per-pixel "
+                                               "counts: [1, 2, 4, 8, 16, 32, 64, 128, 256]")
+        raise ClvError(_lib.CLV_E_INVALID, "the blue-noise sampler is not available in this build (its "
+                                           "precomputed tables are not part of it); use --sampler random")
     if not render_options.input.endswith(".json"):
         raise ClvError(_lib.CLV_E_INVALID, "Unknown file type")
     scene = initialize(render_options.input, render_options.bvh, render_options.width, render_options.height)
@@ -391,6 +409,5 @@ def render(global_options: GlobalOptions, render_options: RenderOptions):
         else:
             raise ValueError("unknown format %r" % fmt)
         written.append(target)
-        if not global_options.quiet:
-            print("Image saved to: %s" % target)
+        print("Image saved to: %s" % target)  # printed in quiet mode too (render.rs:179)
     return written

@@ -1889,24 +1889,15 @@ static constexpr size_t kNoallocHeader = 256;  // WfCounters, padded
 static constexpr size_t kNoallocBytes = kNoallocHeader + (size_t)CLV_NOALLOC_SLOTS * clv_device_scene::kWfSlotBytes;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
 
-// Device addresses of g_noalloc_scratch, looked up once per device.
-static std::mutex g_noalloc_mutex;
-static void* g_noalloc_ptr[256];
-
+// Device address of g_noalloc_scratch in the current context, looked up on
+// every call (cheap, allocates nothing, and stays right if the context is
+// torn down and the module loaded again at another address).
 static int noalloc_scratch_address(void** out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return fail(CLV_E_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
-  if (dev < 0 || dev >= 256) return fail(CLV_E_INVALID, "device ordinal out of range");
-  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-  if (!g_noalloc_ptr[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p)
-      return fail(CLV_E_CUDA, std::string("cudaGetSymbolAddress(g_noalloc_scratch): ") + cudaGetErrorString(e));
-    g_noalloc_ptr[dev] = p;
-  }
-  *out = g_noalloc_ptr[dev];
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || !p)
+    return fail(CLV_E_CUDA, std::string("cudaGetSymbolAddress(g_noalloc_scratch): ") + cudaGetErrorString(e));
+  *out = p;
   return CLV_OK;
 }
 

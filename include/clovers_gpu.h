@@ -146,12 +146,14 @@ int clv_render_batch(clv_device_scene* const* dscenes, const clv_render_opts* op
  * calls no cudaMalloc/cudaFree: path state, queues and counters live in one
  * static device array of 65536 path slots (about 10 MB, reserved on every GPU
  * that loads the library until the process exits).  opts->path_slots above
- * 65536 is rejected with CLV_E_INVALID; 0 means 65536.  The first call on a
- * device looks up the array's address on that device (cudaGetSymbolAddress),
- * so make that first call before any stream capture.  Every call shares the
- * array and leaves its contents behind: calls that overlap on the GPU (other
- * streams, other threads) race and must be serialised by the caller.  Returns
- * once the film is complete, like clv_render_device. */
+ * 65536 is rejected with CLV_E_INVALID; 0 means 65536.  The scene's tuned
+ * wavefront shape applies (its path slots capped at 65536); scenes whose BVH
+ * is deeper than 64 levels are refused (their traversal stacks would need
+ * device memory).  Every call shares the array and leaves its contents
+ * behind: calls that overlap on the GPU (other streams, other threads) race
+ * and must be serialised by the caller.  The call synchronises its stream
+ * (it polls the live-path count), so it cannot be captured into a CUDA
+ * graph; it returns once the film is complete, like clv_render_device. */
 int clv_render_device_noalloc(clv_device_scene* dscene, const clv_render_opts* opts, double* film_dev, void* stream);
 
 /* Film resolve (clovers-cli/src/write.rs:39-44): mean = film / spp (f64) ->

@@ -58,3 +58,25 @@ def test_module_entry_point(tmp_path):
     p = subprocess.run([sys.executable, "-m", "clovers_gb300", "validate", good], cwd=ROOT,
                        capture_output=True, text=True, timeout=120)
     assert p.returncode == 0 and "successfully validated" in p.stdout
+
+
+def test_render_banner_and_quiet(capsys):
+    """render.rs:112-125: the banner unless quiet (checked before any GPU work: the
+    scene file type is refused right after it)."""
+    assert cli.main(["render", "-i", "scene.txt", "-w", "32", "-h", "16", "-s", "4", "-d", "8"]) == 1
+    out = capsys.readouterr().out
+    assert out.splitlines()[:6] == ["clovers \U0001F340 path tracing renderer", "", "32x16 resolution",
+                                    "4 samples per pixel", "using the random sampler", "8 max bounce depth"]
+    assert cli.main(["render", "-i", "scene.txt", "-m", "normal-map"]) == 1
+    assert "rendering a normalmap" in capsys.readouterr().out
+    assert cli.main(["-q", "render", "-i", "scene.txt"]) == 1
+    assert capsys.readouterr().out == ""
+
+
+def test_blue_sampler_is_refused_clearly(capsys):
+    """--sampler blue: the reference's spp check (render.rs:127-129), then a clear
+    refusal (the blue-noise tables are not part of this build)."""
+    assert cli.main(["-q", "render", "-i", "a.json", "--sampler", "blue", "-s", "3"]) == 1
+    assert "only supports the following sample-per-pixel counts" in capsys.readouterr().err
+    assert cli.main(["-q", "render", "-i", "a.json", "--sampler", "blue", "-s", "4"]) == 1
+    assert "blue-noise sampler is not available" in capsys.readouterr().err
