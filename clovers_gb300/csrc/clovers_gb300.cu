@@ -1387,9 +1387,7 @@ static int render_wavefront(clv_device_scene* d, const clv_render_opts* o, doubl
       prof->ms_init = ms;
     }
     // one bounce: counters, closest hits, the shading passes, path ends
-    // (guided renders keep one stream: no gain per sample measured there, and
-    // the guided times to relMSE 1e-3 scattered higher in the runs with it)
-    const bool fork = !guide && d->fork_streams();
+    const bool fork = d->fork_streams();
     auto bounce = [&](cudaStream_t s, int k) {
       cudaMemsetAsync(&d->wf_counters->live, 0, 5 * sizeof(unsigned int), s);  // live + 4 queue lengths
       if (prof) cudaEventRecord(evs[4 * k], s);
@@ -1619,7 +1617,7 @@ static int render_batch_part(clv_device_scene* const* ds, const clv_render_opts*
     uint32_t max_depth = 0;
     for (uint32_t k = 0; k < n; ++k) max_depth = std::max(max_depth, opts[k].max_depth);
     const int batch = 8;
-    const bool fork = !guide && d0->fork_streams();  // as in render_wavefront
+    const bool fork = d0->fork_streams();
     auto bounces = [&](cudaStream_t s) {
       for (int k = 0; k < batch; ++k) {
         cudaMemsetAsync(&C->live, 0, 5 * sizeof(unsigned int), s);
