@@ -43,6 +43,9 @@ struct WfState {
 };
 
 #define WF_Q_FINISH 0  // misses, emitters and paths ended in the shade kernels
+// meta.w flag: the path ended in a shade kernel on a surface that emits nothing
+// (depth limit or no scatter), so wf_finish has nothing to add for it
+#define WF_ENDED_DARK 2u
 #define WF_Q_SPEC 1    // metal, dielectric, dispersive
 #define WF_Q_DIFF 2    // lambertian, isotropic (isotropic only in guided renders)
 #define WF_Q_GUIDE 3   // lambertian in guided renders
@@ -394,7 +397,7 @@ __device__ __forceinline__ bool wf_advance(const WfParams& P, const WfState& W, 
                                            V origin, V nd) {
   const uint32_t depth = p.meta.y + 1;
   if (depth > P.max_depth) {  // trace at depth > max_depth returns 0
-    W.meta[i].z = p.rng.counter;
+    W.meta[i] = make_uint4(p.meta.x, p.meta.y, p.rng.counter, p.meta.w | WF_ENDED_DARK);
     return false;
   }
   W.o_time[i] = make_float4(origin.x, origin.y, origin.z, p.ray.time);
@@ -505,7 +508,7 @@ __device__ __forceinline__ bool diffuse_slot(const ClvDeviceScene& S, const WfPa
     spdf = 1.0f / (4.0f * CLV_PI);
   }
   if (!scatter) {
-    W.meta[i].z = p.rng.counter;
+    W.meta[i] = make_uint4(p.meta.x, p.meta.y, p.rng.counter, p.meta.w | WF_ENDED_DARK);
     return false;
   }
   float atten[4];
@@ -655,6 +658,7 @@ __device__ __forceinline__ bool guide_post_slot(const ClvDeviceScene& S, const W
     }
   }
   if (cs < 0.0f) {  // Lambertian::scattering_pdf is None below the surface
+    W.meta[i].w = p.meta.w | WF_ENDED_DARK;
     return false;
   }
   const float spdf = cs / CLV_PI;
@@ -722,25 +726,13 @@ __device__ __forceinline__ void film_deposit(const ClvDeviceScene& S, double* fi
 
 // Background on a miss (trace.rs:42-48) or emission of a light (trace.rs:51-58), then the film deposit.
 __device__ __forceinline__ void finish_slot(const ClvDeviceScene& S, const WfState& W, double* film, uint32_t i) {
-  {  // a path that ends on a surface that does not emit adds nothing: skip its hit record
-    const uint32_t ref = __float_as_uint(W.hit[i].y);
-    if (ref != CLV_REF_EMPTY) {
-      const uint32_t kind = CLV_REF_KIND(ref), idx = CLV_REF_INDEX(ref);
-      uint32_t mat;
-      if (kind == CLV_REF_TRI) mat = S.tri_mat[idx];
-      else if (kind == CLV_REF_QUAD) mat = S.quad_mat[idx];
-      else if (kind == CLV_REF_SPHERE) mat = S.sphere_mat[idx];
-      else mat = __float_as_uint(W.full[3 * i + 2].y);
-      const uint32_t k = S.materials[mat].kind;
-      if (k != CLV_MAT_DIFFUSELIGHT && k != CLV_MAT_CONELIGHT) {
-        if (W.gslot) {  // the path's recorded vertices carry zero radiance
-          const uint4 gs = W.gslot[i];
-          if (gs.x != 0xFFFFFFFFu) reinterpret_cast<float*>(W.grec + GD_REC_F4 * (size_t)gs.x + 2)[3] = 0.0f;
-          if (gs.y != 0xFFFFFFFFu) reinterpret_cast<float*>(W.grec + GD_REC_F4 * (size_t)gs.y + 2)[3] = 0.0f;
-        }
-        return;
-      }
+  if (W.meta[i].w & WF_ENDED_DARK) {  // ended on a surface that emits nothing: skip its hit record
+    if (W.gslot) {  // the path's recorded vertices carry zero radiance
+      const uint4 gs = W.gslot[i];
+      if (gs.x != 0xFFFFFFFFu) reinterpret_cast<float*>(W.grec + GD_REC_F4 * (size_t)gs.x + 2)[3] = 0.0f;
+      if (gs.y != 0xFFFFFFFFu) reinterpret_cast<float*>(W.grec + GD_REC_F4 * (size_t)gs.y + 2)[3] = 0.0f;
     }
+    return;
   }
   const float4 a = W.o_time[i], b = W.d_lambda[i];
   const Ray ray{mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, __float_as_int(b.w)};
