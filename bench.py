@@ -268,6 +268,10 @@ def run_batch(args):
     n = len(dev)
     handles = (ctypes.c_void_p * n)(*[d.handle.value for d in dev])
     optarr = (_lib.RenderOptsC * n)(*opts)
+    batch_opts = (_lib.RenderOptsC * n)(*opts)
+    batch_opts[0].path_slots = args.batch_slots  # the batch's paths in flight (0: clv_render_batch's default)
+    for k in range(n):
+        optarr[k].path_slots = args.single_slots  # the one-by-one renders' paths in flight (0: their defaults)
     ptrs = (ctypes.c_void_p * n)(*[f.data_ptr() for f in films])
 
     def timed(fn):
@@ -280,7 +284,7 @@ def run_batch(args):
         return e0.elapsed_time(e1)
 
     def batched():
-        _lib.check(L.clv_render_batch(handles, optarr, ptrs, n, sp))
+        _lib.check(L.clv_render_batch(handles, batch_opts, ptrs, n, sp))
 
     def one_by_one():
         for k in range(n):
@@ -295,7 +299,9 @@ def run_batch(args):
             "higher_is_better": True, "dtype": "f32", "data": "synthetic (seeds 100..%d)" % (99 + n),
             "config": {"workload": "%d scenes in one wavefront: displaced geodesic spheres 1k-200k triangles, "
                                    "0-3 smoke boxes, 128^2-1024^2, 16-512 spp, depth %d" % (n, DEPTH),
-                       "samples_per_step": samples, "triangles": tris, "scene_load_s": round(load_s, 2)},
+                       "samples_per_step": samples, "triangles": tris, "scene_load_s": round(load_s, 2),
+                       "batch_path_slots": args.batch_slots or "default", "single_path_slots":
+                       args.single_slots or "default"},
             "one_by_one": {"ms": round(t_seq, 3), "value": round(samples / (t_seq / 1e3) / 1e6, 3)}}
     line["small_scenes"] = batch_small(args, L, sp, tmp, n, timed)
     conv = None if args.no_convergence else batch_convergence(args, dev, tmp)
@@ -740,6 +746,10 @@ def main():
     ap.add_argument("--max-spp", type=int, default=8192, help="cap of the progressive relMSE measurement")
     ap.add_argument("--batch", action="store_true", help="measure the batched multi-scene workload")
     ap.add_argument("--batch-scenes", type=int, default=64)
+    ap.add_argument("--batch-slots", type=int, default=0,
+                    help="paths in flight of the batched render (0: clv_render_batch's default)")
+    ap.add_argument("--single-slots", type=int, default=0,
+                    help="paths in flight of each one-by-one render (0: clv_render_device's default)")
     ap.add_argument("--no-convergence", action="store_true",
                     help="with --batch: skip the per-scene time to relMSE 1e-3 (launch lists of the timed renders)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline legs")
