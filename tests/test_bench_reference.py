@@ -24,3 +24,16 @@ def test_reference_arm_line():
     assert (e2e["value"], e2e["unit"], e2e["h2d_bytes_per_step"], e2e["d2h_bytes_per_step"]) == (
         line["value"], line["unit"], 0, 0)
     assert "enclosed box 512x512, 256 spp" in line["config"]["workload"]
+
+
+def test_reference_arm_under_torchrun_prints_once():
+    """Launched like the multi-GPU arm (torchrun, 2 ranks): rank 0 alone runs and
+    prints; the other rank exits 0 without work."""
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
+           "--master-addr", "127.0.0.1", "--master-port", "29731", "bench.py", "--impl", "reference", "--gpus", "2",
+           "--steps", "1", "--warmup", "3", "--cpu-spp", "1"]
+    p = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=300)
+    assert p.returncode == 0, p.stderr[-2000:]
+    lines = [ln for ln in p.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    assert json.loads(lines[0])["impl"] == "reference"
