@@ -753,7 +753,7 @@ __device__ __forceinline__ void finish_slot(const ClvDeviceScene& S, const WfSta
 #pragma unroll
       for (int j = 0; j < 4; ++j) L[j] += beta[j] * mat_emit(S, m, ray, waves[j], rec);
     }
-    // paths that ended in the shade kernels (depth limit, no scatter) add nothing here
+    // (paths that the shade kernels ended never get here: WF_ENDED_DARK above)
   }
   film_deposit(S, film, W.meta[i].x, ray.lambda, L);
   if (W.gslot) {  // training weights: hero power of the path / hero throughput before each recorded vertex
