@@ -2,16 +2,23 @@
 // unrolled over bounces and split into small kernels over structure-of-arrays
 // path state in HBM.
 //
-//   wf_init       fills every path slot with the camera ray of one sample
-//                 (work item w -> sample w / npix, pixel w % npix)
-//   wf_intersect  closest hit of each live path (BVHNode::hit, bit-exact)
-//   wf_shade      one bounce: emission, scatter, MixturePDF light sampling,
-//                 throughput update; a finished path deposits its spectral
-//                 powers in the f64 film (draw_cpu.rs:131-142) and its slot
-//                 takes the next work item (warp-aggregated atomic fetch), so
-//                 slots stay busy without compaction.
+//   wf_init            fills every path slot with the camera ray of one sample
+//                      (work item w -> sample w / npix, pixel w % npix)
+//   wf_intersect       closest hit of each live path (BVHNode::hit, bit-exact);
+//                      appends the slot to the queue of its material class
+//   wf_shade_specular  metal / dielectric / dispersive bounce
+//   wf_shade_diffuse   Lambertian / isotropic bounce with MixturePDF light sampling
+//   wf_guide_pre/post  guided Lambertian bounce around the guide network (guide.cu)
+//   wf_finish          emission or background of paths that ended, deposit of
+//                      their spectral powers in the f64 film (draw_cpu.rs:131-142);
+//                      each freed slot takes the next work item (one atomic per
+//                      block), so slots stay busy without compaction.
 //
-// The host runs [intersect, shade] in CUDA-graph batches until no slot is live.
+// The host replays [intersect, shade, finish] bounces in CUDA-graph batches of
+// eight until no slot is live; the two shade kernels work on disjoint queues,
+// so the specular one runs on a second stream beside the diffuse one.  The
+// *_slot functions hold the per-path arithmetic; the same kernels render a
+// single scene (BATCH false) or many (BATCH true: scene tables in constant memory).
 #pragma once
 
 #include "clv_device.cuh"
