@@ -776,7 +776,7 @@ __device__ __forceinline__ void finish_slot(const ClvDeviceScene& S, const WfSta
   }
 }
 
-// Ends paths, then each slot takes the next work item (one atomic per warp).
+// Ends paths, then each freed slot takes the next work item (one atomic per block and round).
 template <bool BATCH>
 __global__ void __launch_bounds__(128, CLV_MINB_SHADE) wf_finish(ClvDeviceScene S, WfParams P, WfState W, WfCounters* C,
                                                  double* __restrict__ film, WfBatch B) {
